@@ -1,0 +1,181 @@
+"""ctypes binding of the CPU FP64 oracle -- TEST INFRASTRUCTURE ONLY.
+
+Imported only by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg
+of ``bench.py``, where it is the checker (or the timed CPU baseline), never
+the thing measured as the product. Parity with tblite is unpinned: see
+``qcx_oracle.h``.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqcxoracle.so")
+
+
+def build(force=False):
+    src = os.path.join(HERE, "qcx_oracle.c")
+    deps = [src, os.path.join(HERE, "qcx_oracle.h"),
+            os.path.join(HERE, "..", "qcxms_gb300", "csrc", "qcx_params.h"),
+            os.path.join(HERE, "..", "qcxms_gb300", "csrc", "qcx_consts.h")]
+    if not force and os.path.exists(LIB_PATH) and \
+            os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(d) for d in deps):
+        return LIB_PATH
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-o", LIB_PATH, src, "-lm"]
+    subprocess.check_call(cmd)
+    return LIB_PATH
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("econv", ctypes.c_double),
+                ("pconv", ctypes.c_double), ("broyden_alpha", ctypes.c_double)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("e_band", "e_ies", "e_3", "e_aes", "e_axc", "e_disp", "e_atm", "e_rep", "e_ts", "e_total")] + \
+               [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("nao", ctypes.c_int),
+                ("nsh", ctypes.c_int), ("nel", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.qcxo_egrad.restype = ctypes.c_int
+        _lib.qcxo_nao.restype = ctypes.c_int
+        _lib.qcxo_nsh.restype = ctypes.c_int
+        _lib.qcxo_gnorm.restype = ctypes.c_double
+        _lib.qcxo_getspin.restype = ctypes.c_int
+        _lib.qcxo_checkqc.restype = ctypes.c_int
+        _lib.qcxo_md_batch.restype = ctypes.c_int
+    return _lib
+
+
+def _p(a, t=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def default_opts(**kw):
+    o = Opts()
+    lib().qcxo_default_opts(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def nao(Z):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    return lib().qcxo_nao(len(Z), _p(Z, ctypes.c_int))
+
+
+def nsh(Z):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    return lib().qcxo_nsh(len(Z), _p(Z, ctypes.c_int))
+
+
+def egrad(Z, xyz, charge=0, kT=300.0 * 3.166808578545117e-06, opts=None):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    nat = len(Z)
+    e = ctypes.c_double()
+    g = np.zeros((nat, 3))
+    q = np.zeros(nat)
+    info = Info()
+    o = opts if opts is not None else default_opts()
+    rc = lib().qcxo_egrad(nat, _p(Z, ctypes.c_int), _p(xyz), ctypes.c_double(charge), ctypes.c_double(kT),
+                          ctypes.byref(o), ctypes.byref(e), _p(g), _p(q), ctypes.byref(info))
+    return rc, e.value, g, q, info.as_dict()
+
+
+def integrals(Z, xyz):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    n = nao(Z)
+    S = np.zeros((n, n)); H0 = np.zeros((n, n))
+    Dm = np.zeros((3, n, n)); Qm = np.zeros((6, n, n))
+    cn = np.zeros(len(Z)); cnd = np.zeros(len(Z))
+    rc = lib().qcxo_integrals(len(Z), _p(Z, ctypes.c_int), _p(xyz), _p(S), _p(H0), _p(Dm), _p(Qm), _p(cn), _p(cnd))
+    assert rc == 0
+    return S, H0, Dm, Qm, cn, cnd
+
+
+def scc(Z, xyz, charge=0, kT=300.0 * 3.166808578545117e-06, opts=None):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    n, ns, nat = nao(Z), nsh(Z), len(Z)
+    P = np.zeros((n, n)); qsh = np.zeros(ns); dp = np.zeros((nat, 3)); qp = np.zeros((nat, 6))
+    eps = np.zeros(n); focc = np.zeros(n)
+    info = Info()
+    o = opts if opts is not None else default_opts()
+    rc = lib().qcxo_scc(nat, _p(Z, ctypes.c_int), _p(xyz), ctypes.c_double(charge), ctypes.c_double(kT),
+                        ctypes.byref(o), _p(P), _p(qsh), _p(dp), _p(qp), _p(eps), _p(focc), ctypes.byref(info))
+    assert rc == 0
+    return P, qsh, dp, qp, eps, focc, info.as_dict()
+
+
+def syev(A):
+    A = np.array(A, dtype=np.float64, order="C")
+    n = A.shape[0]
+    w = np.zeros(n); V = np.zeros((n, n))
+    rc = lib().qcxo_syev(n, _p(A), _p(w), _p(V))
+    return rc, w, V
+
+
+def leapfrog(grad, mass, tstep, xyz, vel):
+    grad = np.ascontiguousarray(grad, dtype=np.float64)
+    mass = np.ascontiguousarray(mass, dtype=np.float64)
+    xyz = np.array(xyz, dtype=np.float64, order="C")
+    vel = np.array(vel, dtype=np.float64, order="C")
+    ke = ctypes.c_double()
+    lib().qcxo_leapfrog(len(mass), _p(grad), _p(mass), ctypes.c_double(tstep), _p(xyz), _p(vel), ctypes.byref(ke))
+    return xyz, vel, ke.value
+
+
+def getspin(Z, charge):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    return lib().qcxo_getspin(len(Z), _p(Z, ctypes.c_int), int(charge))
+
+
+def gnorm(grad):
+    grad = np.ascontiguousarray(grad, dtype=np.float64)
+    return lib().qcxo_gnorm(grad.shape[0], _p(grad))
+
+
+def checkqc(e, grad, qat, charge):
+    grad = np.ascontiguousarray(grad, dtype=np.float64)
+    qat = np.ascontiguousarray(qat, dtype=np.float64)
+    ee = ctypes.c_double(e)
+    ok = lib().qcxo_checkqc(grad.shape[0], ctypes.byref(ee), _p(grad), _p(qat), int(charge))
+    return bool(ok), ee.value
+
+
+def md_batch(mols, nsteps, tstep, grad0, kT, opts=None, nthreads=0):
+    """CPU MD over a list of molecules (dicts with Z, xyz, vel, mass, charge)."""
+    off = np.zeros(len(mols) + 1, dtype=np.int32)
+    for i, m in enumerate(mols):
+        off[i + 1] = off[i] + len(m["Z"])
+    Z = np.ascontiguousarray(np.concatenate([m["Z"] for m in mols]), dtype=np.int32)
+    xyz = np.ascontiguousarray(np.concatenate([m["xyz"] for m in mols]), dtype=np.float64)
+    vel = np.ascontiguousarray(np.concatenate([m["vel"] for m in mols]), dtype=np.float64)
+    mass = np.ascontiguousarray(np.concatenate([m["mass"] for m in mols]), dtype=np.float64)
+    grad = np.ascontiguousarray(np.concatenate(grad0), dtype=np.float64)
+    charge = np.array([m["charge"] for m in mols], dtype=np.float64)
+    kTa = np.full(len(mols), kT, dtype=np.float64)
+    epot = np.zeros(len(mols))
+    iters = np.zeros(len(mols), dtype=np.int32)
+    o = opts if opts is not None else default_opts()
+    fails = lib().qcxo_md_batch(len(mols), _p(off, ctypes.c_int), _p(Z, ctypes.c_int), _p(xyz), _p(vel), _p(mass),
+                                _p(grad), _p(epot), _p(charge), _p(kTa), int(nsteps), ctypes.c_double(tstep),
+                                ctypes.byref(o), int(nthreads), _p(iters, ctypes.c_int))
+    return fails, xyz, vel, grad, epot, iters

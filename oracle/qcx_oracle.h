@@ -1,0 +1,85 @@
+/*
+ * CPU FP64 oracle for the QCxMS trajectory-step hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA path
+ * (libqcxgpu.so) is compared against; only tests, the smoke check and the
+ * CPU-baseline leg of bench.py load it. The product path never calls it.
+ *
+ * It restates, in plain C:
+ *   - the GFN2-xTB energy + analytic gradient evaluation that QCxMS requests
+ *     from tblite v0.2.1 through get_xtb_egrad (src/tblite.f90:65-175),
+ *     following the published GFN2-xTB functional form (Bannwarth, Ehlert,
+ *     Grimme, JCTC 15, 1652 (2019)) with the synthetic parameter set in
+ *     qcxms_gb300/csrc/qcx_params.h;
+ *   - leapfrog (src/md.f90:749-773), ekinet (src/mdinit.f90:57-76),
+ *     getspin (src/utility.f90:449-464), checkqc/gnorm (src/iniqm.f90:684-732).
+ *
+ * Parity with tblite is UNPINNED: tblite and its GFN2 parameter tables are not
+ * part of the QCxMS sources, and QCxMS ships no reference energies/gradients.
+ */
+#ifndef QCX_ORACLE_H
+#define QCX_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int max_iter;          /* SCC iteration cap */
+  double econv;          /* |E_i - E_{i-1}| threshold (Eh) */
+  double pconv;          /* rms(x_out - x_in) threshold over the mixed moments */
+  double broyden_alpha;  /* linear mixing parameter of the modified Broyden scheme */
+} qcxo_opts;
+
+typedef struct {
+  double e_band, e_ies, e_3, e_aes, e_axc, e_disp, e_atm, e_rep, e_ts, e_total;
+  int iterations, converged, nao, nsh;
+  double nel;
+} qcxo_info;
+
+void qcxo_default_opts(qcxo_opts* o);
+int qcxo_nao(int nat, const int* Z);
+int qcxo_nsh(int nat, const int* Z);
+
+/* Energy + gradient. xyz and grad are [nat][3] (Fortran xyz(3,nat)), Bohr.
+ * kT in Hartree. Returns 0 on success, 1 if the SCC did not converge,
+ * -1 on invalid input. */
+int qcxo_egrad(int nat, const int* Z, const double* xyz, double charge, double kT,
+               const qcxo_opts* opts, double* energy, double* grad, double* qat,
+               qcxo_info* info);
+
+/* Intermediate quantities for kernel-level parity tests.
+ * S, H0: [nao][nao]; Dm: [3][nao][nao]; Qm: [6][nao][nao]; cn, cnd: [nat]. */
+int qcxo_integrals(int nat, const int* Z, const double* xyz, double* S, double* H0,
+                   double* Dm, double* Qm, double* cn, double* cnd);
+
+/* Converged SCC quantities: P [nao][nao], qsh [nsh], dipm [nat][3], qp [nat][6],
+ * eps [nao], focc [nao] (occupation per MO, 0..2). */
+int qcxo_scc(int nat, const int* Z, const double* xyz, double charge, double kT,
+             const qcxo_opts* opts, double* P, double* qsh, double* dipm, double* qp,
+             double* eps, double* focc, qcxo_info* info);
+
+/* Symmetric eigensolver used by the oracle (Householder + implicit QL).
+ * A [n][n] is destroyed; V [n][n] holds eigenvectors as columns. */
+int qcxo_syev(int n, double* A, double* w, double* V);
+
+/* Reference MD helpers. */
+void qcxo_leapfrog(int nat, const double* grad, const double* mass, double tstep,
+                   double* xyz, double* vel, double* ke);
+void qcxo_ekinet(int nat, const double* vel, const double* mass, double* ekin, double* temp);
+int qcxo_getspin(int nat, const int* Z, int charge);
+double qcxo_gnorm(int nat, const double* grad);
+int qcxo_checkqc(int nat, double* e, const double* grad, const double* qat, int charge);
+
+/* Batched MD on the CPU: ntraj independent trajectories, each advanced nsteps
+ * leapfrog + egrad steps (OpenMP over trajectories). Arrays are concatenated
+ * per trajectory using atom offsets off[ntraj+1]. grad must hold the gradient
+ * at the initial geometry. Returns the number of failed trajectory-steps. */
+int qcxo_md_batch(int ntraj, const int* off, const int* Z, double* xyz, double* vel,
+                  const double* mass, double* grad, double* epot, const double* charge,
+                  const double* kT, int nsteps, double tstep, const qcxo_opts* opts,
+                  int nthreads, int* scc_iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,101 @@
+"""Seeded synthetic molecules and initial velocities for the trajectory workloads.
+
+No public dataset is involved: every structure is generated from a seed.
+Heavy atoms form a random tree (or a chain) with 1.45 Angstrom bonds, hydrogens
+are attached at 1.09 Angstrom, and every coordinate gets Gaussian jitter.
+"""
+import numpy as np
+
+from .constants import AATOAU, KB_AU, MASS_AU
+
+VALENCE = {1: 1, 6: 4, 7: 3, 8: 2, 9: 1, 15: 3, 16: 2, 17: 1, 14: 4, 5: 3}
+
+
+def _place(rng, xyz, parent, bond, mindist):
+    best, best_d = None, -1.0
+    for _ in range(64):
+        v = rng.normal(size=3)
+        v /= np.linalg.norm(v)
+        cand = xyz[parent] + bond * v
+        d = np.min(np.linalg.norm(np.asarray(xyz) - cand, axis=1))
+        if d >= mindist:
+            return cand
+        if d > best_d:
+            best, best_d = cand, d
+    return best
+
+
+def build_molecule(heavy, n_h, rng, chain=False, bond_heavy=1.45, bond_h=1.09, jitter=0.05):
+    """Return (Z, xyz[Bohr]) for the given heavy-atom list and hydrogen count."""
+    Z = list(heavy)
+    xyz = [np.zeros(3)]
+    nbond = [0] * len(heavy)
+    for i in range(1, len(heavy)):
+        if chain:
+            parent = i - 1
+        else:
+            free = [j for j in range(i) if nbond[j] < VALENCE.get(heavy[j], 4)]
+            parent = int(rng.choice(free)) if free else int(rng.integers(0, i))
+        xyz.append(_place(rng, xyz, parent, bond_heavy, 0.9 * bond_heavy))
+        nbond[parent] += 1
+        nbond[i] += 1
+    k = 0
+    for _ in range(n_h):
+        free = [j for j in range(len(heavy)) if nbond[j] < VALENCE.get(heavy[j], 4)]
+        if free:
+            parent = free[k % len(free)]
+            k += 1
+        else:
+            parent = int(rng.integers(0, len(heavy)))
+        xyz.append(_place(rng, xyz, parent, bond_h, 0.75 * bond_h))
+        nbond[parent] += 1
+        Z.append(1)
+    xyz = np.array(xyz) + rng.normal(scale=jitter, size=(len(Z), 3))
+    return np.array(Z, dtype=np.int32), xyz * AATOAU
+
+
+def c6h12o2(seed=1234):
+    """The 20-atom C6H12O2 chain (6 C + 2 O heavy-atom chain, 12 H)."""
+    rng = np.random.default_rng(seed)
+    heavy = [6, 6, 6, 8, 6, 6, 8, 6]
+    return build_molecule(heavy, 12, rng, chain=True)
+
+
+def random_chno(nat, seed, fractions=((6, 0.35), (1, 0.5), (7, 0.05), (8, 0.1))):
+    """Random C/H/N/O molecule with ``nat`` atoms and at least one heavy atom."""
+    rng = np.random.default_rng(seed)
+    elems = np.array([e for e, _ in fractions])
+    p = np.array([f for _, f in fractions])
+    p = p / p.sum()
+    draw = rng.choice(elems, size=nat, p=p)
+    heavy = [int(z) for z in draw if z != 1]
+    if not heavy:
+        heavy = [6]
+    n_h = nat - len(heavy)
+    return build_molecule(heavy, n_h, rng)
+
+
+def masses(Z):
+    return np.array([MASS_AU[int(z)] for z in Z])
+
+
+def maxwell_boltzmann(Z, temp, seed):
+    """Velocities (Bohr / au time) at temperature ``temp`` with no centre-of-mass motion."""
+    rng = np.random.default_rng(seed + 7919)
+    m = masses(Z)
+    v = rng.normal(size=(len(Z), 3)) * np.sqrt(KB_AU * temp / m)[:, None]
+    vcom = (m[:, None] * v).sum(0) / m.sum()
+    return v - vcom
+
+
+def batch_workload(ntraj, nmin, nmax, seed0=0, tmin=1000.0, tmax=4000.0):
+    """ntraj random C/H/N/O cations with N ~ U{nmin..nmax} and T0 ~ U(tmin, tmax)."""
+    mols = []
+    for t in range(ntraj):
+        rng = np.random.default_rng(100000 + seed0 + t)
+        nat = int(rng.integers(nmin, nmax + 1))
+        temp = float(rng.uniform(tmin, tmax))
+        Z, xyz = random_chno(nat, seed0 + t)
+        vel = maxwell_boltzmann(Z, temp, seed0 + t)
+        mols.append({"Z": Z, "xyz": xyz, "vel": vel, "mass": masses(Z), "charge": 1, "temp": temp})
+    return mols
