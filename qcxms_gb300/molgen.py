@@ -11,18 +11,17 @@ from .constants import AATOAU, KB_AU, MASS_AU
 VALENCE = {1: 1, 6: 4, 7: 3, 8: 2, 9: 1, 15: 3, 16: 2, 17: 1, 14: 4, 5: 3}
 
 
-def _place(rng, xyz, parent, bond, mindist):
-    best, best_d = None, -1.0
-    for _ in range(64):
-        v = rng.normal(size=3)
-        v /= np.linalg.norm(v)
-        cand = xyz[parent] + bond * v
-        d = np.min(np.linalg.norm(np.asarray(xyz) - cand, axis=1))
-        if d >= mindist:
-            return cand
-        if d > best_d:
-            best, best_d = cand, d
-    return best
+def _place(rng, xyz, parent, bond, ntry=256):
+    """Put a new atom at ``bond`` from ``parent``, as far as possible from all others."""
+    v = rng.normal(size=(ntry, 3))
+    v /= np.linalg.norm(v, axis=1)[:, None]
+    cand = xyz[parent] + bond * v
+    others = [k for k in range(len(xyz)) if k != parent]
+    if not others:
+        return cand[0]
+    o = np.asarray([xyz[k] for k in others])
+    dmin = np.min(np.linalg.norm(cand[:, None, :] - o[None, :, :], axis=2), axis=1)
+    return cand[int(np.argmax(dmin))]
 
 
 def build_molecule(heavy, n_h, rng, chain=False, bond_heavy=1.45, bond_h=1.09, jitter=0.05):
@@ -36,7 +35,7 @@ def build_molecule(heavy, n_h, rng, chain=False, bond_heavy=1.45, bond_h=1.09, j
         else:
             free = [j for j in range(i) if nbond[j] < VALENCE.get(heavy[j], 4)]
             parent = int(rng.choice(free)) if free else int(rng.integers(0, i))
-        xyz.append(_place(rng, xyz, parent, bond_heavy, 0.9 * bond_heavy))
+        xyz.append(_place(rng, xyz, parent, bond_heavy))
         nbond[parent] += 1
         nbond[i] += 1
     k = 0
@@ -47,7 +46,7 @@ def build_molecule(heavy, n_h, rng, chain=False, bond_heavy=1.45, bond_h=1.09, j
             k += 1
         else:
             parent = int(rng.integers(0, len(heavy)))
-        xyz.append(_place(rng, xyz, parent, bond_h, 0.75 * bond_h))
+        xyz.append(_place(rng, xyz, parent, bond_h))
         nbond[parent] += 1
         Z.append(1)
     xyz = np.array(xyz) + rng.normal(scale=jitter, size=(len(Z), 3))

@@ -124,6 +124,11 @@ def contracted_coeffs(alpha, craw, l):
     return c / math.sqrt(s)
 
 
+# Repulsion exponents of H, C, N, O, S chosen so that H2, CH4, NH3, H2O and H2S
+# have zero radial force at their textbook bond lengths (0.74, 1.09, 1.01,
+# 0.96, 1.34 Angstrom) with the rest of this parameter set.
+REP_ALPHA_FIT = {1: 2.105937, 6: 1.715302, 7: 2.175388, 8: 2.656783, 16: 0.834374}
+
 # --------------------------------------------------------------------------
 # element rules
 # --------------------------------------------------------------------------
@@ -177,7 +182,7 @@ def self_energy(z, l):
     if p == 1:
         return -0.50 if z == 1 else -0.90
     if p == 2:
-        return {0: -0.35 - 0.12 * nv, 1: -0.18 - 0.06 * nv}[l]
+        return {0: -0.30 - 0.10 * nv, 1: -0.20 - 0.045 * nv}[l]
     return {0: -0.30 - 0.09 * nv, 1: -0.16 - 0.045 * nv, 2: -0.08}[l]
 
 
@@ -261,7 +266,7 @@ def main():
         return {1: 0.47 if z == 1 else 0.90, 2: 0.35 + 0.05 * nv, 3: 0.30 + 0.04 * nv}[p]
 
     def gam3_atom(z):
-        return 0.10 + 0.02 * nval(z)
+        return 0.04 + 0.01 * nval(z)
 
     arrsh("qcx_sh_hardness", "double", lambda z, i, n, l: eta_atom(z) * {0: 1.0, 1: 0.9, 2: 0.7}[l])
     arrsh("qcx_sh_gamma3", "double", lambda z, i, n, l: gam3_atom(z) * {0: 1.0, 1: 0.5, 2: 0.25}[l])
@@ -292,7 +297,8 @@ def main():
     arr1("qcx_nvalence", "double", [0] + [float(nval(z)) for z in z_all])
     arr1("qcx_en", "double", PAULING)
     arr1("qcx_rcov", "double", [0] + [4.0 / 3.0 * RCOV2009[z] * AATOAU for z in z_all])
-    arr1("qcx_rep_alpha", "double", [0] + [2.2 if z == 1 else (2.0 - 0.03 * nval(z) if period(z) == 2 else 1.6 - 0.02 * nval(z)) for z in z_all])
+    arr1("qcx_rep_alpha", "double", [0] + [REP_ALPHA_FIT.get(z, 2.0 - 0.03 * nval(z) if period(z) == 2 else 1.6 - 0.02 * nval(z))
+                                         for z in z_all])
     arr1("qcx_rep_zeff", "double", [0] + [1.0 if z == 1 else (2.0 if z == 2 else 1.0 + 0.9 * nval(z)) for z in z_all])
     arr1("qcx_aes_dkernel", "double", [0] + [0.010 + 0.002 * nval(z) for z in z_all])
     arr1("qcx_aes_qkernel", "double", [0] + [0.005 + 0.001 * nval(z) for z in z_all])
