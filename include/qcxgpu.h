@@ -1,0 +1,108 @@
+/*
+ * libqcxgpu -- C ABI of the GB300 GFN2-xTB trajectory-step engine.
+ *
+ * Plain pointers and sizes only. Coordinates, velocities and gradients are
+ * [nat][3] row-major doubles, which is the memory order of the Fortran
+ * arrays xyz(3,nat) / grad(3,nat) used by QCxMS. Units: Bohr, Hartree,
+ * atomic time units, electron masses (atomic units), Kelvin for etemp.
+ *
+ * Return codes follow the reference bridge (src/tblite.f90:55-58):
+ *   0  success
+ *   5  unknown or unsupported method
+ *  -1  failure (SCC not converged, non-finite result, invalid input, CUDA error)
+ * qcx_last_error() describes the last failure of the calling process.
+ */
+#ifndef QCXGPU_H
+#define QCXGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QCX_METHOD_GFN1 1
+#define QCX_METHOD_GFN2 2
+#define QCX_METHOD_IPEA1 11
+
+/* status bits reported per trajectory by qcx_batch_get */
+#define QCX_STATUS_SCC_NOT_CONVERGED 1
+#define QCX_STATUS_NON_FINITE 2
+#define QCX_STATUS_CHOLESKY_FAILED 4
+#define QCX_STATUS_EIGEN_NOT_CONVERGED 8
+
+/* Library version (major*10000 + minor*100 + patch). */
+int qcx_version(void);
+
+/* Text of the last error in this process ("" if none). */
+const char* qcx_last_error(void);
+
+/*
+ * Single-structure energy + gradient: the drop-in for
+ *   get_xtb_egrad(num, xyz, charge, multiplicity, method, etemp,
+ *                 output_file, qat, energy, gradient, stat, spec_calc)
+ * of module qcxms_tblite (src/tblite.f90:65-175), as called by egrad
+ * (src/iniqm.f90:641-655) on every MD step. The multiplicity is accepted but,
+ * as in the reference (uhf = min(multiplicity-1, 0), src/tblite.f90:111),
+ * the calculation is spin-restricted with Fermi smearing at etemp.
+ * The device state for a given atom list is cached between calls.
+ * Writes energy (Eh), grad [nat][3] (Eh/Bohr) and qat [nat] (Mulliken charges).
+ */
+int qcx_egrad(int method, int nat, const int32_t* num, const double* xyz, int charge, int multiplicity,
+              double etemp, double* energy, double* grad, double* qat);
+
+/*
+ * Batched trajectories: nmol independent molecules advanced together on one
+ * GPU. Replaces the one-process-per-trajectory fan-out of bin/pqcxms:88-99;
+ * each molecule follows the md.f90 step: leapfrog (src/md.f90:749-773) then
+ * egrad (src/md.f90:396).
+ */
+typedef struct qcx_batch qcx_batch;
+
+/* nat[nmol]; num = atomic numbers of all molecules concatenated;
+ * charge[nmol]; etemp[nmol] in Kelvin. Returns NULL on failure. */
+qcx_batch* qcx_batch_create(int nmol, const int32_t* nat, const int32_t* num, const double* charge,
+                            const double* etemp);
+void qcx_batch_destroy(qcx_batch* b);
+
+/* SCC controls (defaults: 100, 1e-7 Eh, 1e-6, 0.4). max_iter <= 100. */
+int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, double mixing);
+
+/* Copy host state in. Any pointer may be NULL to keep the current value.
+ * xyz, vel: [natom][3]; mass: [natom] (atomic units). */
+int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass);
+
+/* Energy and gradient at the current coordinates. */
+int qcx_batch_egrad(qcx_batch* b);
+
+/* nsteps MD steps of tstep (atomic time units): leapfrog with the current
+ * gradient, then energy + gradient at the new coordinates. The first call
+ * captures one step in a CUDA graph and replays it. Requires a prior
+ * qcx_batch_egrad (the gradient of the starting geometry). */
+int qcx_batch_step(qcx_batch* b, int nsteps, double tstep);
+
+/* Copy results out. Any pointer may be NULL. energy, ekin: [nmol];
+ * status, iters: [nmol] (status bits QCX_STATUS_*, SCC iterations of the
+ * last evaluation); xyz, vel, grad: [natom][3]; qat: [natom]. */
+int qcx_batch_get(qcx_batch* b, double* xyz, double* vel, double* grad, double* energy, double* qat,
+                  double* ekin, int32_t* status, int32_t* iters);
+
+/* Energy decomposition of molecule i: band, isotropic ES, third order,
+ * anisotropic ES, multipole XC, dispersion, three-body, repulsion, -TS,
+ * total, Fermi level (11 doubles). */
+int qcx_batch_get_energy_terms(qcx_batch* b, int i, double* terms);
+
+/* Dense matrices of molecule i for inspection: which = 0 S, 1 H0, 8 P,
+ * 9 W (nao x nao, row-major); returns nao or -1. */
+int qcx_batch_get_matrix(qcx_batch* b, int i, int which, double* out);
+
+/* Number of kernel launches issued by the last qcx_batch_step /
+ * qcx_batch_egrad call (graph replays count their kernel nodes). */
+long long qcx_batch_kernel_launches(qcx_batch* b);
+
+/* Synchronise the batch's stream. */
+int qcx_batch_sync(qcx_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -24,7 +24,7 @@ def build(force=False):
             os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(d) for d in deps):
         return LIB_PATH
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-o", LIB_PATH, src, "-lm"]
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp", "-o", LIB_PATH, src, "-lm"]
     subprocess.check_call(cmd)
     return LIB_PATH
 

@@ -1,0 +1,204 @@
+"""GB300-native GFN2-xTB trajectory-step engine for QCxMS.
+
+The compute path is ``libqcxgpu.so`` (hand-written sm_103a CUDA kernels behind
+the C ABI in ``include/qcxgpu.h``). This package only binds that ABI with
+ctypes and mirrors the reference's Fortran interface:
+
+* :func:`get_xtb_egrad` -- ``module qcxms_tblite``'s ``get_xtb_egrad``
+  (``src/tblite.f90:65-175``): atomic numbers, Bohr coordinates, charge,
+  multiplicity, method and electronic temperature in; charges, energy,
+  gradient and a status code out.
+* :class:`Batch` -- many trajectories advanced together (leapfrog of
+  ``src/md.f90:749-773`` followed by the energy/gradient call, as in the MD
+  loop at ``src/md.f90:390-396``).
+
+There is no CPU fallback: if the CUDA library cannot be loaded, every call
+raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import constants
+
+__all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "load_library", "library_path",
+           "STATUS_SCC_NOT_CONVERGED", "STATUS_NON_FINITE", "STATUS_CHOLESKY_FAILED", "STATUS_EIGEN_NOT_CONVERGED"]
+
+# method selectors, src/tblite.f90:34-40
+gfn1_xtb = 1
+gfn2_xtb = 2
+ipea1_xtb = 11
+
+STATUS_SCC_NOT_CONVERGED = 1
+STATUS_NON_FINITE = 2
+STATUS_CHOLESKY_FAILED = 4
+STATUS_EIGEN_NOT_CONVERGED = 8
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+
+def library_path():
+    return os.path.join(_HERE, "_build", "libqcxgpu.so")
+
+
+def load_library(build_if_missing=True):
+    """Load libqcxgpu.so (building it in-tree first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if build_if_missing:
+        from . import build as _build
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("libqcxgpu.so is missing (%s); run __graft_entry__.build()" % path)
+    lib = ctypes.CDLL(path)
+    c_int, c_double, c_ll = ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    P = ctypes.POINTER
+    lib.qcx_version.restype = c_int
+    lib.qcx_last_error.restype = ctypes.c_char_p
+    lib.qcx_egrad.restype = c_int
+    lib.qcx_egrad.argtypes = [c_int, c_int, P(ctypes.c_int32), P(c_double), c_int, c_int, c_double,
+                              P(c_double), P(c_double), P(c_double)]
+    lib.qcx_batch_create.restype = ctypes.c_void_p
+    lib.qcx_batch_create.argtypes = [c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double), P(c_double)]
+    lib.qcx_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.qcx_batch_set_scc.argtypes = [ctypes.c_void_p, c_int, c_double, c_double, c_double]
+    lib.qcx_batch_set_state.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double)]
+    lib.qcx_batch_egrad.argtypes = [ctypes.c_void_p]
+    lib.qcx_batch_step.argtypes = [ctypes.c_void_p, c_int, c_double]
+    lib.qcx_batch_get.argtypes = [ctypes.c_void_p] + [P(c_double)] * 6 + [P(ctypes.c_int32)] * 2
+    lib.qcx_batch_get_energy_terms.argtypes = [ctypes.c_void_p, c_int, P(c_double)]
+    lib.qcx_batch_get_matrix.argtypes = [ctypes.c_void_p, c_int, c_int, P(c_double)]
+    lib.qcx_batch_kernel_launches.restype = c_ll
+    lib.qcx_batch_kernel_launches.argtypes = [ctypes.c_void_p]
+    lib.qcx_batch_sync.argtypes = [ctypes.c_void_p]
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def _err(lib):
+    return lib.qcx_last_error().decode()
+
+
+def get_xtb_egrad(num, xyz, charge, multiplicity, method=gfn2_xtb, etemp=300.0, output_file=None):
+    """Energy, gradient and Mulliken charges of one structure.
+
+    Mirrors ``get_xtb_egrad`` of ``src/tblite.f90:65-175``. Returns
+    ``(qat, energy, gradient, stat)`` with ``stat`` = 0 (ok), 5 (unknown or
+    unsupported method) or -1 (failure). When ``output_file`` is given a
+    one-line summary is written there, as the reference always (re)creates it.
+    """
+    lib = load_library()
+    num = np.ascontiguousarray(num, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(len(num), 3)
+    e = np.zeros(1)
+    g = np.zeros((len(num), 3))
+    q = np.zeros(len(num))
+    stat = lib.qcx_egrad(int(method), len(num), _ip(num), _dp(xyz), int(charge), int(multiplicity),
+                         float(etemp), _dp(e), _dp(g), _dp(q))
+    if output_file:
+        with open(output_file, "w") as f:
+            f.write("qcxgpu GFN2-xTB energy %.12f Eh stat %d %s\n" % (e[0], stat, _err(lib) if stat else ""))
+    return q, float(e[0]), g, int(stat)
+
+
+class Batch:
+    """Independent trajectories on one GPU (one molecule each)."""
+
+    def __init__(self, mols, etemp=300.0):
+        lib = load_library()
+        self._lib = lib
+        self.nmol = len(mols)
+        self.nat = np.array([len(m["Z"]) for m in mols], dtype=np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.nat)]).astype(np.int64)
+        self.natom = int(self.offsets[-1])
+        Z = np.ascontiguousarray(np.concatenate([np.asarray(m["Z"]) for m in mols]), dtype=np.int32)
+        charge = np.array([float(m.get("charge", 0)) for m in mols], dtype=np.float64)
+        et = np.array([float(m.get("etemp", etemp)) for m in mols], dtype=np.float64)
+        self.Z = Z
+        h = lib.qcx_batch_create(self.nmol, _ip(self.nat), _ip(Z), _dp(charge), _dp(et))
+        if not h:
+            raise RuntimeError("qcx_batch_create failed: " + _err(lib))
+        self._h = ctypes.c_void_p(h)
+        xyz = np.concatenate([np.asarray(m["xyz"], dtype=np.float64).reshape(-1, 3) for m in mols])
+        vel = np.concatenate([np.asarray(m.get("vel", np.zeros((len(m["Z"]), 3))), dtype=np.float64).reshape(-1, 3)
+                              for m in mols])
+        mass = np.concatenate([np.asarray(m.get("mass", np.ones(len(m["Z"]))), dtype=np.float64) for m in mols])
+        self.set_state(xyz, vel, mass)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError("%s failed: %s" % (what, _err(self._lib)))
+
+    def set_scc(self, max_iter=100, econv=1e-7, pconv=1e-6, mixing=0.4):
+        self._check(self._lib.qcx_batch_set_scc(self._h, int(max_iter), float(econv), float(pconv), float(mixing)),
+                    "set_scc")
+
+    def set_state(self, xyz=None, vel=None, mass=None):
+        c = lambda a, s: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(s)
+        xyz, vel, mass = c(xyz, (self.natom, 3)), c(vel, (self.natom, 3)), c(mass, (self.natom,))
+        self._check(self._lib.qcx_batch_set_state(self._h, _dp(xyz), _dp(vel), _dp(mass)), "set_state")
+        self._lib.qcx_batch_sync(self._h)
+
+    def egrad(self):
+        self._check(self._lib.qcx_batch_egrad(self._h), "egrad")
+
+    def step(self, nsteps, tstep=0.5 * constants.FSTOAU):
+        self._check(self._lib.qcx_batch_step(self._h, int(nsteps), float(tstep)), "step")
+
+    def sync(self):
+        self._check(self._lib.qcx_batch_sync(self._h), "sync")
+
+    def get(self):
+        xyz = np.zeros((self.natom, 3)); vel = np.zeros((self.natom, 3)); grad = np.zeros((self.natom, 3))
+        energy = np.zeros(self.nmol); qat = np.zeros(self.natom); ekin = np.zeros(self.nmol)
+        status = np.zeros(self.nmol, dtype=np.int32); iters = np.zeros(self.nmol, dtype=np.int32)
+        self._check(self._lib.qcx_batch_get(self._h, _dp(xyz), _dp(vel), _dp(grad), _dp(energy), _dp(qat), _dp(ekin),
+                                            _ip(status), _ip(iters)), "get")
+        return {"xyz": xyz, "vel": vel, "grad": grad, "energy": energy, "qat": qat, "ekin": ekin,
+                "status": status, "iters": iters}
+
+    def energy_terms(self, i):
+        t = np.zeros(11)
+        self._check(self._lib.qcx_batch_get_energy_terms(self._h, int(i), _dp(t)), "energy_terms")
+        names = ["band", "ies", "e3", "aes", "axc", "disp", "atm", "rep", "ts", "total", "efermi"]
+        return dict(zip(names, t))
+
+    def matrix(self, i, which):
+        nat = int(self.nat[i])
+        Zi = self.Z[self.offsets[i]:self.offsets[i] + nat]
+        from .basis import nao_of
+        n = nao_of(Zi)
+        out = np.zeros((n, n))
+        rc = self._lib.qcx_batch_get_matrix(self._h, int(i), int(which), _dp(out))
+        if rc < 0:
+            raise RuntimeError("get_matrix failed: " + _err(self._lib))
+        return out
+
+    def kernel_launches(self):
+        return int(self._lib.qcx_batch_kernel_launches(self._h))
+
+    def split(self, arr):
+        return [arr[self.offsets[i]:self.offsets[i + 1]] for i in range(self.nmol)]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.qcx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,439 @@
+// Host side of libqcxgpu: batch construction, launch sequencing, CUDA graph
+// capture of one MD step, and the C ABI declared in include/qcxgpu.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/qcxgpu.h"
+#include "qcx_batch.cuh"
+#include "qcx_kernels.h"
+
+using namespace qcx;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& s) { g_last_error = s; }
+
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      set_error(std::string(#call) + ": " + cudaGetErrorString(e_));              \
+      return -1;                                                                   \
+    }                                                                              \
+  } while (0)
+
+double prim_norm(double a, int l) { return std::pow(2.0 * a / QCX_PI, 0.75) * std::pow(4.0 * a, 0.5 * l); }
+
+void fill_params(Params& p) {
+  std::memset(&p, 0, sizeof(p));
+  for (int z = 0; z <= kMaxZ; ++z) {
+    p.nsh[z] = qcx_nsh[z];
+    for (int k = 0; k < kMaxSh; ++k) {
+      p.sh_l[z][k] = qcx_sh_l[z][k];
+      p.sh_nprim[z][k] = qcx_sh_nprim[z][k];
+      p.zeta[z][k] = qcx_sh_zeta[z][k];
+      p.refocc[z][k] = qcx_sh_refocc[z][k];
+      p.selfenergy[z][k] = qcx_sh_selfenergy[z][k];
+      p.kcn[z][k] = qcx_sh_kcn[z][k];
+      p.kpoly[z][k] = qcx_sh_kpoly[z][k];
+      p.hardness[z][k] = qcx_sh_hardness[z][k];
+      p.gamma3[z][k] = qcx_sh_gamma3[z][k];
+      for (int i = 0; i < kMaxPrim; ++i) {
+        p.alpha[z][k][i] = qcx_prim_alpha[z][k][i];
+        p.cnorm[z][k][i] = (i < qcx_sh_nprim[z][k] && z > 0 && k < qcx_nsh[z])
+                               ? qcx_prim_coeff[z][k][i] * prim_norm(qcx_prim_alpha[z][k][i], qcx_sh_l[z][k])
+                               : 0.0;
+      }
+    }
+    p.en[z] = qcx_en[z];
+    p.rcov[z] = qcx_rcov[z];
+    p.rep_alpha[z] = qcx_rep_alpha[z];
+    p.rep_zeff[z] = qcx_rep_zeff[z];
+    p.aes_dk[z] = qcx_aes_dkernel[z];
+    p.aes_qk[z] = qcx_aes_qkernel[z];
+    p.aes_rad0[z] = qcx_aes_rad0[z];
+    p.aes_valcn[z] = qcx_aes_valcn[z];
+    p.d4_nref[z] = qcx_d4_nref[z];
+    for (int i = 0; i < kMaxRef; ++i) {
+      p.d4_cnref[z][i] = qcx_d4_cnref[z][i];
+      p.d4_alpha0[z][i] = qcx_d4_alpha0[z][i];
+      p.d4_omega[z][i] = qcx_d4_omega[z][i];
+    }
+    p.d4_eta[z] = qcx_d4_eta[z];
+    p.r4r2[z] = qcx_r4r2[z];
+  }
+}
+
+template <typename T>
+int dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  CK(cudaMalloc((void**)p, sizeof(T) * n));
+  return 0;
+}
+
+}  // namespace
+
+struct qcx_batch {
+  int nmol = 0, natom = 0, nshell = 0, npair = 0, max_nao = 0;
+  std::vector<MolDesc> mol;
+  std::vector<int> Z;
+  cudaStream_t stream = nullptr;
+  DevBatch dev{};
+  // device allocations
+  Params* d_prm = nullptr;
+  MolDesc* d_mol = nullptr;
+  int *d_Z = nullptr, *d_atom_mol = nullptr, *d_sh_atom = nullptr, *d_sh_k = nullptr, *d_sh_ao = nullptr;
+  ShellPair* d_pairs = nullptr;
+  double *d_xyz = nullptr, *d_grad = nullptr, *d_vel = nullptr, *d_mass = nullptr;
+  double *d_cn = nullptr, *d_cnd = nullptr, *d_dedcn = nullptr, *d_dedcnd = nullptr, *d_mrad = nullptr,
+         *d_dmrad = nullptr, *d_w4 = nullptr, *d_dw4 = nullptr, *d_qat = nullptr;
+  double *d_mats = nullptr, *d_vecs = nullptr, *d_energy = nullptr, *d_ekin = nullptr;
+  int *d_status = nullptr, *d_iters = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  double graph_tstep = 0.0;
+  long long launches = 0;
+  size_t bytes = 0;
+};
+
+namespace {
+
+void enqueue_egrad(qcx_batch* b) {
+  const DevBatch& d = b->dev;
+  launch_cn(d, b->stream);
+  launch_integrals(d, b->stream);
+  launch_scc(d, 0, b->stream);
+  launch_zero_grad(d, b->stream);
+  launch_grad_pairs(d, b->stream);
+  launch_grad_atoms(d, b->stream);
+}
+constexpr int kEgradLaunches = 6;
+
+void free_batch(qcx_batch* b) {
+  if (!b) return;
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  void* ptrs[] = {b->d_prm, b->d_mol, b->d_Z, b->d_atom_mol, b->d_sh_atom, b->d_sh_k, b->d_sh_ao, b->d_pairs,
+                  b->d_xyz, b->d_grad, b->d_vel, b->d_mass, b->d_cn, b->d_cnd, b->d_dedcn, b->d_dedcnd,
+                  b->d_mrad, b->d_dmrad, b->d_w4, b->d_dw4, b->d_qat, b->d_mats, b->d_vecs, b->d_energy,
+                  b->d_ekin, b->d_status, b->d_iters};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, const double* charge,
+                const double* etemp) {
+  b->nmol = nmol;
+  std::vector<int> atom_mol, sh_atom, sh_k, sh_ao;
+  std::vector<ShellPair> pairs;
+  long long mat_off = 0, vec_off = 0;
+  int aoff = 0;
+  for (int m = 0; m < nmol; ++m) {
+    if (nat[m] < 1) {
+      set_error("molecule with no atoms");
+      return -1;
+    }
+    MolDesc md{};
+    md.nat = nat[m];
+    md.atom_off = aoff;
+    md.sh_off = (int)sh_atom.size();
+    int nao = 0;
+    double nel = -charge[m];
+    for (int a = 0; a < nat[m]; ++a) {
+      int z = num[aoff + a];
+      if (z < 1 || z > kMaxZ) {
+        set_error("atomic number outside the parameterised range 1..18");
+        return -1;
+      }
+      b->Z.push_back(z);
+      atom_mol.push_back(m);
+      for (int k = 0; k < qcx_nsh[z]; ++k) {
+        sh_atom.push_back(aoff + a);
+        sh_k.push_back(k);
+        sh_ao.push_back(nao);
+        nao += 2 * qcx_sh_l[z][k] + 1;
+        nel += qcx_sh_refocc[z][k];
+      }
+    }
+    md.nsh = (int)sh_atom.size() - md.sh_off;
+    md.nao = nao;
+    md.len = md.nsh + 9 * md.nat;
+    md.nmem = QCX_SCC_MAXITER;
+    md.nel = nel;
+    md.kT = etemp[m] * QCX_KTOAU;
+    md.charge = charge[m];
+    md.mat_off = mat_off;
+    mat_off += (long long)kNumMat * slot_size(nao);
+    md.vec_off = vec_off;
+    vec_off += VecLayout::make(md.nat, md.nsh, nao, md.len, md.nmem).total;
+    for (int s = 0; s < md.nsh; ++s)
+      for (int t = 0; t < md.nsh; ++t) pairs.push_back({md.sh_off + s, md.sh_off + t});
+    b->mol.push_back(md);
+    b->max_nao = nao > b->max_nao ? nao : b->max_nao;
+    aoff += nat[m];
+  }
+  b->natom = aoff;
+  b->nshell = (int)sh_atom.size();
+  b->npair = (int)pairs.size();
+  CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  Params hp;
+  fill_params(hp);
+  int na = b->natom;
+  if (dalloc(&b->d_prm, 1) || dalloc(&b->d_mol, nmol) || dalloc(&b->d_Z, na) || dalloc(&b->d_atom_mol, na) ||
+      dalloc(&b->d_sh_atom, b->nshell) || dalloc(&b->d_sh_k, b->nshell) || dalloc(&b->d_sh_ao, b->nshell) ||
+      dalloc(&b->d_pairs, b->npair) || dalloc(&b->d_xyz, 3 * na) || dalloc(&b->d_grad, 3 * na) ||
+      dalloc(&b->d_vel, 3 * na) || dalloc(&b->d_mass, na) || dalloc(&b->d_cn, na) || dalloc(&b->d_cnd, na) ||
+      dalloc(&b->d_dedcn, na) || dalloc(&b->d_dedcnd, na) || dalloc(&b->d_mrad, na) || dalloc(&b->d_dmrad, na) ||
+      dalloc(&b->d_w4, (size_t)na * kMaxRef) || dalloc(&b->d_dw4, (size_t)na * kMaxRef) || dalloc(&b->d_qat, na) ||
+      dalloc(&b->d_mats, (size_t)mat_off) || dalloc(&b->d_vecs, (size_t)vec_off) ||
+      dalloc(&b->d_energy, (size_t)nmol * kNumEnergy) || dalloc(&b->d_ekin, nmol) || dalloc(&b->d_status, nmol) ||
+      dalloc(&b->d_iters, nmol))
+    return -1;
+  b->bytes = sizeof(double) * ((size_t)mat_off + (size_t)vec_off);
+  CK(cudaMemcpy(b->d_prm, &hp, sizeof(Params), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_mol, b->mol.data(), sizeof(MolDesc) * nmol, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_Z, b->Z.data(), sizeof(int) * na, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_atom_mol, atom_mol.data(), sizeof(int) * na, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_sh_atom, sh_atom.data(), sizeof(int) * b->nshell, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_sh_k, sh_k.data(), sizeof(int) * b->nshell, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_sh_ao, sh_ao.data(), sizeof(int) * b->nshell, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_pairs, pairs.data(), sizeof(ShellPair) * b->npair, cudaMemcpyHostToDevice));
+  CK(cudaMemset(b->d_vel, 0, sizeof(double) * 3 * na));
+  CK(cudaMemset(b->d_grad, 0, sizeof(double) * 3 * na));
+  CK(cudaMemset(b->d_xyz, 0, sizeof(double) * 3 * na));
+  CK(cudaMemset(b->d_status, 0, sizeof(int) * nmol));
+  CK(cudaMemset(b->d_energy, 0, sizeof(double) * nmol * kNumEnergy));
+  CK(cudaMemset(b->d_ekin, 0, sizeof(double) * nmol));
+  {
+    std::vector<double> m(na, 1.0);
+    CK(cudaMemcpy(b->d_mass, m.data(), sizeof(double) * na, cudaMemcpyHostToDevice));
+  }
+  DevBatch& d = b->dev;
+  d.nmol = nmol;
+  d.natom = na;
+  d.nshell = b->nshell;
+  d.npair = b->npair;
+  d.prm = b->d_prm;
+  d.mol = b->d_mol;
+  d.Z = b->d_Z;
+  d.atom_mol = b->d_atom_mol;
+  d.xyz = b->d_xyz;
+  d.grad = b->d_grad;
+  d.vel = b->d_vel;
+  d.mass = b->d_mass;
+  d.cn = b->d_cn;
+  d.cnd = b->d_cnd;
+  d.dedcn = b->d_dedcn;
+  d.dedcnd = b->d_dedcnd;
+  d.mrad = b->d_mrad;
+  d.dmrad = b->d_dmrad;
+  d.w4 = b->d_w4;
+  d.dw4 = b->d_dw4;
+  d.qat = b->d_qat;
+  d.sh_atom = b->d_sh_atom;
+  d.sh_k = b->d_sh_k;
+  d.sh_ao = b->d_sh_ao;
+  d.pairs = b->d_pairs;
+  d.mats = b->d_mats;
+  d.vecs = b->d_vecs;
+  d.energy = b->d_energy;
+  d.status = b->d_status;
+  d.iters = b->d_iters;
+  d.ekin = b->d_ekin;
+  d.max_nao = b->max_nao;
+  d.smem_bytes = (int)scc_smem_bytes(b->max_nao, 0);
+  d.max_iter = QCX_SCC_MAXITER;
+  d.econv = QCX_SCC_ECONV;
+  d.pconv = QCX_SCC_PCONV;
+  d.mix_alpha = QCX_BROYDEN_ALPHA;
+  return 0;
+}
+
+int check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("kernel launch: ") + cudaGetErrorString(e));
+    return -1;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qcx_version(void) { return 100; }
+
+const char* qcx_last_error(void) { return g_last_error.c_str(); }
+
+qcx_batch* qcx_batch_create(int nmol, const int32_t* nat, const int32_t* num, const double* charge,
+                            const double* etemp) {
+  if (nmol < 1 || !nat || !num || !charge || !etemp) {
+    set_error("qcx_batch_create: invalid arguments");
+    return nullptr;
+  }
+  qcx_batch* b = new qcx_batch();
+  if (build_batch(b, nmol, nat, num, charge, etemp)) {
+    free_batch(b);
+    return nullptr;
+  }
+  return b;
+}
+
+void qcx_batch_destroy(qcx_batch* b) { free_batch(b); }
+
+int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, double mixing) {
+  if (!b || max_iter < 1 || max_iter > QCX_SCC_MAXITER || !(econv > 0) || !(pconv > 0) || !(mixing > 0)) {
+    set_error("qcx_batch_set_scc: invalid arguments");
+    return -1;
+  }
+  b->dev.max_iter = max_iter;
+  b->dev.econv = econv;
+  b->dev.pconv = pconv;
+  b->dev.mix_alpha = mixing;
+  if (b->graph_exec) {
+    cudaGraphExecDestroy(b->graph_exec);
+    cudaGraphDestroy(b->graph);
+    b->graph_exec = nullptr;
+    b->graph = nullptr;
+  }
+  return 0;
+}
+
+int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass) {
+  if (!b) return -1;
+  size_t n3 = sizeof(double) * 3 * b->natom;
+  if (xyz) CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));
+  if (vel) CK(cudaMemcpyAsync(b->d_vel, vel, n3, cudaMemcpyHostToDevice, b->stream));
+  if (mass) CK(cudaMemcpyAsync(b->d_mass, mass, sizeof(double) * b->natom, cudaMemcpyHostToDevice, b->stream));
+  return 0;
+}
+
+int qcx_batch_egrad(qcx_batch* b) {
+  if (!b) return -1;
+  enqueue_egrad(b);
+  b->launches = kEgradLaunches;
+  return check_launch();
+}
+
+int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
+  if (!b || nsteps < 0) return -1;
+  if (!b->graph_exec || b->graph_tstep != tstep) {
+    if (b->graph_exec) {
+      cudaGraphExecDestroy(b->graph_exec);
+      cudaGraphDestroy(b->graph);
+      b->graph_exec = nullptr;
+      b->graph = nullptr;
+    }
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    launch_leapfrog(b->dev, tstep, b->stream);
+    enqueue_egrad(b);
+    CK(cudaStreamEndCapture(b->stream, &b->graph));
+    CK(cudaGraphInstantiate(&b->graph_exec, b->graph, 0));
+    b->graph_tstep = tstep;
+  }
+  for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(b->graph_exec, b->stream));
+  b->launches = (long long)nsteps * (kEgradLaunches + 1);
+  return check_launch();
+}
+
+int qcx_batch_get(qcx_batch* b, double* xyz, double* vel, double* grad, double* energy, double* qat, double* ekin,
+                  int32_t* status, int32_t* iters) {
+  if (!b) return -1;
+  size_t n3 = sizeof(double) * 3 * b->natom;
+  if (xyz) CK(cudaMemcpyAsync(xyz, b->d_xyz, n3, cudaMemcpyDeviceToHost, b->stream));
+  if (vel) CK(cudaMemcpyAsync(vel, b->d_vel, n3, cudaMemcpyDeviceToHost, b->stream));
+  if (grad) CK(cudaMemcpyAsync(grad, b->d_grad, n3, cudaMemcpyDeviceToHost, b->stream));
+  if (qat) CK(cudaMemcpyAsync(qat, b->d_qat, sizeof(double) * b->natom, cudaMemcpyDeviceToHost, b->stream));
+  if (ekin) CK(cudaMemcpyAsync(ekin, b->d_ekin, sizeof(double) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  if (status) CK(cudaMemcpyAsync(status, b->d_status, sizeof(int) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  if (iters) CK(cudaMemcpyAsync(iters, b->d_iters, sizeof(int) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  if (energy) {
+    std::vector<double> e((size_t)b->nmol * kNumEnergy);
+    CK(cudaMemcpyAsync(e.data(), b->d_energy, sizeof(double) * e.size(), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    for (int m = 0; m < b->nmol; ++m) energy[m] = e[(size_t)m * kNumEnergy + kETotal];
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int qcx_batch_get_energy_terms(qcx_batch* b, int i, double* terms) {
+  if (!b || i < 0 || i >= b->nmol || !terms) return -1;
+  CK(cudaMemcpyAsync(terms, b->d_energy + (size_t)i * kNumEnergy, sizeof(double) * kNumEnergy,
+                     cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int qcx_batch_get_matrix(qcx_batch* b, int i, int which, double* out) {
+  if (!b || i < 0 || i >= b->nmol || which < 0 || which >= kNumMat || !out) return -1;
+  const MolDesc& md = b->mol[i];
+  const double* src = b->d_mats + md.mat_off + (long long)which * slot_size(md.nao);
+  CK(cudaMemcpyAsync(out, src, sizeof(double) * md.nao * md.nao, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return md.nao;
+}
+
+long long qcx_batch_kernel_launches(qcx_batch* b) { return b ? b->launches : -1; }
+
+int qcx_batch_sync(qcx_batch* b) {
+  if (!b) return -1;
+  CK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// single-structure drop-in with a per-process cache of the device state
+// ---------------------------------------------------------------------------
+int qcx_egrad(int method, int nat, const int32_t* num, const double* xyz, int charge, int multiplicity,
+              double etemp, double* energy, double* grad, double* qat) {
+  static std::mutex mtx;
+  static qcx_batch* cached = nullptr;
+  static std::vector<int> cached_num;
+  static double cached_charge = 0.0, cached_etemp = -1.0;
+  (void)multiplicity;
+  if (method != QCX_METHOD_GFN2) {
+    set_error("only the GFN2-xTB Hamiltonian is implemented");
+    return 5;
+  }
+  if (nat < 1 || !num || !xyz || !energy || !grad || !qat) {
+    set_error("qcx_egrad: invalid arguments");
+    return -1;
+  }
+  std::lock_guard<std::mutex> lock(mtx);
+  std::vector<int> key(num, num + nat);
+  if (!cached || key != cached_num || cached_charge != (double)charge || cached_etemp != etemp) {
+    if (cached) free_batch(cached);
+    int32_t n1 = nat;
+    double ch = charge, et = etemp;
+    cached = qcx_batch_create(1, &n1, num, &ch, &et);
+    if (!cached) return -1;
+    cached_num = key;
+    cached_charge = charge;
+    cached_etemp = etemp;
+  }
+  if (qcx_batch_set_state(cached, xyz, nullptr, nullptr)) return -1;
+  if (qcx_batch_egrad(cached)) return -1;
+  int32_t st = 0;
+  if (qcx_batch_get(cached, nullptr, nullptr, grad, energy, qat, nullptr, &st, nullptr)) return -1;
+  if (st != 0) {
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), "calculation failed, status bits 0x%x", st);
+    set_error(buf);
+    return -1;
+  }
+  return 0;
+}
+
+}  // extern "C"

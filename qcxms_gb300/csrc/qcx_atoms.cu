@@ -1,0 +1,347 @@
+// Atom-level kernels: coordination numbers, the pairwise/three-body gradient
+// terms with the coordination-number chain rule, and the leapfrog update.
+#include "qcx_batch.cuh"
+#include "qcx_kernels.h"
+
+namespace qcx {
+
+// ---------------------------------------------------------------------------
+// coordination numbers, multipole radii and dispersion reference weights
+// ---------------------------------------------------------------------------
+__global__ void k_cn(DevBatch bt) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= bt.natom) return;
+  const Params& P = *bt.prm;
+  const MolDesc md = bt.mol[bt.atom_mol[a]];
+  int za = bt.Z[a];
+  double xa = bt.xyz[3 * a], ya = bt.xyz[3 * a + 1], zz = bt.xyz[3 * a + 2];
+  double cn = 0.0, cnd = 0.0;
+  for (int b = md.atom_off; b < md.atom_off + md.nat; ++b) {
+    if (b == a) continue;
+    double dx = xa - bt.xyz[3 * b], dy = ya - bt.xyz[3 * b + 1], dz = zz - bt.xyz[3 * b + 2];
+    double r = sqrt(dx * dx + dy * dy + dz * dz);
+    double rc = P.rcov[za] + P.rcov[bt.Z[b]], f, df;
+    cn_exp_pair(r, rc, f, df);
+    cn += f;
+    cn_erf_pair(r, rc, f, df);
+    cnd += f;
+  }
+  bt.cn[a] = cn;
+  bt.cnd[a] = cnd;
+  double r, dr;
+  mpole_radius(P, za, cn, r, dr);
+  bt.mrad[a] = r;
+  bt.dmrad[a] = dr;
+  d4_weights(P, za, cnd, bt.w4 + (long long)a * kMaxRef, bt.dw4 + (long long)a * kMaxRef);
+}
+
+void launch_cn(const DevBatch& bt, cudaStream_t st) {
+  int threads = 128;
+  k_cn<<<(bt.natom + threads - 1) / threads, threads, 0, st>>>(bt);
+}
+
+__global__ void k_zero_grad(DevBatch bt) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= bt.natom) return;
+  bt.grad[3 * a] = 0.0;
+  bt.grad[3 * a + 1] = 0.0;
+  bt.grad[3 * a + 2] = 0.0;
+  bt.dedcn[a] = 0.0;
+  bt.dedcnd[a] = 0.0;
+}
+
+void launch_zero_grad(const DevBatch& bt, cudaStream_t st) {
+  int threads = 128;
+  k_zero_grad<<<(bt.natom + threads - 1) / threads, threads, 0, st>>>(bt);
+}
+
+// ---------------------------------------------------------------------------
+// per-molecule gradient assembly (one CTA per molecule)
+// ---------------------------------------------------------------------------
+constexpr int kAtomThreads = 256;
+
+__device__ inline double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < kAtomThreads / 32; ++i) s += red[i];
+  __syncthreads();
+  return s;
+}
+
+__global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
+  extern __shared__ __align__(16) double sm[];
+  const int mol = blockIdx.x;
+  const MolDesc md = bt.mol[mol];
+  if (bt.status[mol] & kCholeskyFailed) return;
+  const Params& P = *bt.prm;
+  const int nat = md.nat, nsh = md.nsh, n = md.nao;
+  const int off = md.atom_off;
+  VecLayout vl = VecLayout::make(nat, nsh, n, md.len, md.nmem);
+  const double* vec = bt.vecs + md.vec_off;
+  const double* xout = vec + vl.xout;
+  const double* qsh = xout;
+  const double* dp = xout + nsh;
+  const double* qp = xout + nsh + 3 * nat;
+  const double* qa = vec + vl.qat;
+  const double* zeta = vec + vl.zeta;
+  const double* gam = vec + vl.gam;
+  double* g = sm;                // [3 nat]
+  double* dcn = sm + 3 * nat;    // [nat]
+  double* dcnd = sm + 4 * nat;   // [nat]
+  double* red = sm + 5 * nat;    // [32]
+  const double* xyz = bt.xyz + 3LL * off;
+  const int* Z = bt.Z + off;
+  const int* sh_atom = bt.sh_atom + md.sh_off;
+  const int* sh_k = bt.sh_k + md.sh_off;
+  const int* sh_ao = bt.sh_ao + md.sh_off;
+  const double* Pm = mat_ptr(bt, md, kP);
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+    g[3 * a] = 0.0;
+    g[3 * a + 1] = 0.0;
+    g[3 * a + 2] = 0.0;
+    // on-site self-energy CN dependence
+    double d = 0.0;
+    for (int s = 0; s < nsh; ++s) {
+      if (sh_atom[s] - off != a) continue;
+      int l = P.sh_l[Z[a]][sh_k[s]];
+      for (int i = 0; i < 2 * l + 1; ++i) {
+        int mu = sh_ao[s] + i;
+        d += P.kcn[Z[a]][sh_k[s]] * Pm[(long long)mu * n + mu];
+      }
+    }
+    dcn[a] = d;
+    dcnd[a] = 0.0;
+  }
+  __syncthreads();
+  // (a) pair terms, one thread per atom, all partners (each pair visited twice)
+  double erep = 0.0;
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+    double ga[3] = {0, 0, 0}, dca = 0.0, dcda = 0.0;
+    int za = Z[a];
+    const double* ma = dp + 3 * a;
+    const double* ta = qp + 6 * a;
+    for (int b = 0; b < nat; ++b) {
+      if (b == a) continue;
+      int zb = Z[b];
+      double r[3] = {xyz[3 * a] - xyz[3 * b], xyz[3 * a + 1] - xyz[3 * b + 1], xyz[3 * a + 2] - xyz[3 * b + 2]};
+      double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+      double R = sqrt(r2);
+      double dEdR = 0.0;
+      // isotropic electrostatics
+      for (int s = 0; s < nsh; ++s) {
+        if (sh_atom[s] - off != a) continue;
+        for (int t = 0; t < nsh; ++t) {
+          if (sh_atom[t] - off != b) continue;
+          double gm = gam[s * nsh + t];
+          dEdR += qsh[s] * qsh[t] * (-R * gm * gm * gm);
+        }
+      }
+      // dispersion (two-body): E = -zeta_a zeta_b C6_ab g_ab
+      double gd, dgd;
+      bj_kernel(P, za, zb, R, gd, dgd);
+      double c6 = 0.0, dc6a = 0.0;
+      const double* wa = bt.w4 + (long long)(off + a) * kMaxRef;
+      const double* dwa = bt.dw4 + (long long)(off + a) * kMaxRef;
+      const double* wb = bt.w4 + (long long)(off + b) * kMaxRef;
+      for (int i = 0; i < P.d4_nref[za]; ++i)
+        for (int j = 0; j < P.d4_nref[zb]; ++j) {
+          double cr = c6ref(P, za, i, zb, j);
+          c6 += wa[i] * wb[j] * cr;
+          dc6a += dwa[i] * wb[j] * cr;
+        }
+      double zz = zeta[a] * zeta[b];
+      dEdR += -zz * c6 * dgd;
+      dcda += -zz * gd * dc6a;
+      // repulsion
+      {
+        double al = sqrt(P.rep_alpha[za] * P.rep_alpha[zb]);
+        double rk = pow(R, QCX_REP_KEXP);
+        double v = P.rep_zeff[za] * P.rep_zeff[zb] / R * exp(-al * rk);
+        erep += 0.5 * v;
+        dEdR += v * (-1.0 / R - QCX_REP_KEXP * al * rk / R);
+      }
+      // anisotropic electrostatics
+      long long ab = (long long)a * nat + b;
+      double f3 = vec[vl.f3 + ab], f5 = vec[vl.f5 + ab];
+      double d3r = vec[vl.d3r + ab], d3r0 = vec[vl.d3r0 + ab], d5r = vec[vl.d5r + ab], d5r0 = vec[vl.d5r0 + ab];
+      const double* mb = dp + 3 * b;
+      const double* tb = qp + 6 * b;
+      double mar = ma[0] * r[0] + ma[1] * r[1] + ma[2] * r[2];
+      double mbr = mb[0] * r[0] + mb[1] * r[1] + mb[2] * r[2];
+      double mab = ma[0] * mb[0] + ma[1] * mb[1] + ma[2] * mb[2];
+      double rr[6] = {r[0] * r[0], r[1] * r[1], r[2] * r[2], 2 * r[0] * r[1], 2 * r[0] * r[2], 2 * r[1] * r[2]};
+      double rta = 0, rtb = 0;
+      for (int q = 0; q < 6; ++q) {
+        rta += ta[q] * rr[q];
+        rtb += tb[q] * rr[q];
+      }
+      double s1 = qa[a] * mbr - qa[b] * mar;
+      double s2 = qa[a] * rtb + qa[b] * rta + mab * r2 - 3.0 * mar * mbr;
+      double tar[3], tbr[3];
+      tar[0] = ta[0] * r[0] + ta[3] * r[1] + ta[4] * r[2];
+      tar[1] = ta[3] * r[0] + ta[1] * r[1] + ta[5] * r[2];
+      tar[2] = ta[4] * r[0] + ta[5] * r[1] + ta[2] * r[2];
+      tbr[0] = tb[0] * r[0] + tb[3] * r[1] + tb[4] * r[2];
+      tbr[1] = tb[3] * r[0] + tb[1] * r[1] + tb[5] * r[2];
+      tbr[2] = tb[4] * r[0] + tb[5] * r[1] + tb[2] * r[2];
+      for (int k = 0; k < 3; ++k) {
+        double ds2 = 2.0 * qa[a] * tbr[k] + 2.0 * qa[b] * tar[k] + 2.0 * mab * r[k] - 3.0 * (mbr * ma[k] + mar * mb[k]);
+        ga[k] += (d3r * s1 + d5r * s2 + dEdR) * r[k] / R + f3 * (qa[a] * mb[k] - qa[b] * ma[k]) + f5 * ds2;
+      }
+      dca += (d3r0 * s1 + d5r0 * s2) * 0.5 * bt.dmrad[off + a];
+    }
+    g[3 * a] += ga[0];
+    g[3 * a + 1] += ga[1];
+    g[3 * a + 2] += ga[2];
+    dcn[a] += dca;
+    dcnd[a] += dcda;
+  }
+  __syncthreads();
+  // (b) three-body dispersion, one thread per ordered triple a > b > c
+  double eatm = 0.0;
+  long long ntrip = (long long)nat * nat * nat;
+  for (long long t = threadIdx.x; t < ntrip; t += blockDim.x) {
+    int a = (int)(t / ((long long)nat * nat)), b = (int)((t / nat) % nat), c = (int)(t % nat);
+    if (!(a > b && b > c)) continue;
+    int za = Z[a], zb = Z[b], zc = Z[c];
+    double rab[3], rbc[3], rca[3], x = 0, y = 0, z = 0;
+    for (int k = 0; k < 3; ++k) {
+      rab[k] = xyz[3 * a + k] - xyz[3 * b + k];
+      rbc[k] = xyz[3 * b + k] - xyz[3 * c + k];
+      rca[k] = xyz[3 * c + k] - xyz[3 * a + k];
+      x += rab[k] * rab[k];
+      y += rbc[k] * rbc[k];
+      z += rca[k] * rca[k];
+    }
+    const double* w[3] = {bt.w4 + (long long)(off + a) * kMaxRef, bt.w4 + (long long)(off + b) * kMaxRef,
+                          bt.w4 + (long long)(off + c) * kMaxRef};
+    const double* dw[3] = {bt.dw4 + (long long)(off + a) * kMaxRef, bt.dw4 + (long long)(off + b) * kMaxRef,
+                           bt.dw4 + (long long)(off + c) * kMaxRef};
+    int zs[3] = {za, zb, zc};
+    // C6 of the three pairs and their CN' derivatives: pair (i,j) for (0,1),(1,2),(2,0)
+    double c6p[3], dc6[3][2];
+    const int pi[3] = {0, 1, 2}, pj[3] = {1, 2, 0};
+    for (int pr = 0; pr < 3; ++pr) {
+      int i0 = pi[pr], j0 = pj[pr];
+      double s = 0.0, di = 0.0, dj = 0.0;
+      for (int ii = 0; ii < P.d4_nref[zs[i0]]; ++ii)
+        for (int jj = 0; jj < P.d4_nref[zs[j0]]; ++jj) {
+          double cr = c6ref(P, zs[i0], ii, zs[j0], jj);
+          s += w[i0][ii] * w[j0][jj] * cr;
+          di += dw[i0][ii] * w[j0][jj] * cr;
+          dj += w[i0][ii] * dw[j0][jj] * cr;
+        }
+      c6p[pr] = s;
+      dc6[pr][0] = di;
+      dc6[pr][1] = dj;
+    }
+    double c9 = QCX_D4_S9 * sqrt(c6p[0] * c6p[1] * c6p[2]);
+    double r0 = cbrt(bj_radius(P, za, zb) * bj_radius(P, zb, zc) * bj_radius(P, zc, za));
+    double rrr = sqrt(x) * sqrt(y) * sqrt(z);
+    double rbar = cbrt(rrr);
+    double alp3 = QCX_ATM_ALP / 3.0;
+    double tt = 6.0 * pow(r0 / rbar, alp3);
+    double fd = 1.0 / (1.0 + tt);
+    double u1 = x + z - y, u2 = x + y - z, u3 = y + z - x;
+    double num = u1 * u2 * u3;
+    double den = 8.0 * x * y * z;
+    double ang = 3.0 * num / den + 1.0;
+    double r3 = rrr * rrr * rrr;
+    double h = fd / r3;
+    double en = c9 * ang * h;
+    eatm += en;
+    double dnx = u2 * u3 + u1 * u3 - u1 * u2;
+    double dny = -u2 * u3 + u1 * u3 + u1 * u2;
+    double dnz = u2 * u3 - u1 * u3 + u1 * u2;
+    double dlnh = fd * tt * alp3 - 9.0;
+    double ex = c9 * (3.0 * (dnx / den - num / (den * x)) * h + ang * h * dlnh / (6.0 * x));
+    double ey = c9 * (3.0 * (dny / den - num / (den * y)) * h + ang * h * dlnh / (6.0 * y));
+    double ez = c9 * (3.0 * (dnz / den - num / (den * z)) * h + ang * h * dlnh / (6.0 * z));
+    for (int k = 0; k < 3; ++k) {
+      double gx = 2.0 * ex * rab[k], gy = 2.0 * ey * rbc[k], gz = 2.0 * ez * rca[k];
+      atomicAdd(&g[3 * a + k], gx - gz);
+      atomicAdd(&g[3 * b + k], -gx + gy);
+      atomicAdd(&g[3 * c + k], -gy + gz);
+    }
+    // d ln C9 / d CN'_p = 1/2 sum over the two pairs containing p of dC6/C6
+    double da = 0.5 * (dc6[0][0] / c6p[0] + dc6[2][1] / c6p[2]);
+    double db = 0.5 * (dc6[0][1] / c6p[0] + dc6[1][0] / c6p[1]);
+    double dc = 0.5 * (dc6[1][1] / c6p[1] + dc6[2][0] / c6p[2]);
+    atomicAdd(&dcnd[a], en * da);
+    atomicAdd(&dcnd[b], en * db);
+    atomicAdd(&dcnd[c], en * dc);
+  }
+  __syncthreads();
+  // dedcn from the shell-pair kernel
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) dcn[a] += bt.dedcn[off + a];
+  __syncthreads();
+  // (c) coordination-number chain rule
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+    double ga[3] = {0, 0, 0};
+    for (int b = 0; b < nat; ++b) {
+      if (b == a) continue;
+      double r[3] = {xyz[3 * a] - xyz[3 * b], xyz[3 * a + 1] - xyz[3 * b + 1], xyz[3 * a + 2] - xyz[3 * b + 2]};
+      double R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+      double rc = P.rcov[Z[a]] + P.rcov[Z[b]], f, df1, df2;
+      cn_exp_pair(R, rc, f, df1);
+      cn_erf_pair(R, rc, f, df2);
+      double s = (dcn[a] + dcn[b]) * df1 + (dcnd[a] + dcnd[b]) * df2;
+      for (int k = 0; k < 3; ++k) ga[k] += s * r[k] / R;
+    }
+    for (int k = 0; k < 3; ++k) bt.grad[3LL * (off + a) + k] += g[3 * a + k] + ga[k];
+  }
+  erep = block_sum(erep, red);
+  eatm = block_sum(eatm, red);
+  if (threadIdx.x == 0) {
+    double* E = bt.energy + (long long)mol * kNumEnergy;
+    E[kEAtm] = eatm;
+    E[kERep] = erep;
+    E[kETotal] += eatm + erep;
+    if (!isfinite(E[kETotal])) bt.status[mol] |= kNonFinite;
+  }
+}
+
+void launch_grad_atoms(const DevBatch& bt, cudaStream_t st) {
+  // largest molecule bounds the shared memory: 5 nat + 32 doubles
+  size_t smem = sizeof(double) * (5 * (size_t)bt.max_nao + 64);
+  k_grad_atoms<<<bt.nmol, kAtomThreads, smem, st>>>(bt);
+}
+
+// ---------------------------------------------------------------------------
+// leapfrog step (src/md.f90:749-773) and kinetic energy, one CTA per molecule
+// ---------------------------------------------------------------------------
+__global__ void k_leapfrog(DevBatch bt, double tstep) {
+  __shared__ double red[32];
+  const int mol = blockIdx.x;
+  const MolDesc md = bt.mol[mol];
+  double ke = 0.0;
+  for (int i = threadIdx.x; i < 3 * md.nat; i += blockDim.x) {
+    long long e = 3LL * md.atom_off + i;
+    double mass = bt.mass[md.atom_off + i / 3];
+    double vold = bt.vel[e];
+    // explicit roundings: no FMA contraction, same operations as the reference loop
+    double vnew = __dsub_rn(vold, __ddiv_rn(__dmul_rn(tstep, bt.grad[e]), mass));
+    double vavg = __dmul_rn(0.5, __dadd_rn(vold, vnew));
+    bt.vel[e] = vnew;
+    bt.xyz[e] = __dadd_rn(bt.xyz[e], __dmul_rn(tstep, vnew));
+    ke += 0.5 * (mass * vavg * vavg);
+  }
+  for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = ke;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x / 32); ++i) s += red[i];
+    bt.ekin[mol] = s;
+  }
+}
+
+void launch_leapfrog(const DevBatch& bt, double tstep, cudaStream_t st) {
+  k_leapfrog<<<bt.nmol, 128, 0, st>>>(bt, tstep);
+}
+
+}  // namespace qcx

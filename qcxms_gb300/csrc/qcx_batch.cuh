@@ -1,0 +1,146 @@
+// Device layout of a batch of independent trajectories (one molecule each).
+//
+// All molecules of a batch live in flat pools; a MolDesc gives each
+// molecule's offsets. Per-molecule dense matrices are n x n row-major blocks
+// (n = number of atomic orbitals); indices inside a molecule are local.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "qcx_device.cuh"
+
+namespace qcx {
+
+// matrix slots inside a molecule's matrix block (each n*n doubles)
+enum MatSlot {
+  kS = 0, kH0, kX, kF, kT, kA, kV, kC, kP, kW,
+  kDm0, kDm1, kDm2,
+  kQm0, kQm1, kQm2, kQm3, kQm4, kQm5,
+  kNumMat
+};
+
+// per-molecule energy terms
+enum EnergySlot {
+  kEBand = 0, kEIes, kE3, kEAes, kEAxc, kEDisp, kEAtm, kERep, kETs, kETotal, kEFermi, kNumEnergy
+};
+
+// per-molecule status bits
+enum Status : int {
+  kOk = 0,
+  kSccNotConverged = 1,
+  kNonFinite = 2,
+  kCholeskyFailed = 4,
+  kEigenNotConverged = 8,
+};
+
+struct MolDesc {
+  int nat, nsh, nao, len;      // len = nsh + 9 nat (mixed moment vector)
+  int atom_off, sh_off;        // offsets into atom / shell arrays
+  int nmem;                    // Broyden history capacity
+  int pad_;
+  long long mat_off;           // offset (doubles) of the matrix block
+  long long vec_off;           // offset (doubles) of the vector block
+  double nel, kT, charge, pad2_;
+};
+
+// offsets inside a molecule's vector block
+struct VecLayout {
+  long long eps, focc, xin, xout, vsh, vdp, vqp, qat, vat, gam, c6g, f3, f5, d3r, d3r0, d5r, d5r0, zeta, dzeta,
+      bdf, bu, ba, bxl, bfl, bc, bm, total;
+  __host__ __device__ static VecLayout make(int nat, int nsh, int nao, int len, int nmem) {
+    VecLayout v;
+    long long o = 0;
+    auto take = [&o](long long n) {
+      long long r = o;
+      o += (n + 3) & ~3LL;  // keep 32-byte alignment
+      return r;
+    };
+    v.eps = take(nao);
+    v.focc = take(nao);
+    v.xin = take(len);
+    v.xout = take(len);
+    v.vsh = take(nsh);
+    v.vdp = take(3LL * nat);
+    v.vqp = take(6LL * nat);
+    v.qat = take(nat);
+    v.vat = take(nat);
+    v.gam = take((long long)nsh * nsh);
+    v.c6g = take((long long)nat * nat);
+    v.f3 = take((long long)nat * nat);
+    v.f5 = take((long long)nat * nat);
+    v.d3r = take((long long)nat * nat);
+    v.d3r0 = take((long long)nat * nat);
+    v.d5r = take((long long)nat * nat);
+    v.d5r0 = take((long long)nat * nat);
+    v.zeta = take(nat);
+    v.dzeta = take(nat);
+    v.bdf = take((long long)nmem * len);
+    v.bu = take((long long)nmem * len);
+    v.ba = take((long long)nmem * nmem);
+    v.bxl = take(len);
+    v.bfl = take(len);
+    v.bc = take(nmem);
+    v.bm = take((long long)nmem * nmem + nmem);
+    v.total = o;
+    return v;
+  }
+};
+
+struct ShellPair {
+  int s, t;  // global shell indices (same molecule)
+};
+
+// Pointers handed to every kernel of a batch (by value).
+struct DevBatch {
+  int nmol, natom, nshell, npair;
+  const Params* prm;
+  const MolDesc* mol;
+  // atoms (global index)
+  const int* Z;
+  const int* atom_mol;
+  double* xyz;     // [natom][3]
+  double* grad;    // [natom][3]
+  double* vel;     // [natom][3]
+  const double* mass;
+  double* cn;
+  double* cnd;
+  double* dedcn;
+  double* dedcnd;
+  double* mrad;
+  double* dmrad;
+  double* w4;      // [natom][kMaxRef]
+  double* dw4;     // [natom][kMaxRef]
+  double* qat;     // output atomic charges
+  // shells (global index)
+  const int* sh_atom;  // global atom index
+  const int* sh_k;     // shell index within the element
+  const int* sh_ao;    // local AO offset within the molecule
+  // shell pairs (ordered, both directions, same molecule)
+  const ShellPair* pairs;
+  // pools
+  double* mats;
+  double* vecs;
+  double* energy;  // [nmol][kNumEnergy]
+  int* status;     // [nmol]
+  int* iters;      // [nmol]
+  double* ekin;    // [nmol]
+  int max_nao;
+  int smem_bytes;  // dynamic shared memory granted to the SCC kernel
+  // SCC controls
+  int max_iter;
+  double econv, pconv, mix_alpha;
+};
+
+// every matrix slot holds np*np doubles, np = nao rounded up to even, so the
+// padded Jacobi matrices fit in a slot; S, H0, ... use leading dimension nao.
+__host__ __device__ inline long long slot_size(int nao) {
+  long long np = nao + (nao & 1);
+  return np * np;
+}
+
+__host__ __device__ inline double* mat_ptr(const DevBatch& b, const MolDesc& m, int slot) {
+  return b.mats + m.mat_off + (long long)slot * slot_size(m.nao);
+}
+
+}  // namespace qcx

@@ -1,0 +1,863 @@
+// Self-consistent-charge loop: one CTA per molecule runs the whole SCC
+// (potentials, Fock build, generalized eigensolve, Fermi smearing, density,
+// Mulliken moments, modified Broyden mixing) without returning to the host,
+// so a batch of uneven molecules advances in one launch and molecules that
+// converge early simply retire their CTA.
+//
+// Generalized eigenproblem F C = S C e: S = L L^T (Cholesky, once per
+// geometry), X = L^-T, A = X^T F X, cyclic parallel Jacobi on A (round-robin
+// pair ordering, n/2 disjoint rotations per round), C = X V.
+#include <cfloat>
+
+#include "qcx_batch.cuh"
+#include "qcx_kernels.h"
+
+namespace qcx {
+
+constexpr int kSccThreads = 512;
+constexpr int kWarps = kSccThreads / 32;
+
+// ---------------------------------------------------------------------------
+// CTA helpers
+// ---------------------------------------------------------------------------
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ inline double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Sum K values over the CTA; result valid in all threads. red: K*kWarps doubles.
+template <int K>
+__device__ void cta_sum(double (&v)[K], double* red) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double s = warp_sum(v[k]);
+    if (lane == 0) red[k * kWarps + w] = s;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double s = 0.0;
+    for (int i = 0; i < kWarps; ++i) s += red[k * kWarps + i];
+    v[k] = s;
+  }
+  __syncthreads();
+}
+
+__device__ double cta_max(double v, double* red) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double s = warp_max(v);
+  if (lane == 0) red[w] = s;
+  __syncthreads();
+  double m = red[0];
+  for (int i = 1; i < kWarps; ++i) m = fmax(m, red[i]);
+  __syncthreads();
+  return m;
+}
+
+// C[M][N] = op(A) op(B), row-major, FP64. ta: A is stored K x M; tb: B is stored N x K.
+__device__ void cta_gemm(int M, int N, int K, const double* A, int lda, bool ta, const double* B, int ldb, bool tb,
+                         double* C, int ldc) {
+  int tilesM = (M + 1) / 2, tilesN = (N + 1) / 2;
+  for (int t = threadIdx.x; t < tilesM * tilesN; t += blockDim.x) {
+    int i0 = (t / tilesN) * 2, j0 = (t % tilesN) * 2;
+    double c00 = 0, c01 = 0, c10 = 0, c11 = 0;
+    bool i1ok = i0 + 1 < M, j1ok = j0 + 1 < N;
+    int i1 = i1ok ? i0 + 1 : i0, j1 = j1ok ? j0 + 1 : j0;
+    for (int k = 0; k < K; ++k) {
+      double a0 = ta ? A[(long long)k * lda + i0] : A[(long long)i0 * lda + k];
+      double a1 = ta ? A[(long long)k * lda + i1] : A[(long long)i1 * lda + k];
+      double b0 = tb ? B[(long long)j0 * ldb + k] : B[(long long)k * ldb + j0];
+      double b1 = tb ? B[(long long)j1 * ldb + k] : B[(long long)k * ldb + j1];
+      c00 = fma(a0, b0, c00);
+      c01 = fma(a0, b1, c01);
+      c10 = fma(a1, b0, c10);
+      c11 = fma(a1, b1, c11);
+    }
+    C[(long long)i0 * ldc + j0] = c00;
+    if (j1ok) C[(long long)i0 * ldc + j1] = c01;
+    if (i1ok) {
+      C[(long long)i1 * ldc + j0] = c10;
+      if (j1ok) C[(long long)i1 * ldc + j1] = c11;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory layout
+// ---------------------------------------------------------------------------
+struct SccShared {
+  int* ao_sh;      // [n] local shell of each AO
+  int* ao_at;      // [n] local atom of each AO
+  int* perm;       // [np]
+  int* rp;         // [np/2] rotation pair p
+  int* rq;         // [np/2] rotation pair q
+  double* rc;      // [np/2]
+  double* rs;      // [np/2]
+  double* mom;     // [10][n] per-AO moment partials
+  double* red;     // [16*kWarps] reductions
+  double* scal;    // [32] scalars
+  double* jac;     // Jacobi region (A, maybe V)
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+__host__ __device__ inline size_t scc_fixed_bytes(int n) {
+  int np = n + (n & 1);
+  size_t b = 0;
+  b += align16(sizeof(int) * n) * 2;
+  b += align16(sizeof(int) * np);
+  b += align16(sizeof(int) * (np / 2)) * 2;
+  b += align16(sizeof(double) * (np / 2)) * 2;
+  b += align16(sizeof(double) * 10 * n);
+  b += align16(sizeof(double) * 16 * kWarps);
+  b += align16(sizeof(double) * 32);
+  return b;
+}
+
+constexpr size_t kSmemCap = 220 * 1024;
+
+// Jacobi storage mode for a molecule with n AOs given the granted dynamic
+// shared memory: 0 = A and V in shared memory, 1 = A shared / V global,
+// 2 = both global (L2 resident).
+__host__ __device__ inline int jacobi_mode(int n, size_t granted) {
+  int np = n + (n & 1);
+  size_t fixed = scc_fixed_bytes(n);
+  size_t m2 = sizeof(double) * (size_t)np * np;
+  if (fixed + 2 * m2 <= granted) return 0;
+  if (fixed + m2 <= granted) return 1;
+  return 2;
+}
+
+size_t scc_smem_bytes(int max_nao, int precision) {
+  (void)precision;
+  int n = max_nao;
+  int np = n + (n & 1);
+  size_t want = scc_fixed_bytes(n) + 2 * sizeof(double) * (size_t)np * np;
+  return want < kSmemCap ? want : kSmemCap;
+}
+
+__device__ SccShared carve(char* base, int n) {
+  int np = n + (n & 1);
+  SccShared s;
+  size_t o = 0;
+  s.ao_sh = (int*)(base + o); o += align16(sizeof(int) * n);
+  s.ao_at = (int*)(base + o); o += align16(sizeof(int) * n);
+  s.perm = (int*)(base + o); o += align16(sizeof(int) * np);
+  s.rp = (int*)(base + o); o += align16(sizeof(int) * (np / 2));
+  s.rq = (int*)(base + o); o += align16(sizeof(int) * (np / 2));
+  s.rc = (double*)(base + o); o += align16(sizeof(double) * (np / 2));
+  s.rs = (double*)(base + o); o += align16(sizeof(double) * (np / 2));
+  s.mom = (double*)(base + o); o += align16(sizeof(double) * 10 * n);
+  s.red = (double*)(base + o); o += align16(sizeof(double) * 16 * kWarps);
+  s.scal = (double*)(base + o); o += align16(sizeof(double) * 32);
+  s.jac = (double*)(base + o);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// electrostatic + dispersion potentials of a moment vector x
+// ---------------------------------------------------------------------------
+struct MolView {
+  const DevBatch* bt;
+  MolDesc md;
+  VecLayout vl;
+  double* vec;
+  const int* Z;      // Z of local atoms (pointer offset)
+  const double* xyz;  // local atoms
+};
+
+// energies: [0]=ies [1]=e3 [2]=aes [3]=axc [4]=disp
+__device__ void potentials(const MolView& mv, const double* x, double* en, double* red) {
+  const Params& P = *mv.bt->prm;
+  const int nat = mv.md.nat, nsh = mv.md.nsh;
+  const double* qsh = x;
+  const double* dp = x + nsh;
+  const double* qp = x + nsh + 3 * nat;
+  double* vec = mv.vec;
+  double* qat = vec + mv.vl.qat;
+  double* vat = vec + mv.vl.vat;
+  double* vsh = vec + mv.vl.vsh;
+  double* vdp = vec + mv.vl.vdp;
+  double* vqp = vec + mv.vl.vqp;
+  double* zeta = vec + mv.vl.zeta;
+  double* dzeta = vec + mv.vl.dzeta;
+  const double* gam = vec + mv.vl.gam;
+  const double* c6g = vec + mv.vl.c6g;
+  const double* f3m = vec + mv.vl.f3;
+  const double* f5m = vec + mv.vl.f5;
+  const int* sh_k = mv.bt->sh_k + mv.md.sh_off;
+  const int* sh_atom = mv.bt->sh_atom + mv.md.sh_off;
+  const int aoff = mv.md.atom_off;
+  // atomic charges and charge scaling
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+    double q = 0.0;
+    for (int s = 0; s < nsh; ++s)
+      if (sh_atom[s] - aoff == a) q += qsh[s];
+    qat[a] = q;
+    double zt, dzt;
+    d4_zeta(P, mv.Z[a], q, zt, dzt);
+    zeta[a] = zt;
+    dzeta[a] = dzt;
+  }
+  __syncthreads();
+  double e[5] = {0, 0, 0, 0, 0};
+  // atom-resolved terms: multipoles, XC kernels, dispersion
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+    double va = 0.0, vd[3] = {0, 0, 0}, vq[6] = {0, 0, 0, 0, 0, 0};
+    const double* ma = dp + 3 * a;
+    const double* ta = qp + 6 * a;
+    double eaes = 0.0, sdisp = 0.0;
+    for (int b = 0; b < nat; ++b) {
+      if (b == a) continue;
+      double r[3] = {mv.xyz[3 * a] - mv.xyz[3 * b], mv.xyz[3 * a + 1] - mv.xyz[3 * b + 1],
+                     mv.xyz[3 * a + 2] - mv.xyz[3 * b + 2]};
+      double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+      double f3 = f3m[a * nat + b], f5 = f5m[a * nat + b];
+      const double* mb = dp + 3 * b;
+      const double* tb = qp + 6 * b;
+      double mar = ma[0] * r[0] + ma[1] * r[1] + ma[2] * r[2];
+      double mbr = mb[0] * r[0] + mb[1] * r[1] + mb[2] * r[2];
+      double mab = ma[0] * mb[0] + ma[1] * mb[1] + ma[2] * mb[2];
+      double rr[6] = {r[0] * r[0], r[1] * r[1], r[2] * r[2], 2 * r[0] * r[1], 2 * r[0] * r[2], 2 * r[1] * r[2]};
+      double rta = 0, rtb = 0;
+      for (int q = 0; q < 6; ++q) {
+        rta += ta[q] * rr[q];
+        rtb += tb[q] * rr[q];
+      }
+      eaes += f3 * (qat[a] * mbr - qat[b] * mar) + f5 * (qat[a] * rtb + qat[b] * rta + mab * r2 - 3.0 * mar * mbr);
+      va += f3 * mbr + f5 * rtb;
+      for (int k = 0; k < 3; ++k) vd[k] += -f3 * qat[b] * r[k] + f5 * (mb[k] * r2 - 3.0 * mbr * r[k]);
+      for (int q = 0; q < 6; ++q) vq[q] += f5 * qat[b] * rr[q];
+      sdisp += zeta[b] * c6g[a * nat + b];
+    }
+    int z = mv.Z[a];
+    double fd = P.aes_dk[z], fq = P.aes_qk[z];
+    double eaxc = fd * (ma[0] * ma[0] + ma[1] * ma[1] + ma[2] * ma[2]) +
+                  fq * (ta[0] * ta[0] + ta[1] * ta[1] + ta[2] * ta[2] + 2.0 * (ta[3] * ta[3] + ta[4] * ta[4] + ta[5] * ta[5]));
+    for (int k = 0; k < 3; ++k) vd[k] += 2.0 * fd * ma[k];
+    for (int q = 0; q < 3; ++q) vq[q] += 2.0 * fq * ta[q];
+    for (int q = 3; q < 6; ++q) vq[q] += 4.0 * fq * ta[q];
+    va += -dzeta[a] * sdisp;
+    vat[a] = va;
+    for (int k = 0; k < 3; ++k) vdp[3 * a + k] = vd[k];
+    for (int q = 0; q < 6; ++q) vqp[6 * a + q] = vq[q];
+    e[2] += 0.5 * eaes;
+    e[3] += eaxc;
+    e[4] += -0.5 * zeta[a] * sdisp;
+  }
+  __syncthreads();
+  // shell-resolved isotropic electrostatics and third order
+  for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
+    double v = 0.0;
+    for (int t = 0; t < nsh; ++t) v += gam[s * nsh + t] * qsh[t];
+    int a = sh_atom[s] - aoff;
+    double g3 = P.gamma3[mv.Z[a]][sh_k[s]];
+    e[0] += 0.5 * qsh[s] * v;
+    e[1] += g3 * qsh[s] * qsh[s] * qsh[s] / 3.0;
+    vsh[s] = v + g3 * qsh[s] * qsh[s] + vat[a];
+  }
+  cta_sum<5>(e, red);
+  for (int k = 0; k < 5; ++k) en[k] = e[k];
+}
+
+// ---------------------------------------------------------------------------
+// cyclic parallel Jacobi on the symmetric np x np matrix A (lda = np);
+// Vt (ld = np) accumulates eigenvectors as rows. Returns sweeps used.
+// ---------------------------------------------------------------------------
+__device__ int jacobi(double* A, double* Vt, int n, SccShared& sh, int max_sweeps) {
+  const int np = n + (n & 1);
+  const int half = np / 2;
+  const int m = np - 1;
+  for (int i = threadIdx.x; i < np * np; i += blockDim.x) {
+    int r = i / np, c = i % np;
+    Vt[i] = (r == c) ? 1.0 : 0.0;
+    if (r >= n || c >= n) A[i] = 0.0;
+  }
+  __syncthreads();
+  double amax = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) amax = fmax(amax, fabs(A[i * np + i]));
+  amax = cta_max(amax, sh.red);
+  const double tol = 1e-12 * fmax(1.0, amax);
+  int sweep;
+  for (sweep = 0; sweep < max_sweeps; ++sweep) {
+    double offmax = 0.0;
+    for (int r = 0; r < m; ++r) {
+      for (int k = threadIdx.x; k < half; k += blockDim.x) {
+        int p, q;
+        if (k == 0) {
+          p = m;
+          q = r;
+        } else {
+          p = (r + k) % m;
+          q = (r - k + m) % m;
+        }
+        if (p > q) {
+          int t = p;
+          p = q;
+          q = t;
+        }
+        double apq = A[p * np + q];
+        double c = 1.0, s = 0.0;
+        offmax = fmax(offmax, fabs(apq));
+        if (fabs(apq) > 1e-300) {
+          double app = A[p * np + p], aqq = A[q * np + q];
+          double theta = (aqq - app) / (2.0 * apq);
+          double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
+          c = 1.0 / sqrt(1.0 + t * t);
+          s = t * c;
+        }
+        sh.rp[k] = p;
+        sh.rq[k] = q;
+        sh.rc[k] = c;
+        sh.rs[k] = s;
+      }
+      __syncthreads();
+      // rows of A and of Vt
+      for (int i = threadIdx.x; i < half * np; i += blockDim.x) {
+        int k = i / np, j = i % np;
+        double c = sh.rc[k], s = sh.rs[k];
+        if (s == 0.0) continue;
+        int p = sh.rp[k], q = sh.rq[k];
+        double ap = A[p * np + j], aq = A[q * np + j];
+        A[p * np + j] = c * ap - s * aq;
+        A[q * np + j] = s * ap + c * aq;
+        double vp = Vt[p * np + j], vq = Vt[q * np + j];
+        Vt[p * np + j] = c * vp - s * vq;
+        Vt[q * np + j] = s * vp + c * vq;
+      }
+      __syncthreads();
+      // columns of A
+      for (int i = threadIdx.x; i < half * np; i += blockDim.x) {
+        int k = i % half, j = i / half;
+        double c = sh.rc[k], s = sh.rs[k];
+        if (s == 0.0) continue;
+        int p = sh.rp[k], q = sh.rq[k];
+        double ap = A[j * np + p], aq = A[j * np + q];
+        A[j * np + p] = c * ap - s * aq;
+        A[j * np + q] = s * ap + c * aq;
+      }
+      __syncthreads();
+    }
+    offmax = cta_max(offmax, sh.red);
+    if (offmax <= tol) return sweep + 1;
+  }
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Fermi level by safeguarded Newton/bisection (one warp); returns -T S.
+// ---------------------------------------------------------------------------
+__device__ double fermi_warp(int n, const double* eps, double nel, double kT, double* focc, double* efermi) {
+  int lane = threadIdx.x & 31;
+  if (nel <= 0.0) {
+    for (int i = lane; i < n; i += 32) focc[i] = 0.0;
+    *efermi = eps[0];
+    return 0.0;
+  }
+  if (nel >= 2.0 * n) {
+    for (int i = lane; i < n; i += 32) focc[i] = 2.0;
+    *efermi = eps[n - 1];
+    return 0.0;
+  }
+  int ho = (int)ceil(nel / 2.0) - 1;
+  if (ho < 0) ho = 0;
+  int lu = ho + 1 < n ? ho + 1 : n - 1;
+  double lo = eps[0] - 1.0, hi = eps[n - 1] + 1.0;
+  double mu = 0.5 * (eps[ho] + eps[lu]);
+  for (int it = 0; it < QCX_FERMI_ITERS; ++it) {
+    double N = 0.0, dN = 0.0;
+    for (int i = lane; i < n; i += 32) {
+      double f = 1.0 / (1.0 + exp((eps[i] - mu) / kT));
+      N += 2.0 * f;
+      dN += 2.0 * f * (1.0 - f) / kT;
+    }
+    N = warp_sum(N);
+    dN = warp_sum(dN);
+    double r = N - nel;
+    if (fabs(r) < 1e-13 * (nel > 1.0 ? nel : 1.0)) break;
+    if (r < 0) lo = mu;
+    else hi = mu;
+    double mn = (dN > 1e-300) ? mu - r / dN : 0.5 * (lo + hi);
+    if (!(mn > lo && mn < hi)) mn = 0.5 * (lo + hi);
+    mu = mn;
+  }
+  double ts = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    double x = (eps[i] - mu) / kT, ax = fabs(x);
+    double fs = 1.0 / (1.0 + exp(ax));
+    double s = -(fs * ax + log1p(exp(-ax)));
+    focc[i] = 2.0 / (1.0 + exp(x));
+    ts += 2.0 * kT * s;
+  }
+  ts = warp_sum(ts);
+  *efermi = mu;
+  return ts;
+}
+
+// ---------------------------------------------------------------------------
+// modified Broyden update of x (len) given x_out; it = number of previous updates
+// ---------------------------------------------------------------------------
+__device__ void broyden(const MolView& mv, double* x, const double* xout, int it, double alpha, SccShared& sh) {
+  const int len = mv.md.len, nmem = mv.md.nmem;
+  double* vec = mv.vec;
+  double* df = vec + mv.vl.bdf;
+  double* u = vec + mv.vl.bu;
+  double* a = vec + mv.vl.ba;
+  double* xl = vec + mv.vl.bxl;
+  double* fl = vec + mv.vl.bfl;
+  double* cvec = vec + mv.vl.bc;
+  if (it == 0) {
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+      double f = xout[i] - x[i];
+      xl[i] = x[i];
+      fl[i] = f;
+      x[i] += alpha * f;
+    }
+    __syncthreads();
+    return;
+  }
+  int m = it - 1;
+  if (m >= nmem) m = nmem - 1;  // history full: overwrite the newest slot
+  double* dfm = df + (long long)m * len;
+  double* um = u + (long long)m * len;
+  double nrm[1] = {0.0};
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    double f = xout[i] - x[i];
+    double d = f - fl[i];
+    dfm[i] = d;
+    nrm[0] += d * d;
+  }
+  cta_sum<1>(nrm, sh.red);
+  double nr = sqrt(nrm[0]);
+  if (nr < 1e-300) nr = 1e-300;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    dfm[i] /= nr;
+    um[i] = alpha * dfm[i] + (x[i] - xl[i]) / nr;
+  }
+  __syncthreads();
+  int k = m + 1;
+  // a[j][m] = df_j . df_m ; c_j = df_j . f   (one warp per j)
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = w; j < k; j += kWarps) {
+    const double* dfj = df + (long long)j * len;
+    double s1 = 0.0, s2 = 0.0;
+    for (int i = lane; i < len; i += 32) {
+      s1 += dfj[i] * dfm[i];
+      s2 += dfj[i] * (xout[i] - x[i]);
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if (lane == 0) {
+      a[j * nmem + m] = s1;
+      a[m * nmem + j] = s1;
+      cvec[j] = s2;
+    }
+  }
+  __syncthreads();
+  // solve (w0^2 I + a) gamma = c by Gaussian elimination with partial pivoting (one warp)
+  double* Ms = vec + mv.vl.bm;
+  double* rhs = Ms + k * k;
+  for (int i = threadIdx.x; i < k * k; i += blockDim.x) {
+    int r = i / k, c = i % k;
+    Ms[i] = a[r * nmem + c] + (r == c ? QCX_BROYDEN_W0 * QCX_BROYDEN_W0 : 0.0);
+  }
+  for (int i = threadIdx.x; i < k; i += blockDim.x) rhs[i] = cvec[i];
+  __syncthreads();
+  if (w == 0) {
+    for (int col = 0; col < k; ++col) {
+      // pivot search
+      double best = -1.0;
+      int bi = col;
+      for (int r = col + lane; r < k; r += 32) {
+        double v = fabs(Ms[r * k + col]);
+        if (v > best) {
+          best = v;
+          bi = r;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (bi != col) {
+        for (int c = lane; c < k; c += 32) {
+          double t = Ms[col * k + c];
+          Ms[col * k + c] = Ms[bi * k + c];
+          Ms[bi * k + c] = t;
+        }
+        if (lane == 0) {
+          double t = rhs[col];
+          rhs[col] = rhs[bi];
+          rhs[bi] = t;
+        }
+      }
+      __syncwarp();
+      double piv = Ms[col * k + col];
+      for (int r = col + 1 + lane; r < k; r += 32) {
+        double f = Ms[r * k + col] / piv;
+        for (int c = col; c < k; ++c) Ms[r * k + c] -= f * Ms[col * k + c];
+        rhs[r] -= f * rhs[col];
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      for (int r = k - 1; r >= 0; --r) {
+        double s = rhs[r];
+        for (int c = r + 1; c < k; ++c) s -= Ms[r * k + c] * rhs[c];
+        rhs[r] = s / Ms[r * k + r];
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    double f = xout[i] - x[i];
+    double s = 0.0;
+    for (int j = 0; j < k; ++j) s += rhs[j] * u[(long long)j * len + i];
+    xl[i] = x[i];
+    fl[i] = f;
+    x[i] += alpha * f - s;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// the SCC kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
+  extern __shared__ __align__(16) char smem_raw[];
+  const int mol = blockIdx.x;
+  MolView mv;
+  mv.bt = &bt;
+  mv.md = bt.mol[mol];
+  const MolDesc& md = mv.md;
+  const int n = md.nao, nat = md.nat, nsh = md.nsh, len = md.len;
+  const int np = n + (n & 1);
+  mv.vl = VecLayout::make(nat, nsh, n, len, md.nmem);
+  mv.vec = bt.vecs + md.vec_off;
+  mv.Z = bt.Z + md.atom_off;
+  mv.xyz = bt.xyz + 3LL * md.atom_off;
+  const Params& P = *bt.prm;
+  SccShared sh = carve(smem_raw, n);
+  double* vec = mv.vec;
+  const long long nn = (long long)n * n;
+  double* S = mat_ptr(bt, md, kS);
+  double* H0 = mat_ptr(bt, md, kH0);
+  double* X = mat_ptr(bt, md, kX);
+  double* F = mat_ptr(bt, md, kF);
+  double* T = mat_ptr(bt, md, kT);
+  double* Ag = mat_ptr(bt, md, kA);
+  double* Vg = mat_ptr(bt, md, kV);
+  double* C = mat_ptr(bt, md, kC);
+  double* Pm = mat_ptr(bt, md, kP);
+  double* Wm = mat_ptr(bt, md, kW);
+  double* Dm = mat_ptr(bt, md, kDm0);
+  double* Qm = mat_ptr(bt, md, kQm0);
+  double* eps = vec + mv.vl.eps;
+  double* focc = vec + mv.vl.focc;
+  double* xin = vec + mv.vl.xin;
+  double* xout = vec + mv.vl.xout;
+  const int mode = jacobi_mode(n, (size_t)bt.smem_bytes);
+  // Jacobi working storage (np x np each): shared memory when it fits, else
+  // the A slot and the T slot (T is free once A = X^T F X is formed).
+  double* JA = (mode <= 1) ? sh.jac : Ag;
+  double* JV = (mode == 0) ? sh.jac + (long long)np * np : T;
+
+  // --- per-AO maps -------------------------------------------------------
+  const int* sh_atom = bt.sh_atom + md.sh_off;
+  const int* sh_ao = bt.sh_ao + md.sh_off;
+  const int* sh_k = bt.sh_k + md.sh_off;
+  for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
+    int a = sh_atom[s] - md.atom_off;
+    int l = P.sh_l[mv.Z[a]][sh_k[s]];
+    for (int i = 0; i < 2 * l + 1; ++i) {
+      sh.ao_sh[sh_ao[s] + i] = s;
+      sh.ao_at[sh_ao[s] + i] = a;
+    }
+  }
+  // --- geometry-dependent precomputation ------------------------------
+  for (int i = threadIdx.x; i < nsh * nsh; i += blockDim.x) {
+    int s = i / nsh, t = i % nsh;
+    int a = sh_atom[s] - md.atom_off, b = sh_atom[t] - md.atom_off;
+    double ea = P.hardness[mv.Z[a]][sh_k[s]], eb = P.hardness[mv.Z[b]][sh_k[t]];
+    double eta = 0.5 * (ea + eb);
+    double r2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      double d = mv.xyz[3 * a + k] - mv.xyz[3 * b + k];
+      r2 += d * d;
+    }
+    vec[mv.vl.gam + i] = 1.0 / sqrt(r2 + 1.0 / (eta * eta));
+  }
+  for (int i = threadIdx.x; i < nat * nat; i += blockDim.x) {
+    int a = i / nat, b = i % nat;
+    double c6g = 0.0, f3 = 0.0, f5 = 0.0, d3r = 0, d3r0 = 0, d5r = 0, d5r0 = 0;
+    if (a != b) {
+      int za = mv.Z[a], zb = mv.Z[b];
+      int ga = md.atom_off + a, gb = md.atom_off + b;
+      double r2 = 0;
+      for (int k = 0; k < 3; ++k) {
+        double d = mv.xyz[3 * a + k] - mv.xyz[3 * b + k];
+        r2 += d * d;
+      }
+      double r = sqrt(r2);
+      double c6 = 0.0;
+      for (int ii = 0; ii < P.d4_nref[za]; ++ii)
+        for (int jj = 0; jj < P.d4_nref[zb]; ++jj)
+          c6 += bt.w4[ga * kMaxRef + ii] * bt.w4[gb * kMaxRef + jj] * c6ref(P, za, ii, zb, jj);
+      double g, dg;
+      bj_kernel(P, za, zb, r, g, dg);
+      c6g = c6 * g;
+      double r0 = 0.5 * (bt.mrad[ga] + bt.mrad[gb]);
+      mp_kernel(3, QCX_AES_A3, r, r0, f3, d3r, d3r0);
+      mp_kernel(5, QCX_AES_A5, r, r0, f5, d5r, d5r0);
+    }
+    vec[mv.vl.c6g + i] = c6g;
+    vec[mv.vl.f3 + i] = f3;
+    vec[mv.vl.f5 + i] = f5;
+    vec[mv.vl.d3r + i] = d3r;
+    vec[mv.vl.d3r0 + i] = d3r0;
+    vec[mv.vl.d5r + i] = d5r;
+    vec[mv.vl.d5r0 + i] = d5r0;
+  }
+  double nel = md.nel;
+  // --- Cholesky S = L L^T (L stored in T, lower) -------------------------
+  for (long long i = threadIdx.x; i < nn; i += blockDim.x) T[i] = S[i];
+  __syncthreads();
+  int status = 0;
+  for (int j = 0; j < n; ++j) {
+    double djj = T[(long long)j * n + j];
+    if (!(djj > 0.0)) {
+      status |= kCholeskyFailed;
+      break;
+    }
+    double ljj = sqrt(djj);
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) T[(long long)i * n + j] /= ljj;
+    __syncthreads();
+    if (threadIdx.x == 0) T[(long long)j * n + j] = ljj;
+    int m = n - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      int i = j + 1 + e / m, k = j + 1 + e % m;
+      if (k <= i) T[(long long)i * n + k] -= T[(long long)i * n + j] * T[(long long)k * n + j];
+    }
+    __syncthreads();
+  }
+  if (status) {
+    if (threadIdx.x == 0) {
+      bt.status[mol] = status;
+      bt.iters[mol] = 0;
+    }
+    return;
+  }
+  // Linv (lower) by forward substitution, one column per thread; X = Linv^T
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    // X[j][i] = Linv[i][j]
+    X[(long long)j * n + j] = 1.0 / T[(long long)j * n + j];
+    for (int i = 0; i < j; ++i) X[(long long)j * n + i] = 0.0;
+    for (int i = j + 1; i < n; ++i) {
+      double s = 0.0;
+      for (int k = j; k < i; ++k) s -= T[(long long)i * n + k] * X[(long long)j * n + k];
+      X[(long long)j * n + i] = s / T[(long long)i * n + i];
+    }
+  }
+  // X currently holds Linv^T row j = column j of Linv -> X[j][i] = Linv[i][j] = (L^-T)[j][i]. Done.
+  for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = 0.0;
+  __syncthreads();
+
+  double en[5];
+  double eprev = 0.0, eel = 0.0, ets = 0.0, eband = 0.0, efermi = 0.0;
+  int it, converged = 0, eig_fail = 0;
+  for (it = 1; it <= bt.max_iter; ++it) {
+    potentials(mv, xin, en, sh.red);
+    // Fock matrix
+    {
+      const double* vsh = vec + mv.vl.vsh;
+      const double* vdp = vec + mv.vl.vdp;
+      const double* vqp = vec + mv.vl.vqp;
+      for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+        int i = (int)(e / n), j = (int)(e % n);
+        int A = sh.ao_at[i], B = sh.ao_at[j];
+        long long ji = (long long)j * n + i;
+        double f = H0[e] - 0.5 * S[e] * (vsh[sh.ao_sh[i]] + vsh[sh.ao_sh[j]]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f -= 0.5 * (vdp[3 * A + c] * Dm[c * nn + e] + vdp[3 * B + c] * Dm[c * nn + ji]);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) f -= 0.5 * (vqp[6 * A + c] * Qm[c * nn + e] + vqp[6 * B + c] * Qm[c * nn + ji]);
+        F[e] = f;
+      }
+    }
+    __syncthreads();
+    // A = X^T F X  (T = F X, then X^T T into the Jacobi matrix with ld np)
+    cta_gemm(n, n, n, F, n, false, X, n, false, T, n);
+    __syncthreads();
+    cta_gemm(n, n, n, X, n, true, T, n, false, JA, np);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      int i = e / n, j = e % n;
+      if (j < i) {
+        double s = 0.5 * (JA[i * np + j] + JA[j * np + i]);
+        JA[i * np + j] = s;
+        JA[j * np + i] = s;
+      }
+    }
+    __syncthreads();
+    int sweeps = jacobi(JA, JV, n, sh, 50);
+    if (sweeps < 0) eig_fail = 1;
+    // sort eigenvalues
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double di = JA[i * np + i];
+      int rank = 0;
+      for (int j = 0; j < n; ++j) {
+        double dj = JA[j * np + j];
+        rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
+      }
+      sh.perm[rank] = i;
+      eps[rank] = di;
+    }
+    __syncthreads();
+    // V (sorted eigenvectors as rows, ld n) into Vg; C = X V^T
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+      int k = (int)(e / n), l = (int)(e % n);
+      Vg[e] = JV[(long long)sh.perm[k] * np + l];
+    }
+    __syncthreads();
+    cta_gemm(n, n, n, X, n, false, Vg, n, true, C, n);
+    if (threadIdx.x < 32) {
+      double ef;
+      double ts = fermi_warp(n, eps, nel, md.kT, focc, &ef);
+      if (threadIdx.x == 0) {
+        sh.scal[0] = ts;
+        sh.scal[1] = ef;
+      }
+    }
+    __syncthreads();
+    ets = sh.scal[0];
+    efermi = sh.scal[1];
+    int nocc = 0;
+    for (int k = 0; k < n; ++k)
+      if (focc[k] > 0.0) nocc = k + 1;
+    // P = C f C^T
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+      int i = (int)(e / n), j = (int)(e % n);
+      if (j < i) continue;
+      double p = 0.0;
+      for (int k = 0; k < nocc; ++k) p += focc[k] * C[(long long)i * n + k] * C[(long long)j * n + k];
+      Pm[(long long)i * n + j] = p;
+      Pm[(long long)j * n + i] = p;
+    }
+    __syncthreads();
+    // moments: per-AO rows (one warp per row)
+    {
+      int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      for (int i = w; i < n; i += kWarps) {
+        double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int j = lane; j < n; j += 32) {
+          long long e = (long long)i * n + j;
+          double p = Pm[e];
+          acc[0] += p * S[e];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) acc[1 + c] += p * Dm[c * nn + e];
+#pragma unroll
+          for (int c = 0; c < 6; ++c) acc[4 + c] += p * Qm[c * nn + e];
+        }
+#pragma unroll
+        for (int c = 0; c < 10; ++c) acc[c] = warp_sum(acc[c]);
+        if (lane == 0)
+          for (int c = 0; c < 10; ++c) sh.mom[c * n + i] = acc[c];
+      }
+      __syncthreads();
+      for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
+        int a = sh_atom[s] - md.atom_off;
+        double q = P.refocc[mv.Z[a]][sh_k[s]];
+        int l = P.sh_l[mv.Z[a]][sh_k[s]];
+        for (int i = 0; i < 2 * l + 1; ++i) q -= sh.mom[sh_ao[s] + i];
+        xout[s] = q;
+      }
+      for (int t = threadIdx.x; t < 9 * nat; t += blockDim.x) {
+        int a = t / 9, c = t % 9;
+        double v = 0.0;
+        for (int i = 0; i < n; ++i)
+          if (sh.ao_at[i] == a) v -= sh.mom[(1 + c) * n + i];
+        if (c < 3) xout[nsh + 3 * a + c] = v;
+        else xout[nsh + 3 * nat + 6 * a + (c - 3)] = v;
+      }
+      __syncthreads();
+    }
+    potentials(mv, xout, en, sh.red);
+    {
+      double acc[2] = {0.0, 0.0};
+      for (long long e = threadIdx.x; e < nn; e += blockDim.x) acc[0] += Pm[e] * H0[e];
+      for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        double d = xout[i] - xin[i];
+        acc[1] += d * d;
+      }
+      cta_sum<2>(acc, sh.red);
+      eband = acc[0];
+      double res = sqrt(acc[1] / len);
+      eel = eband + en[0] + en[1] + en[2] + en[3] + en[4] + ets;
+      double de = fabs(eel - eprev);
+      eprev = eel;
+      if (it > 1 && de < bt.econv && res < bt.pconv) {
+        converged = 1;
+        break;
+      }
+    }
+    if (it == bt.max_iter) break;
+    broyden(mv, xin, xout, it - 1, bt.mix_alpha, sh);
+  }
+  if (it > bt.max_iter) it = bt.max_iter;
+  // energy-weighted density W = C f e C^T
+  int nocc = 0;
+  for (int k = 0; k < n; ++k)
+    if (focc[k] > 0.0) nocc = k + 1;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    int i = (int)(e / n), j = (int)(e % n);
+    if (j < i) continue;
+    double w = 0.0;
+    for (int k = 0; k < nocc; ++k) w += focc[k] * eps[k] * C[(long long)i * n + k] * C[(long long)j * n + k];
+    Wm[(long long)i * n + j] = w;
+    Wm[(long long)j * n + i] = w;
+  }
+  // outputs
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) bt.qat[md.atom_off + a] = vec[mv.vl.qat + a];
+  if (threadIdx.x == 0) {
+    double* E = bt.energy + (long long)mol * kNumEnergy;
+    E[kEBand] = eband;
+    E[kEIes] = en[0];
+    E[kE3] = en[1];
+    E[kEAes] = en[2];
+    E[kEAxc] = en[3];
+    E[kEDisp] = en[4];
+    E[kETs] = ets;
+    E[kEFermi] = efermi;
+    E[kETotal] = eel;  // electronic part; three-body and repulsion added by the gradient kernel
+    int st = 0;
+    if (!converged) st |= kSccNotConverged;
+    if (eig_fail) st |= kEigenNotConverged;
+    if (!isfinite(eel)) st |= kNonFinite;
+    bt.status[mol] = st;
+    bt.iters[mol] = it;
+  }
+}
+
+void launch_scc(const DevBatch& bt, int precision, cudaStream_t st) {
+  (void)precision;
+  static int configured = 0;
+  if (!configured) {
+    cudaFuncSetAttribute(k_scc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
+    configured = 1;
+  }
+  k_scc<<<bt.nmol, kSccThreads, bt.smem_bytes, st>>>(bt);
+}
+
+}  // namespace qcx

@@ -1,0 +1,43 @@
+"""The C ABI library builds for sm_103a, loads, and exports every declared symbol.
+
+No kernel is launched here (CPU-only checks)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+import qcxms_gb300
+from qcxms_gb300 import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "qcxgpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(qcx_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_builds_and_exports_all_symbols():
+    path = build.build()
+    assert os.path.exists(path)
+    lib = ctypes.CDLL(path)
+    syms = declared_symbols()
+    assert "qcx_egrad" in syms and "qcx_batch_step" in syms
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_host_side_validation_without_gpu():
+    lib = qcxms_gb300.load_library()
+    assert lib.qcx_version() >= 100
+    q, e, g, stat = qcxms_gb300.get_xtb_egrad([1, 1], np.zeros((2, 3)), 0, 1, method=qcxms_gb300.gfn1_xtb)
+    assert stat == 5
+    nat = np.array([1], dtype=np.int32)
+    Z = np.array([99], dtype=np.int32)
+    ch = np.zeros(1)
+    et = np.full(1, 300.0)
+    h = lib.qcx_batch_create(1, qcxms_gb300._ip(nat), qcxms_gb300._ip(Z), qcxms_gb300._dp(ch), qcxms_gb300._dp(et))
+    assert not h
+    assert b"1..18" in lib.qcx_last_error()

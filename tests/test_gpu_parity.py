@@ -1,0 +1,136 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU FP64 oracle.
+
+Tolerances (FP64 path): energies 1e-8 Eh, gradients 1e-7 Eh/Bohr, integrals
+1e-12; both sides run the same SCC algorithm and thresholds, so differences
+come only from floating-point summation order and the eigensolver."""
+import numpy as np
+import pytest
+
+import qcxms_gb300 as qg
+from qcxms_gb300 import constants, molgen
+from tests import molecules
+
+pytestmark = pytest.mark.gpu
+KT = 300.0 * constants.KB_AU
+
+
+def _batch(mols, etemp=300.0):
+    return qg.Batch([{"Z": Z, "xyz": xyz, "charge": c} for Z, xyz, c in mols], etemp=etemp)
+
+
+@pytest.mark.parametrize("name", sorted(molecules.ALL_SMALL))
+def test_energy_gradient_small(gpu, oracle_lib, name):
+    Z, xyz, c = molecules.ALL_SMALL[name]()
+    b = _batch([(Z, xyz, c)])
+    b.egrad()
+    r = b.get()
+    rc, e, g, q, info = oracle_lib.egrad(Z, xyz, c, kT=KT)
+    assert r["status"][0] == 0
+    assert abs(r["energy"][0] - e) < 1e-8
+    assert np.abs(r["grad"] - g).max() < 1e-7
+    assert np.abs(r["qat"] - q).max() < 1e-7
+    assert abs(int(r["iters"][0]) - info["iterations"]) <= 1
+
+
+def test_integrals_match_oracle(gpu, oracle_lib):
+    Z, xyz, c = molecules.h2s_ch_cation()
+    b = _batch([(Z, xyz, c)])
+    b.egrad()
+    S, H0, Dm, Qm, cn, cnd = oracle_lib.integrals(Z, xyz)
+    assert np.abs(b.matrix(0, 0) - S).max() < 1e-12
+    assert np.abs(b.matrix(0, 1) - H0).max() < 1e-12
+    P = oracle_lib.scc(Z, xyz, c, kT=KT)[0]
+    assert np.abs(b.matrix(0, 8) - P).max() < 1e-7
+
+
+def test_c6h12o2_and_random_batch(gpu, oracle_lib):
+    mols = [molecules.c6h12o2()] + [molecules.random_chno(n, s) for s, n in enumerate([5, 12, 23, 31, 40])]
+    b = _batch(mols)
+    b.egrad()
+    r = b.get()
+    g = b.split(r["grad"])
+    for i, (Z, xyz, c) in enumerate(mols):
+        rc, e, gref, q, info = oracle_lib.egrad(Z, xyz, c, kT=KT)
+        assert r["status"][i] == 0
+        assert abs(r["energy"][i] - e) < 1e-8, (i, r["energy"][i], e)
+        assert np.abs(g[i] - gref).max() < 1e-7
+
+
+def test_batch_equals_single_runs(gpu):
+    mols = [molecules.random_chno(n, 50 + n) for n in (7, 19, 33)]
+    b = _batch(mols)
+    b.egrad()
+    r = b.get()
+    for i, m in enumerate(mols):
+        s = _batch([m])
+        s.egrad()
+        rs = s.get()
+        assert abs(rs["energy"][0] - r["energy"][i]) < 1e-12
+        assert np.abs(rs["grad"] - b.split(r["grad"])[i]).max() < 1e-12
+
+
+def test_dropin_get_xtb_egrad(gpu, oracle_lib, tmp_path):
+    Z, xyz, c = molecules.c6h12o2()
+    out = tmp_path / "xtb.last"
+    q, e, g, stat = qg.get_xtb_egrad(Z, xyz, c, 2, qg.gfn2_xtb, 300.0, str(out))
+    assert stat == 0 and out.exists()
+    rc, e0, g0, q0, _ = oracle_lib.egrad(Z, xyz, c, kT=KT)
+    assert abs(e - e0) < 1e-8 and np.abs(g - g0).max() < 1e-7
+    # second call with moved atoms reuses the cached device state
+    xyz2 = xyz + 0.01
+    q, e2, g2, stat = qg.get_xtb_egrad(Z, xyz2, c, 2, qg.gfn2_xtb, 300.0)
+    rc, e1, g1, _, _ = oracle_lib.egrad(Z, xyz2, c, kT=KT)
+    assert stat == 0 and abs(e2 - e1) < 1e-8
+    assert qg.get_xtb_egrad(Z, xyz, c, 2, qg.gfn1_xtb, 300.0)[3] == 5
+
+
+def test_gpu_gradient_central_differences(gpu):
+    Z, xyz, c = molecules.ch2o_cation()
+    b = _batch([(Z, xyz, c)])
+    b.set_scc(100, 1e-12, 1e-10, 0.4)
+    b.egrad()
+    g = b.get()["grad"]
+    h = 1e-4
+    for a in range(len(Z)):
+        for k in range(3):
+            e = []
+            for sgn in (1, -1):
+                x = xyz.copy(); x[a, k] += sgn * h
+                b.set_state(xyz=x)
+                b.egrad()
+                e.append(b.get()["energy"][0])
+            assert abs((e[0] - e[1]) / (2 * h) - g[a, k]) < 1e-6
+
+
+def test_md_steps_match_oracle(gpu, oracle_lib):
+    mols = []
+    for s, n in enumerate([6, 14, 20]):
+        Z, xyz = molgen.random_chno(n, 200 + s)
+        mols.append({"Z": Z, "xyz": xyz, "vel": molgen.maxwell_boltzmann(Z, 1500.0, s), "mass": molgen.masses(Z),
+                     "charge": 1})
+    b = qg.Batch(mols)
+    b.egrad()
+    g0 = b.split(b.get()["grad"])
+    nsteps, dt = 10, 0.5 * constants.FSTOAU
+    b.step(nsteps, dt)
+    r = b.get()
+    fails, xyz, vel, grad, epot, iters = oracle_lib.md_batch(mols, nsteps, dt, g0, KT)
+    assert fails == 0
+    assert np.abs(r["xyz"] - xyz).max() < 1e-8
+    assert np.abs(r["vel"] - vel).max() < 1e-10
+    assert np.abs(r["energy"] - epot).max() < 1e-7
+    assert b.kernel_launches() == nsteps * 7
+
+
+def test_nve_energy_conservation(gpu):
+    Z, xyz = molgen.c6h12o2()
+    vel = molgen.maxwell_boltzmann(Z, 500.0, 1234)
+    b = qg.Batch([{"Z": Z, "xyz": xyz, "vel": vel, "mass": molgen.masses(Z), "charge": 1}])
+    b.egrad()
+    etot = []
+    for _ in range(10):
+        b.step(20, 0.5 * constants.FSTOAU)
+        r = b.get()
+        assert r["status"][0] == 0
+        etot.append(r["energy"][0] + r["ekin"][0])
+    assert max(etot) - min(etot) < 2e-3
