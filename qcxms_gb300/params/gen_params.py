@@ -124,10 +124,17 @@ def contracted_coeffs(alpha, craw, l):
     return c / math.sqrt(s)
 
 
-# Repulsion exponents of H, C, N, O, S chosen so that H2, CH4, NH3, H2O and H2S
-# have zero radial force at their textbook bond lengths (0.74, 1.09, 1.01,
-# 0.96, 1.34 Angstrom) with the rest of this parameter set.
-REP_ALPHA_FIT = {1: 2.105937, 6: 1.715302, 7: 2.175388, 8: 2.656783, 16: 0.834374}
+# The s-p and p-p H0 pair scalings, the repulsion exponents of H, C, N, O, S
+# and the p-shell H0 distance polynomials of C, N, O, S were least-squares
+# fitted so that
+# H2, CH4, NH3, H2O, H2S (X-H 0.74, 1.09, 1.01, 0.96, 1.34 Angstrom) and the
+# saturated dimers H3C-CH3, H2N-NH2, HO-OH, HS-SH (X-X 1.50, 1.45, 1.45,
+# 2.05 Angstrom) have zero bond-stretch force with the rest of this set.
+# (REP_ZEFF_FIT is unused: the default effective charges are kept.)
+REP_ZEFF_FIT = {}
+KPOLY_P_FIT = {6: -0.237795, 7: 0.658507, 8: -0.329019, 16: 0.081975}
+K_PAIR_FIT = {'pp': 1.202193, 'sp': 2.431030}
+REP_ALPHA_FIT = {1: 2.011406, 6: 1.421563, 7: 2.236515, 8: 2.149226, 16: 0.771833}
 
 # --------------------------------------------------------------------------
 # element rules
@@ -215,8 +222,8 @@ def main():
         ("QCX_KERF", 7.5, "steepness of the erf coordination number (dispersion)"),
         ("QCX_KEN", 0.02, "electronegativity scaling of H0 off-diagonals"),
         ("QCX_K_SS", 1.85, "H0 shell-pair scaling s-s"),
-        ("QCX_K_SP", 2.00, "H0 shell-pair scaling s-p"),
-        ("QCX_K_PP", 2.15, "H0 shell-pair scaling p-p"),
+        ("QCX_K_SP", K_PAIR_FIT.get("sp", 2.00), "H0 shell-pair scaling s-p"),
+        ("QCX_K_PP", K_PAIR_FIT.get("pp", 2.15), "H0 shell-pair scaling p-p"),
         ("QCX_K_XD", 2.00, "H0 shell-pair scaling for pairs with a d shell"),
         ("QCX_REP_KEXP", 1.5, "distance exponent of the repulsion"),
         ("QCX_AES_A3", 3.0, "damping exponent for R^-3 multipole kernels"),
@@ -259,7 +266,8 @@ def main():
     arrsh("qcx_sh_refocc", "double", lambda z, i, n, l: refocc(z)[i])
     arrsh("qcx_sh_selfenergy", "double", lambda z, i, n, l: self_energy(z, l))
     arrsh("qcx_sh_kcn", "double", lambda z, i, n, l: {0: 0.006, 1: 0.003, 2: 0.001}[l])
-    arrsh("qcx_sh_kpoly", "double", lambda z, i, n, l: {0: -0.005, 1: 0.05, 2: 0.02}[l])
+    arrsh("qcx_sh_kpoly", "double",
+          lambda z, i, n, l: KPOLY_P_FIT.get(z, 0.05) if l == 1 else {0: -0.005, 2: 0.02}[l])
 
     def eta_atom(z):
         p, nv = period(z), nval(z)
@@ -299,7 +307,8 @@ def main():
     arr1("qcx_rcov", "double", [0] + [4.0 / 3.0 * RCOV2009[z] * AATOAU for z in z_all])
     arr1("qcx_rep_alpha", "double", [0] + [REP_ALPHA_FIT.get(z, 2.0 - 0.03 * nval(z) if period(z) == 2 else 1.6 - 0.02 * nval(z))
                                          for z in z_all])
-    arr1("qcx_rep_zeff", "double", [0] + [1.0 if z == 1 else (2.0 if z == 2 else 1.0 + 0.9 * nval(z)) for z in z_all])
+    arr1("qcx_rep_zeff", "double", [0] + [REP_ZEFF_FIT.get(z, 1.0 if z == 1 else (2.0 if z == 2 else 1.0 + 0.9 * nval(z)))
+                                        for z in z_all])
     arr1("qcx_aes_dkernel", "double", [0] + [0.010 + 0.002 * nval(z) for z in z_all])
     arr1("qcx_aes_qkernel", "double", [0] + [0.005 + 0.001 * nval(z) for z in z_all])
     arr1("qcx_aes_rad0", "double", [0] + [1.2 * RCOV2009[z] * AATOAU + 0.8 for z in z_all])
