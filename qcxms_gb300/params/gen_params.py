@@ -184,6 +184,12 @@ def slater_zeta(z, n, l):
 
 
 def self_energy(z, l):
+    if z in (10, 18):  # closed-shell noble gases: deeper levels (ionisation energies near 16-22 eV)
+        return 1.6 * _self_energy_rule(z, l)
+    return _self_energy_rule(z, l)
+
+
+def _self_energy_rule(z, l):
     nv = nval(z)
     p = period(z)
     if p == 1:
