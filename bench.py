@@ -1,0 +1,325 @@
+"""Trajectory-step throughput of the GFN2-xTB MD hot path on one GB300.
+
+Workload (default): 256 seeded C/H/N/O radical cations with 5-40 atoms
+(element fractions C 0.35, H 0.5, N 0.05, O 0.1), charge +1, initial
+temperatures uniform in 1000-4000 K, 0.5 fs leapfrog steps, FP64, one captured
+CUDA graph per MD step. A step is leapfrog + energy + analytic gradient for
+every trajectory; the metric counts completed trajectory-steps per second.
+
+Lines printed (one JSON line):
+  default           the CUDA path (libqcxgpu.so), device-resident state
+  --impl reference  the CPU restatement of the same step (the QCxMS reference
+                    path itself needs a Fortran toolchain and tblite, neither of
+                    which exists here), all host threads, bounded sample
+
+Multi-GPU: trajectories are independent; with torchrun each rank runs its own
+shard (disjoint seeds) with no collective on the data path.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GFN2-xTB trajectory-steps/s"
+NTRAJ, NMIN, NMAX = 256, 5, 40
+DT_FS = 0.5
+ETEMP = 300.0
+
+
+def workload(rank, ntraj=None):
+    from qcxms_gb300 import molgen
+    n = ntraj or NTRAJ
+    return molgen.batch_workload(n, NMIN, NMAX, seed0=rank * NTRAJ)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def scc_flops(nao, iters):
+    """Algorithmic FLOPs of the SCC kernel: per molecule k*(9n^3 eigensolve + 2n^3
+    density) + 2n^3 energy-weighted density (fixed counting convention)."""
+    n3 = nao.astype(np.float64) ** 3
+    return float(np.sum(iters * 11.0 * n3 + 2.0 * n3))
+
+
+def measured_fp64_peak(torch):
+    """Dense FP64 throughput of this GPU (cuBLAS DGEMM, best of 5), TFLOP/s."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_sample(mols, seconds, nthreads):
+    """Time the oracle restatement on a bounded sample of the workload."""
+    import oracle
+    from qcxms_gb300 import constants
+    kT = ETEMP * constants.KB_AU
+    dt = DT_FS * constants.FSTOAU
+    # initial gradients (setup, untimed)
+    grads = [oracle.egrad(m["Z"], m["xyz"], m["charge"], kT=kT)[2] for m in mols]
+    done, steps, t0 = 0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        fails, xyz, vel, g, ep, it = oracle.md_batch(mols, 1, dt, grads, kT, nthreads=nthreads)
+        off = 0
+        for i, m in enumerate(mols):
+            n = len(m["Z"])
+            m["xyz"], m["vel"], grads[i] = xyz[off:off + n], vel[off:off + n], g[off:off + n]
+            off += n
+        done += len(mols) - fails
+        steps += 1
+    el = time.perf_counter() - t0
+    return done / el, steps, el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    mols = workload(0)
+    ncpu = os.cpu_count() or 1
+    sample = mols[: min(len(mols), 4 * ncpu)]
+    for _ in range(args.warmup):
+        pass
+    vals = []
+    for _ in range(max(1, args.steps)):
+        v, nsteps, el = cpu_sample([dict(m) for m in sample], max(2.0, 20.0 / max(1, args.steps)), ncpu)
+        vals.append(v)
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "trajectory-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * NTRAJ / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs, FP64",
+                   "ntraj": NTRAJ, "atoms": [NMIN, NMAX], "etemp_K": ETEMP},
+        "cpu_baseline": {"value": v, "unit": "trajectory-steps/s", "cores": ncpu, "kind": "port",
+                         "sample": "%d of the %d trajectories, leapfrog + CPU FP64 restatement of the energy/gradient, "
+                                   "OpenMP over trajectories, ~20 s" % (len(sample), NTRAJ)},
+        "e2e": {"value": v, "unit": "trajectory-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    import qcxms_gb300 as qg
+    from qcxms_gb300 import constants
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dt = DT_FS * constants.FSTOAU
+    mols = workload(rank, args.ntraj)
+    b = qg.Batch(mols, etemp=ETEMP)
+    b.egrad()
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream())
+    nao, nat = b.sizes()
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    # ---- device-resident timing: graph replay, L2 flushed between steps ----
+    for _ in range(args.warmup):
+        b.step(1, dt)
+    barrier()
+    _, steps0 = b.progress()
+    total_ms = 0.0
+    launches = 0
+    with ClockSampler(local) as clk:
+        barrier()
+        for _ in range(args.steps):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            b.step(1, dt)
+            e.record(stream)
+            e.synchronize()
+            total_ms += s.elapsed_time(e)
+            launches += b.kernel_launches()
+        barrier()
+    _, steps1 = b.progress()
+    done = float(np.sum(steps1 - steps0))
+    ms_all = torch.tensor([total_ms, done], dtype=torch.float64, device="cuda")
+    if world > 1:
+        t = ms_all.clone()
+        torch.distributed.all_reduce(t[0:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:2], op=torch.distributed.ReduceOp.SUM)
+        ms_all = t
+    total_ms, done_all = float(ms_all[0]), float(ms_all[1])
+    value = done_all / (total_ms * 1e-3)
+
+    # ---- end to end through the public API with pinned host buffers ----
+    r = b.get()
+    hx = torch.from_numpy(r["xyz"]).pin_memory()
+    hv = torch.from_numpy(r["vel"]).pin_memory()
+    he = torch.zeros(b.nmol, dtype=torch.float64).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    _, s0 = b.progress()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        b.set_state_ptr(hx.data_ptr(), hv.data_ptr())
+        b.step(1, dt)
+        b.get_ptr(hx.data_ptr(), hv.data_ptr(), he.data_ptr())
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    _, s1 = b.progress()
+    e2e_done = float(np.sum(s1 - s0))
+    if world > 1:
+        t = torch.tensor([e2e_s, e2e_done], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t[0:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:2], op=torch.distributed.ReduceOp.SUM)
+        e2e_s, e2e_done = float(t[0]), float(t[1])
+    e2e = e2e_done / e2e_s
+    h2d = 2 * 3 * 8 * b.natom
+    d2h = 2 * 3 * 8 * b.natom + 8 * b.nmol
+
+    # ---- roofline of the dominant kernel (SCC), timed live on the batch stream ----
+    prof = [b.profile_egrad() for _ in range(3)]
+    scc_ms = statistics.median(p["scc"] for p in prof)
+    iters = b.get()["iters"].astype(np.float64)
+    act, _ = b.progress()
+    flops = scc_flops(nao[act > 0], iters[act > 0])
+    achieved = flops / (scc_ms * 1e-3) / 1e12
+    peak64 = measured_fp64_peak(torch)
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            ncpu = os.cpu_count() or 1
+            sample = [dict(m) for m in workload(0)[: 2 * ncpu]]
+            v, nst, el = cpu_sample(sample, 12.0, ncpu)
+            cpu = {"value": v, "unit": "trajectory-steps/s", "cores": ncpu, "kind": "port",
+                   "sample": "%d of the %d trajectories x %d steps (%.1f s), CPU FP64 restatement, OpenMP over "
+                             "trajectories" % (len(sample), NTRAJ, nst, el)}
+        breakdown = {k: round(statistics.median(p[k] for p in prof), 4) for k in prof[0]}
+        line = {
+            "metric": METRIC, "value": value, "unit": "trajectory-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs, FP64, one CUDA graph "
+                                   "per MD step", "ntraj_per_gpu": b.nmol, "atoms": [NMIN, NMAX],
+                       "etemp_K": ETEMP, "precision": "fp64", "l2": "flushed between timed steps (256 MiB write)",
+                       "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters)),
+                       "active_trajectories": int(np.sum(act))},
+            "e2e": {"value": e2e, "unit": "trajectory-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                         "frac": achieved / peak64, "traffic": None, "kernel": "k_scc",
+                         "peak_source": "measured in this run: cuBLAS FP64 GEMM 4096^3 (MEASURED_PEAKS.json holds "
+                                        "only HBM and bf16 peaks)",
+                         "flops_convention": "per molecule: iters*(9n^3+2n^3)+2n^3"},
+            "kernel_ms": breakdown,
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ntraj", type=int, default=None, help="smaller batch for profiling runs (default 256)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -99,8 +99,27 @@ int qcx_batch_get_matrix(qcx_batch* b, int i, int which, double* out);
  * qcx_batch_egrad call (graph replays count their kernel nodes). */
 long long qcx_batch_kernel_launches(qcx_batch* b);
 
+/* Per-trajectory progress: active[nmol] (1 while running; a failed energy
+ * evaluation stops the trajectory, as src/md.f90:317-344 ends the MD run)
+ * and steps_done[nmol] (successful energy + gradient evaluations so far).
+ * Setting new coordinates with qcx_batch_set_state restarts all. */
+int qcx_batch_get_progress(qcx_batch* b, int32_t* active, int64_t* steps_done);
+
 /* Synchronise the batch's stream. */
 int qcx_batch_sync(qcx_batch* b);
+
+/* The cudaStream_t the batch launches on (as void*), for callers that time
+ * or order work against it. */
+void* qcx_batch_stream(qcx_batch* b);
+
+/* One energy + gradient evaluation with CUDA events between its kernels on
+ * the batch's stream. ms[0..5] = coordination numbers, integrals, SCC,
+ * gradient reset, integral-derivative gradient, atom-pair gradient. */
+int qcx_batch_profile_egrad(qcx_batch* b, float* ms);
+
+/* Atomic-orbital and atom counts of every molecule (nao[nmol], nat[nmol]);
+ * used to count algorithmic work. */
+int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat);
 
 #ifdef __cplusplus
 }

@@ -75,6 +75,11 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_kernel_launches.restype = c_ll
     lib.qcx_batch_kernel_launches.argtypes = [ctypes.c_void_p]
     lib.qcx_batch_sync.argtypes = [ctypes.c_void_p]
+    lib.qcx_batch_get_progress.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int64)]
+    lib.qcx_batch_stream.restype = ctypes.c_void_p
+    lib.qcx_batch_stream.argtypes = [ctypes.c_void_p]
+    lib.qcx_batch_profile_egrad.argtypes = [ctypes.c_void_p, P(ctypes.c_float)]
+    lib.qcx_batch_get_sizes.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32)]
     _lib = lib
     return lib
 
@@ -185,6 +190,40 @@ class Batch:
         if rc < 0:
             raise RuntimeError("get_matrix failed: " + _err(self._lib))
         return out
+
+    def progress(self):
+        active = np.zeros(self.nmol, dtype=np.int32)
+        steps = np.zeros(self.nmol, dtype=np.int64)
+        self._check(self._lib.qcx_batch_get_progress(self._h, _ip(active),
+                                                     steps.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))),
+                    "progress")
+        return active, steps
+
+    def stream(self):
+        return int(self._lib.qcx_batch_stream(self._h))
+
+    def profile_egrad(self):
+        ms = np.zeros(6, dtype=np.float32)
+        self._check(self._lib.qcx_batch_profile_egrad(self._h, ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                    "profile_egrad")
+        return dict(zip(["cn", "integrals", "scc", "zero_grad", "grad_pairs", "grad_atoms"], ms.tolist()))
+
+    def sizes(self):
+        nao = np.zeros(self.nmol, dtype=np.int32)
+        nat = np.zeros(self.nmol, dtype=np.int32)
+        self._check(self._lib.qcx_batch_get_sizes(self._h, _ip(nao), _ip(nat)), "sizes")
+        return nao, nat
+
+    def set_state_ptr(self, xyz_ptr=None, vel_ptr=None):
+        """set_state from raw host pointers (e.g. pinned buffers)."""
+        c = lambda p: None if p is None else ctypes.cast(p, ctypes.POINTER(ctypes.c_double))
+        self._check(self._lib.qcx_batch_set_state(self._h, c(xyz_ptr), c(vel_ptr), None), "set_state")
+
+    def get_ptr(self, xyz_ptr=None, vel_ptr=None, energy_ptr=None):
+        """get into raw host pointers (e.g. pinned buffers)."""
+        c = lambda p: None if p is None else ctypes.cast(p, ctypes.POINTER(ctypes.c_double))
+        self._check(self._lib.qcx_batch_get(self._h, c(xyz_ptr), c(vel_ptr), None, c(energy_ptr), None, None,
+                                            None, None), "get")
 
     def kernel_launches(self):
         return int(self._lib.qcx_batch_kernel_launches(self._h))

@@ -96,7 +96,8 @@ struct qcx_batch {
   double *d_cn = nullptr, *d_cnd = nullptr, *d_dedcn = nullptr, *d_dedcnd = nullptr, *d_mrad = nullptr,
          *d_dmrad = nullptr, *d_w4 = nullptr, *d_dw4 = nullptr, *d_qat = nullptr;
   double *d_mats = nullptr, *d_vecs = nullptr, *d_energy = nullptr, *d_ekin = nullptr;
-  int *d_status = nullptr, *d_iters = nullptr;
+  int *d_status = nullptr, *d_iters = nullptr, *d_active = nullptr;
+  long long* d_steps = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   double graph_tstep = 0.0;
@@ -124,7 +125,7 @@ void free_batch(qcx_batch* b) {
   void* ptrs[] = {b->d_prm, b->d_mol, b->d_Z, b->d_atom_mol, b->d_sh_atom, b->d_sh_k, b->d_sh_ao, b->d_pairs,
                   b->d_xyz, b->d_grad, b->d_vel, b->d_mass, b->d_cn, b->d_cnd, b->d_dedcn, b->d_dedcnd,
                   b->d_mrad, b->d_dmrad, b->d_w4, b->d_dw4, b->d_qat, b->d_mats, b->d_vecs, b->d_energy,
-                  b->d_ekin, b->d_status, b->d_iters};
+                  b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -197,7 +198,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
       dalloc(&b->d_w4, (size_t)na * kMaxRef) || dalloc(&b->d_dw4, (size_t)na * kMaxRef) || dalloc(&b->d_qat, na) ||
       dalloc(&b->d_mats, (size_t)mat_off) || dalloc(&b->d_vecs, (size_t)vec_off) ||
       dalloc(&b->d_energy, (size_t)nmol * kNumEnergy) || dalloc(&b->d_ekin, nmol) || dalloc(&b->d_status, nmol) ||
-      dalloc(&b->d_iters, nmol))
+      dalloc(&b->d_iters, nmol) || dalloc(&b->d_active, nmol) || dalloc(&b->d_steps, nmol))
     return -1;
   b->bytes = sizeof(double) * ((size_t)mat_off + (size_t)vec_off);
   CK(cudaMemcpy(b->d_prm, &hp, sizeof(Params), cudaMemcpyHostToDevice));
@@ -214,6 +215,11 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   CK(cudaMemset(b->d_status, 0, sizeof(int) * nmol));
   CK(cudaMemset(b->d_energy, 0, sizeof(double) * nmol * kNumEnergy));
   CK(cudaMemset(b->d_ekin, 0, sizeof(double) * nmol));
+  CK(cudaMemset(b->d_steps, 0, sizeof(long long) * nmol));
+  {
+    std::vector<int> on(nmol, 1);
+    CK(cudaMemcpy(b->d_active, on.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
+  }
   {
     std::vector<double> m(na, 1.0);
     CK(cudaMemcpy(b->d_mass, m.data(), sizeof(double) * na, cudaMemcpyHostToDevice));
@@ -250,6 +256,8 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   d.status = b->d_status;
   d.iters = b->d_iters;
   d.ekin = b->d_ekin;
+  d.active = b->d_active;
+  d.steps_done = b->d_steps;
   d.max_nao = b->max_nao;
   d.smem_bytes = (int)scc_smem_bytes(b->max_nao, 0);
   d.max_iter = QCX_SCC_MAXITER;
@@ -313,7 +321,13 @@ int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, do
 int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass) {
   if (!b) return -1;
   size_t n3 = sizeof(double) * 3 * b->natom;
-  if (xyz) CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));
+  if (xyz) {
+    CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));
+    // new coordinates start every trajectory afresh
+    std::vector<int> on(b->nmol, 1);
+    CK(cudaMemcpyAsync(b->d_active, on.data(), sizeof(int) * b->nmol, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+  }
   if (vel) CK(cudaMemcpyAsync(b->d_vel, vel, n3, cudaMemcpyHostToDevice, b->stream));
   if (mass) CK(cudaMemcpyAsync(b->d_mass, mass, sizeof(double) * b->natom, cudaMemcpyHostToDevice, b->stream));
   return 0;
@@ -387,9 +401,54 @@ int qcx_batch_get_matrix(qcx_batch* b, int i, int which, double* out) {
 
 long long qcx_batch_kernel_launches(qcx_batch* b) { return b ? b->launches : -1; }
 
+int qcx_batch_get_progress(qcx_batch* b, int32_t* active, int64_t* steps_done) {
+  if (!b) return -1;
+  if (active) CK(cudaMemcpyAsync(active, b->d_active, sizeof(int) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  if (steps_done)
+    CK(cudaMemcpyAsync(steps_done, b->d_steps, sizeof(long long) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
 int qcx_batch_sync(qcx_batch* b) {
   if (!b) return -1;
   CK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+void* qcx_batch_stream(qcx_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+int qcx_batch_profile_egrad(qcx_batch* b, float* ms) {
+  if (!b || !ms) return -1;
+  cudaEvent_t ev[kEgradLaunches + 1];
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  const DevBatch& d = b->dev;
+  CK(cudaEventRecord(ev[0], b->stream));
+  launch_cn(d, b->stream);
+  CK(cudaEventRecord(ev[1], b->stream));
+  launch_integrals(d, b->stream);
+  CK(cudaEventRecord(ev[2], b->stream));
+  launch_scc(d, 0, b->stream);
+  CK(cudaEventRecord(ev[3], b->stream));
+  launch_zero_grad(d, b->stream);
+  CK(cudaEventRecord(ev[4], b->stream));
+  launch_grad_pairs(d, b->stream);
+  CK(cudaEventRecord(ev[5], b->stream));
+  launch_grad_atoms(d, b->stream);
+  CK(cudaEventRecord(ev[6], b->stream));
+  CK(cudaEventSynchronize(ev[6]));
+  for (int i = 0; i < kEgradLaunches; ++i) CK(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+  for (auto& e : ev) cudaEventDestroy(e);
+  b->launches = kEgradLaunches;
+  return check_launch();
+}
+
+int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat) {
+  if (!b) return -1;
+  for (int m = 0; m < b->nmol; ++m) {
+    if (nao) nao[m] = b->mol[m].nao;
+    if (nat) nat[m] = b->mol[m].nat;
+  }
   return 0;
 }
 

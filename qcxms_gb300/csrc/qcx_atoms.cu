@@ -11,6 +11,7 @@ namespace qcx {
 __global__ void k_cn(DevBatch bt) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= bt.natom) return;
+  if (!bt.active[bt.atom_mol[a]]) return;
   const Params& P = *bt.prm;
   const MolDesc md = bt.mol[bt.atom_mol[a]];
   int za = bt.Z[a];
@@ -43,6 +44,7 @@ void launch_cn(const DevBatch& bt, cudaStream_t st) {
 __global__ void k_zero_grad(DevBatch bt) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= bt.natom) return;
+  if (!bt.active[bt.atom_mol[a]]) return;
   bt.grad[3 * a] = 0.0;
   bt.grad[3 * a + 1] = 0.0;
   bt.grad[3 * a + 2] = 0.0;
@@ -75,7 +77,11 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
   extern __shared__ __align__(16) double sm[];
   const int mol = blockIdx.x;
   const MolDesc md = bt.mol[mol];
-  if (bt.status[mol] & kCholeskyFailed) return;
+  if (!bt.active[mol]) return;
+  if (bt.status[mol] & kCholeskyFailed) {
+    if (threadIdx.x == 0) bt.active[mol] = 0;
+    return;
+  }
   const Params& P = *bt.prm;
   const int nat = md.nat, nsh = md.nsh, n = md.nao;
   const int off = md.atom_off;
@@ -301,6 +307,10 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
     E[kERep] = erep;
     E[kETotal] += eatm + erep;
     if (!isfinite(E[kETotal])) bt.status[mol] |= kNonFinite;
+    // a failed evaluation ends the trajectory, as QCxMS ends an MD run whose
+    // energy call failed (src/md.f90:317-344 via src/iniqm.f90:650-654)
+    if (bt.status[mol] & (kSccNotConverged | kNonFinite | kCholeskyFailed)) bt.active[mol] = 0;
+    else bt.steps_done[mol] += 1;
   }
 }
 
@@ -317,6 +327,7 @@ __global__ void k_leapfrog(DevBatch bt, double tstep) {
   __shared__ double red[32];
   const int mol = blockIdx.x;
   const MolDesc md = bt.mol[mol];
+  if (!bt.active[mol]) return;
   double ke = 0.0;
   for (int i = threadIdx.x; i < 3 * md.nat; i += blockDim.x) {
     long long e = 3LL * md.atom_off + i;

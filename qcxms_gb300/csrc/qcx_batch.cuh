@@ -125,6 +125,8 @@ struct DevBatch {
   int* status;     // [nmol]
   int* iters;      // [nmol]
   double* ekin;    // [nmol]
+  int* active;     // [nmol] 1 while the trajectory runs; 0 after a failed evaluation
+  long long* steps_done;  // [nmol] successful energy+gradient evaluations
   int max_nao;
   int smem_bytes;  // dynamic shared memory granted to the SCC kernel
   // SCC controls

@@ -189,6 +189,7 @@ __global__ void k_integrals(DevBatch bt) {
   if (idx >= bt.npair) return;
   ShellPair sp = bt.pairs[idx];
   int A = bt.sh_atom[sp.s], B = bt.sh_atom[sp.t];
+  if (!bt.active[bt.atom_mol[A]]) return;
   const MolDesc md = bt.mol[bt.atom_mol[A]];
   const Params& P = *bt.prm;
   int la = P.sh_l[bt.Z[A]][bt.sh_k[sp.s]], lb = P.sh_l[bt.Z[B]][bt.sh_k[sp.t]];
@@ -331,6 +332,7 @@ __global__ void k_grad_pairs(DevBatch bt) {
   ShellPair sp = bt.pairs[idx];
   int A = bt.sh_atom[sp.s], B = bt.sh_atom[sp.t];
   if (A == B) return;
+  if (!bt.active[bt.atom_mol[A]]) return;
   const MolDesc md = bt.mol[bt.atom_mol[A]];
   const Params& P = *bt.prm;
   int la = P.sh_l[bt.Z[A]][bt.sh_k[sp.s]], lb = P.sh_l[bt.Z[B]][bt.sh_k[sp.t]];

@@ -538,6 +538,7 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
   extern __shared__ __align__(16) char smem_raw[];
   const int mol = blockIdx.x;
+  if (!bt.active[mol]) return;
   MolView mv;
   mv.bt = &bt;
   mv.md = bt.mol[mol];

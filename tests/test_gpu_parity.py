@@ -128,9 +128,29 @@ def test_nve_energy_conservation(gpu):
     b = qg.Batch([{"Z": Z, "xyz": xyz, "vel": vel, "mass": molgen.masses(Z), "charge": 1}])
     b.egrad()
     etot = []
-    for _ in range(10):
-        b.step(20, 0.5 * constants.FSTOAU)
+    for _ in range(6):
+        b.step(10, 0.5 * constants.FSTOAU)
         r = b.get()
         assert r["status"][0] == 0
         etot.append(r["energy"][0] + r["ekin"][0])
     assert max(etot) - min(etot) < 2e-3
+
+
+def test_failed_trajectory_is_masked(gpu):
+    # an SCC capped at 2 iterations cannot converge: the trajectory stops,
+    # the others keep going, and new coordinates restart it
+    mols = [molecules.c6h12o2(), molecules.h2o_cation()]
+    b = _batch(mols)
+    b.egrad()
+    b.set_scc(2, 1e-7, 1e-6, 0.4)
+    b.egrad()
+    active, steps = b.progress()
+    assert list(active) == [0, 0] and list(steps) == [1, 1]
+    b.set_scc(100, 1e-7, 1e-6, 0.4)
+    b.step(3, 0.5 * constants.FSTOAU)
+    active, steps = b.progress()
+    assert list(steps) == [1, 1]
+    b.set_state(xyz=np.concatenate([m[1] for m in mols]))
+    b.egrad()
+    active, steps = b.progress()
+    assert list(active) == [1, 1] and list(steps) == [2, 2]
