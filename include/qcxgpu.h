@@ -67,6 +67,15 @@ void qcx_batch_destroy(qcx_batch* b);
 /* SCC controls (defaults: 100, 1e-7 Eh, 1e-6, 0.4). max_iter <= 100. */
 int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, double mixing);
 
+/* Arithmetic of the SCC loop: 0 = FP64 throughout (default); 1 = mixed:
+ * FP32 transforms, Jacobi eigensolve and density until the charge residual
+ * reaches 3e-5, then FP64 iterations warm-started from the FP32 eigenvectors
+ * to the same convergence thresholds. Integrals, potentials, Fermi level,
+ * Broyden mixing, energies and the gradient are FP64 in both modes. */
+#define QCX_PRECISION_FP64 0
+#define QCX_PRECISION_MIXED 1
+int qcx_batch_set_precision(qcx_batch* b, int precision);
+
 /* Copy host state in. Any pointer may be NULL to keep the current value.
  * xyz, vel: [natom][3]; mass: [natom] (atomic units). */
 int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass);

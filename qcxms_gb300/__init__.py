@@ -75,6 +75,7 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_kernel_launches.restype = c_ll
     lib.qcx_batch_kernel_launches.argtypes = [ctypes.c_void_p]
     lib.qcx_batch_sync.argtypes = [ctypes.c_void_p]
+    lib.qcx_batch_set_precision.argtypes = [ctypes.c_void_p, c_int]
     lib.qcx_batch_get_progress.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int64)]
     lib.qcx_batch_stream.restype = ctypes.c_void_p
     lib.qcx_batch_stream.argtypes = [ctypes.c_void_p]
@@ -149,6 +150,11 @@ class Batch:
     def set_scc(self, max_iter=100, econv=1e-7, pconv=1e-6, mixing=0.4):
         self._check(self._lib.qcx_batch_set_scc(self._h, int(max_iter), float(econv), float(pconv), float(mixing)),
                     "set_scc")
+
+    def set_precision(self, precision):
+        """0 / "fp64": FP64 SCC; 1 / "mixed": FP32 SCC iterations finished in FP64."""
+        p = {"fp64": 0, "mixed": 1}.get(precision, precision)
+        self._check(self._lib.qcx_batch_set_precision(self._h, int(p)), "set_precision")
 
     def set_state(self, xyz=None, vel=None, mass=None):
         c = lambda a, s: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(s)

@@ -103,6 +103,7 @@ struct qcx_batch {
   double graph_tstep = 0.0;
   long long launches = 0;
   size_t bytes = 0;
+  int precision = 0;
 };
 
 namespace {
@@ -111,7 +112,7 @@ void enqueue_egrad(qcx_batch* b) {
   const DevBatch& d = b->dev;
   launch_cn(d, b->stream);
   launch_integrals(d, b->stream);
-  launch_scc(d, 0, b->stream);
+  launch_scc(d, b->precision, b->stream);
   launch_zero_grad(d, b->stream);
   launch_grad_pairs(d, b->stream);
   launch_grad_atoms(d, b->stream);
@@ -318,6 +319,21 @@ int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, do
   return 0;
 }
 
+int qcx_batch_set_precision(qcx_batch* b, int precision) {
+  if (!b || (precision != 0 && precision != 1)) {
+    set_error("qcx_batch_set_precision: precision must be 0 (FP64) or 1 (mixed)");
+    return -1;
+  }
+  if (precision != b->precision && b->graph_exec) {
+    cudaGraphExecDestroy(b->graph_exec);
+    cudaGraphDestroy(b->graph);
+    b->graph_exec = nullptr;
+    b->graph = nullptr;
+  }
+  b->precision = precision;
+  return 0;
+}
+
 int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass) {
   if (!b) return -1;
   size_t n3 = sizeof(double) * 3 * b->natom;
@@ -428,7 +444,7 @@ int qcx_batch_profile_egrad(qcx_batch* b, float* ms) {
   CK(cudaEventRecord(ev[1], b->stream));
   launch_integrals(d, b->stream);
   CK(cudaEventRecord(ev[2], b->stream));
-  launch_scc(d, 0, b->stream);
+  launch_scc(d, b->precision, b->stream);
   CK(cudaEventRecord(ev[3], b->stream));
   launch_zero_grad(d, b->stream);
   CK(cudaEventRecord(ev[4], b->stream));

@@ -61,30 +61,32 @@ __device__ double cta_max(double v, double* red) {
   return m;
 }
 
-// C[M][N] = op(A) op(B), row-major, FP64. ta: A is stored K x M; tb: B is stored N x K.
-__device__ void cta_gemm(int M, int N, int K, const double* A, int lda, bool ta, const double* B, int ldb, bool tb,
-                         double* C, int ldc) {
+// C[M][N] = op(A) op(B), row-major; inputs converted to ACC on load.
+// ta: A is stored K x M; tb: B is stored N x K. 2x2 register tile per thread.
+template <typename TA, typename TB, typename TC, typename ACC>
+__device__ void cta_gemm(int M, int N, int K, const TA* A, int lda, bool ta, const TB* B, int ldb, bool tb, TC* C,
+                         int ldc) {
   int tilesM = (M + 1) / 2, tilesN = (N + 1) / 2;
   for (int t = threadIdx.x; t < tilesM * tilesN; t += blockDim.x) {
     int i0 = (t / tilesN) * 2, j0 = (t % tilesN) * 2;
-    double c00 = 0, c01 = 0, c10 = 0, c11 = 0;
+    ACC c00 = 0, c01 = 0, c10 = 0, c11 = 0;
     bool i1ok = i0 + 1 < M, j1ok = j0 + 1 < N;
     int i1 = i1ok ? i0 + 1 : i0, j1 = j1ok ? j0 + 1 : j0;
     for (int k = 0; k < K; ++k) {
-      double a0 = ta ? A[(long long)k * lda + i0] : A[(long long)i0 * lda + k];
-      double a1 = ta ? A[(long long)k * lda + i1] : A[(long long)i1 * lda + k];
-      double b0 = tb ? B[(long long)j0 * ldb + k] : B[(long long)k * ldb + j0];
-      double b1 = tb ? B[(long long)j1 * ldb + k] : B[(long long)k * ldb + j1];
+      ACC a0 = (ACC)(ta ? A[(long long)k * lda + i0] : A[(long long)i0 * lda + k]);
+      ACC a1 = (ACC)(ta ? A[(long long)k * lda + i1] : A[(long long)i1 * lda + k]);
+      ACC b0 = (ACC)(tb ? B[(long long)j0 * ldb + k] : B[(long long)k * ldb + j0]);
+      ACC b1 = (ACC)(tb ? B[(long long)j1 * ldb + k] : B[(long long)k * ldb + j1]);
       c00 = fma(a0, b0, c00);
       c01 = fma(a0, b1, c01);
       c10 = fma(a1, b0, c10);
       c11 = fma(a1, b1, c11);
     }
-    C[(long long)i0 * ldc + j0] = c00;
-    if (j1ok) C[(long long)i0 * ldc + j1] = c01;
+    C[(long long)i0 * ldc + j0] = (TC)c00;
+    if (j1ok) C[(long long)i0 * ldc + j1] = (TC)c01;
     if (i1ok) {
-      C[(long long)i1 * ldc + j0] = c10;
-      if (j1ok) C[(long long)i1 * ldc + j1] = c11;
+      C[(long long)i1 * ldc + j0] = (TC)c10;
+      if (j1ok) C[(long long)i1 * ldc + j1] = (TC)c11;
     }
   }
 }
@@ -98,6 +100,7 @@ struct SccShared {
   int* perm;       // [np]
   int* rp;         // [np/2] rotation pair p
   int* rq;         // [np/2] rotation pair q
+  int* rskip;      // [np/2] 1 if the rotation is the identity
   double* rc;      // [np/2]
   double* rs;      // [np/2]
   double* mom;     // [10][n] per-AO moment partials
@@ -113,7 +116,7 @@ __host__ __device__ inline size_t scc_fixed_bytes(int n) {
   size_t b = 0;
   b += align16(sizeof(int) * n) * 2;
   b += align16(sizeof(int) * np);
-  b += align16(sizeof(int) * (np / 2)) * 2;
+  b += align16(sizeof(int) * (np / 2)) * 3;
   b += align16(sizeof(double) * (np / 2)) * 2;
   b += align16(sizeof(double) * 10 * n);
   b += align16(sizeof(double) * 16 * kWarps);
@@ -152,6 +155,7 @@ __device__ SccShared carve(char* base, int n) {
   s.perm = (int*)(base + o); o += align16(sizeof(int) * np);
   s.rp = (int*)(base + o); o += align16(sizeof(int) * (np / 2));
   s.rq = (int*)(base + o); o += align16(sizeof(int) * (np / 2));
+  s.rskip = (int*)(base + o); o += align16(sizeof(int) * (np / 2));
   s.rc = (double*)(base + o); o += align16(sizeof(double) * (np / 2));
   s.rs = (double*)(base + o); o += align16(sizeof(double) * (np / 2));
   s.mom = (double*)(base + o); o += align16(sizeof(double) * 10 * n);
@@ -268,26 +272,31 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
 }
 
 // ---------------------------------------------------------------------------
-// cyclic parallel Jacobi on the symmetric np x np matrix A (lda = np);
-// Vt (ld = np) accumulates eigenvectors as rows. Returns sweeps used.
+// cyclic parallel Jacobi on the symmetric np x np matrix A (lda = np).
+// Vt (ld = np) holds eigenvectors as rows; with warm = false it starts as the
+// identity, with warm = true it keeps its rows (a previous orthonormal basis in
+// which A was expressed) and the rotations are accumulated onto them.
+// Rounds use the round-robin pairing: n/2 disjoint (p,q) rotations each.
+// Returns the number of sweeps, or -1 if max_sweeps were not enough.
 // ---------------------------------------------------------------------------
-__device__ int jacobi(double* A, double* Vt, int n, SccShared& sh, int max_sweeps) {
+template <typename T>
+__device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& sh, int max_sweeps) {
   const int np = n + (n & 1);
   const int half = np / 2;
   const int m = np - 1;
   for (int i = threadIdx.x; i < np * np; i += blockDim.x) {
     int r = i / np, c = i % np;
-    Vt[i] = (r == c) ? 1.0 : 0.0;
-    if (r >= n || c >= n) A[i] = 0.0;
+    if (!warm || r >= n || c >= n) Vt[i] = (r == c) ? T(1) : T(0);
+    if (r >= n || c >= n) A[i] = T(0);
   }
   __syncthreads();
   double amax = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) amax = fmax(amax, fabs(A[i * np + i]));
+  for (int i = threadIdx.x; i < n; i += blockDim.x) amax = fmax(amax, fabs((double)A[i * np + i]));
   amax = cta_max(amax, sh.red);
-  const double tol = 1e-12 * fmax(1.0, amax);
-  int sweep;
-  for (sweep = 0; sweep < max_sweeps; ++sweep) {
-    double offmax = 0.0;
+  const T tol = (T)(reltol * fmax(1.0, amax));
+  const T tiny = (T)(1e-30);
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    T offmax = 0;
     for (int r = 0; r < m; ++r) {
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
         int p, q;
@@ -303,50 +312,54 @@ __device__ int jacobi(double* A, double* Vt, int n, SccShared& sh, int max_sweep
           p = q;
           q = t;
         }
-        double apq = A[p * np + q];
-        double c = 1.0, s = 0.0;
-        offmax = fmax(offmax, fabs(apq));
-        if (fabs(apq) > 1e-300) {
-          double app = A[p * np + p], aqq = A[q * np + q];
-          double theta = (aqq - app) / (2.0 * apq);
-          double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
-          c = 1.0 / sqrt(1.0 + t * t);
+        T apq = A[p * np + q];
+        T aa = apq < T(0) ? -apq : apq;
+        offmax = aa > offmax ? aa : offmax;
+        int skip = !(aa > tiny);
+        T c = 1, s = 0;
+        if (!skip) {
+          T app = A[p * np + p], aqq = A[q * np + q];
+          T theta = (aqq - app) / (T(2) * apq);
+          T at = theta < T(0) ? -theta : theta;
+          T t = (theta >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + theta * theta));
+          c = T(1) / sqrt(T(1) + t * t);
           s = t * c;
         }
         sh.rp[k] = p;
         sh.rq[k] = q;
-        sh.rc[k] = c;
-        sh.rs[k] = s;
+        sh.rskip[k] = skip;
+        ((T*)sh.rc)[k] = c;
+        ((T*)sh.rs)[k] = s;
       }
       __syncthreads();
       // rows of A and of Vt
       for (int i = threadIdx.x; i < half * np; i += blockDim.x) {
-        int k = i / np, j = i % np;
-        double c = sh.rc[k], s = sh.rs[k];
-        if (s == 0.0) continue;
+        int k = i / np, j = i - k * np;
+        if (sh.rskip[k]) continue;
+        T c = ((T*)sh.rc)[k], s = ((T*)sh.rs)[k];
         int p = sh.rp[k], q = sh.rq[k];
-        double ap = A[p * np + j], aq = A[q * np + j];
+        T ap = A[p * np + j], aq = A[q * np + j];
         A[p * np + j] = c * ap - s * aq;
         A[q * np + j] = s * ap + c * aq;
-        double vp = Vt[p * np + j], vq = Vt[q * np + j];
+        T vp = Vt[p * np + j], vq = Vt[q * np + j];
         Vt[p * np + j] = c * vp - s * vq;
         Vt[q * np + j] = s * vp + c * vq;
       }
       __syncthreads();
       // columns of A
       for (int i = threadIdx.x; i < half * np; i += blockDim.x) {
-        int k = i % half, j = i / half;
-        double c = sh.rc[k], s = sh.rs[k];
-        if (s == 0.0) continue;
+        int j = i / half, k = i - j * half;
+        if (sh.rskip[k]) continue;
+        T c = ((T*)sh.rc)[k], s = ((T*)sh.rs)[k];
         int p = sh.rp[k], q = sh.rq[k];
-        double ap = A[j * np + p], aq = A[j * np + q];
+        T ap = A[j * np + p], aq = A[j * np + q];
         A[j * np + p] = c * ap - s * aq;
         A[j * np + q] = s * ap + c * aq;
       }
       __syncthreads();
     }
-    offmax = cta_max(offmax, sh.red);
-    if (offmax <= tol) return sweep + 1;
+    double om = cta_max((double)offmax, sh.red);
+    if (om <= (double)tol) return sweep + 1;
   }
   return -1;
 }
@@ -534,7 +547,17 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 
 // ---------------------------------------------------------------------------
 // the SCC kernel
+//
+// MIXED = 0: every iteration in FP64.
+// MIXED = 1: iterations run the transforms, the Jacobi eigensolve and the
+//   density in FP32 until the moment residual drops below kMixedSwitch; the
+//   remaining iterations (and always the final one) are FP64, warm-started
+//   from the FP32 eigenvectors after one Newton-Schulz re-orthonormalisation.
+//   Potentials, Fermi level, moments, Broyden and energies are FP64 always.
 // ---------------------------------------------------------------------------
+constexpr double kMixedSwitch = 3e-5;
+
+template <int MIXED>
 __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
   extern __shared__ __align__(16) char smem_raw[];
   const int mol = blockIdx.x;
@@ -570,10 +593,16 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
   double* xin = vec + mv.vl.xin;
   double* xout = vec + mv.vl.xout;
   const int mode = jacobi_mode(n, (size_t)bt.smem_bytes);
-  // Jacobi working storage (np x np each): shared memory when it fits, else
-  // the A slot and the T slot (T is free once A = X^T F X is formed).
+  // FP64 Jacobi storage: shared memory when it fits, else the A / V slots.
   double* JA = (mode <= 1) ? sh.jac : Ag;
-  double* JV = (mode == 0) ? sh.jac + (long long)np * np : T;
+  double* JV = (mode == 0) ? sh.jac + (long long)np * np : Vg;
+  // FP32 storage (mixed): both matrices inside the FP64 A region; X32 and the
+  // FP32 coefficients live in the W and C slots until the FP64 phase.
+  float* JA32 = (float*)JA;
+  float* JV32 = (float*)JA + (long long)np * np;
+  float* T32 = (float*)T;
+  float* X32 = (float*)Wm;
+  float* C32 = (float*)C;
 
   // --- per-AO maps -------------------------------------------------------
   const int* sh_atom = bt.sh_atom + md.sh_off;
@@ -660,9 +689,8 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     }
     return;
   }
-  // Linv (lower) by forward substitution, one column per thread; X = Linv^T
+  // X = L^-T: row j of X = column j of L^-1, one forward substitution per thread
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    // X[j][i] = Linv[i][j]
     X[(long long)j * n + j] = 1.0 / T[(long long)j * n + j];
     for (int i = 0; i < j; ++i) X[(long long)j * n + i] = 0.0;
     for (int i = j + 1; i < n; ++i) {
@@ -671,13 +699,18 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       X[(long long)j * n + i] = s / T[(long long)i * n + i];
     }
   }
-  // X currently holds Linv^T row j = column j of Linv -> X[j][i] = Linv[i][j] = (L^-T)[j][i]. Done.
+  __syncthreads();
+  if (MIXED)
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) X32[e] = (float)X[e];
   for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = 0.0;
   __syncthreads();
 
   double en[5];
   double eprev = 0.0, eel = 0.0, ets = 0.0, eband = 0.0, efermi = 0.0;
   int it, converged = 0, eig_fail = 0;
+  bool fp32_phase = MIXED != 0 && bt.max_iter > 8;
+  bool have64 = false;  // JV holds an orthonormal FP64 basis from a previous iteration
+  bool have32 = false;  // JV32 holds FP32 eigenvectors from a previous iteration
   for (it = 1; it <= bt.max_iter; ++it) {
     potentials(mv, xin, en, sh.red);
     // Fock matrix
@@ -698,41 +731,101 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       }
     }
     __syncthreads();
-    // A = X^T F X  (T = F X, then X^T T into the Jacobi matrix with ld np)
-    cta_gemm(n, n, n, F, n, false, X, n, false, T, n);
-    __syncthreads();
-    cta_gemm(n, n, n, X, n, true, T, n, false, JA, np);
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-      int i = e / n, j = e % n;
-      if (j < i) {
-        double s = 0.5 * (JA[i * np + j] + JA[j * np + i]);
-        JA[i * np + j] = s;
-        JA[j * np + i] = s;
+    int nocc = 0;
+    if (fp32_phase) {
+      // ---- FP32 iteration ----
+      cta_gemm<double, float, float, float>(n, n, n, F, n, false, X32, n, false, T32, n);
+      __syncthreads();
+      cta_gemm<float, float, float, float>(n, n, n, X32, n, true, T32, n, false, JA32, np);
+      __syncthreads();
+      if (have32) {
+        // B = V A V^T in the previous eigenvector basis
+        cta_gemm<float, float, float, float>(n, n, n, JA32, np, false, JV32, np, true, T32, n);
+        __syncthreads();
+        cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, T32, n, false, JA32, np);
+        __syncthreads();
       }
-    }
-    __syncthreads();
-    int sweeps = jacobi(JA, JV, n, sh, 50);
-    if (sweeps < 0) eig_fail = 1;
-    // sort eigenvalues
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      double di = JA[i * np + i];
-      int rank = 0;
-      for (int j = 0; j < n; ++j) {
-        double dj = JA[j * np + j];
-        rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        int i = e / n, j = e % n;
+        if (j < i) {
+          float s = 0.5f * (JA32[i * np + j] + JA32[j * np + i]);
+          JA32[i * np + j] = s;
+          JA32[j * np + i] = s;
+        }
       }
-      sh.perm[rank] = i;
-      eps[rank] = di;
+      __syncthreads();
+      jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, 30);
+      have32 = true;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float di = JA32[i * np + i];
+        int rank = 0;
+        for (int j = 0; j < n; ++j) {
+          float dj = JA32[j * np + j];
+          rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
+        }
+        sh.perm[rank] = i;
+        eps[rank] = (double)di;
+      }
+      __syncthreads();
+      // C32 = X32 V32^T (columns in Jacobi order)
+      cta_gemm<float, float, float, float>(n, n, n, X32, n, false, JV32, np, true, C32, n);
+    } else {
+      // ---- FP64 iteration ----
+      if (MIXED && !have64 && have32) {
+        // FP32 eigenvectors -> FP64 basis with one Newton-Schulz step
+        // V <- (3I - V V^T) V / 2. This runs before A is formed because the
+        // FP32 matrices live inside the FP64 A storage.
+        for (long long e = threadIdx.x; e < (long long)np * np; e += blockDim.x) JV[e] = (double)JV32[e];
+        __syncthreads();
+        cta_gemm<double, double, double, double>(n, n, n, JV, np, false, JV, np, true, T, n);
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+          int i = e / n, j = e % n;
+          T[e] = (i == j ? 1.5 : 0.0) - 0.5 * T[e];
+        }
+        __syncthreads();
+        cta_gemm<double, double, double, double>(n, n, n, T, n, false, JV, np, false, C, n);
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = C[e];
+        __syncthreads();
+        have64 = true;
+      }
+      cta_gemm<double, double, double, double>(n, n, n, F, n, false, X, n, false, T, n);
+      __syncthreads();
+      cta_gemm<double, double, double, double>(n, n, n, X, n, true, T, n, false, JA, np);
+      __syncthreads();
+      if (have64) {
+        cta_gemm<double, double, double, double>(n, n, n, JA, np, false, JV, np, true, T, n);
+        __syncthreads();
+        cta_gemm<double, double, double, double>(n, n, n, JV, np, false, T, n, false, JA, np);
+        __syncthreads();
+      }
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        int i = e / n, j = e % n;
+        if (j < i) {
+          double s = 0.5 * (JA[i * np + j] + JA[j * np + i]);
+          JA[i * np + j] = s;
+          JA[j * np + i] = s;
+        }
+      }
+      __syncthreads();
+      int sweeps = jacobi<double>(JA, JV, n, have64, 1e-12, sh, 50);
+      if (sweeps < 0) eig_fail = 1;
+      have64 = true;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double di = JA[i * np + i];
+        int rank = 0;
+        for (int j = 0; j < n; ++j) {
+          double dj = JA[j * np + j];
+          rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
+        }
+        sh.perm[rank] = i;
+        eps[rank] = di;
+      }
+      __syncthreads();
+      // C = X V^T (columns in Jacobi order)
+      cta_gemm<double, double, double, double>(n, n, n, X, n, false, JV, np, true, C, n);
     }
-    __syncthreads();
-    // V (sorted eigenvectors as rows, ld n) into Vg; C = X V^T
-    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-      int k = (int)(e / n), l = (int)(e % n);
-      Vg[e] = JV[(long long)sh.perm[k] * np + l];
-    }
-    __syncthreads();
-    cta_gemm(n, n, n, X, n, false, Vg, n, true, C, n);
     if (threadIdx.x < 32) {
       double ef;
       double ts = fermi_warp(n, eps, nel, md.kT, focc, &ef);
@@ -744,15 +837,24 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     __syncthreads();
     ets = sh.scal[0];
     efermi = sh.scal[1];
-    int nocc = 0;
     for (int k = 0; k < n; ++k)
       if (focc[k] > 0.0) nocc = k + 1;
-    // P = C f C^T
+    // P = C f C^T over the occupied (sorted) orbitals
     for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
       int i = (int)(e / n), j = (int)(e % n);
       if (j < i) continue;
       double p = 0.0;
-      for (int k = 0; k < nocc; ++k) p += focc[k] * C[(long long)i * n + k] * C[(long long)j * n + k];
+      if (fp32_phase) {
+        for (int k = 0; k < nocc; ++k) {
+          int c = sh.perm[k];
+          p += focc[k] * (double)(C32[(long long)i * n + c] * C32[(long long)j * n + c]);
+        }
+      } else {
+        for (int k = 0; k < nocc; ++k) {
+          int c = sh.perm[k];
+          p += focc[k] * C[(long long)i * n + c] * C[(long long)j * n + c];
+        }
+      }
       Pm[(long long)i * n + j] = p;
       Pm[(long long)j * n + i] = p;
     }
@@ -795,6 +897,7 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       __syncthreads();
     }
     potentials(mv, xout, en, sh.red);
+    bool stop = false;
     {
       double acc[2] = {0.0, 0.0};
       for (long long e = threadIdx.x; e < nn; e += blockDim.x) acc[0] += Pm[e] * H0[e];
@@ -808,16 +911,20 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       eel = eband + en[0] + en[1] + en[2] + en[3] + en[4] + ets;
       double de = fabs(eel - eprev);
       eprev = eel;
-      if (it > 1 && de < bt.econv && res < bt.pconv) {
+      if (fp32_phase) {
+        // hand over to FP64 once the FP32 iterations reach their noise floor
+        if (it > 1 && res < kMixedSwitch) fp32_phase = false;
+        if (it >= bt.max_iter - 8) fp32_phase = false;
+      } else if (it > 1 && de < bt.econv && res < bt.pconv) {
         converged = 1;
-        break;
+        stop = true;
       }
     }
-    if (it == bt.max_iter) break;
+    if (stop || it == bt.max_iter) break;
     broyden(mv, xin, xout, it - 1, bt.mix_alpha, sh);
   }
   if (it > bt.max_iter) it = bt.max_iter;
-  // energy-weighted density W = C f e C^T
+  // energy-weighted density W = C f e C^T (FP64 coefficients of the last iteration)
   int nocc = 0;
   for (int k = 0; k < n; ++k)
     if (focc[k] > 0.0) nocc = k + 1;
@@ -825,7 +932,10 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     int i = (int)(e / n), j = (int)(e % n);
     if (j < i) continue;
     double w = 0.0;
-    for (int k = 0; k < nocc; ++k) w += focc[k] * eps[k] * C[(long long)i * n + k] * C[(long long)j * n + k];
+    for (int k = 0; k < nocc; ++k) {
+      int c = sh.perm[k];
+      w += focc[k] * eps[k] * C[(long long)i * n + c] * C[(long long)j * n + c];
+    }
     Wm[(long long)i * n + j] = w;
     Wm[(long long)j * n + i] = w;
   }
@@ -852,13 +962,16 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
 }
 
 void launch_scc(const DevBatch& bt, int precision, cudaStream_t st) {
-  (void)precision;
   static int configured = 0;
   if (!configured) {
-    cudaFuncSetAttribute(k_scc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
+    cudaFuncSetAttribute(k_scc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
+    cudaFuncSetAttribute(k_scc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
     configured = 1;
   }
-  k_scc<<<bt.nmol, kSccThreads, bt.smem_bytes, st>>>(bt);
+  if (precision == 1)
+    k_scc<1><<<bt.nmol, kSccThreads, bt.smem_bytes, st>>>(bt);
+  else
+    k_scc<0><<<bt.nmol, kSccThreads, bt.smem_bytes, st>>>(bt);
 }
 
 }  // namespace qcx
