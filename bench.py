@@ -191,6 +191,7 @@ def run_gpu(args):
     dt = DT_FS * constants.FSTOAU
     mols = workload(rank, args.ntraj)
     b = qg.Batch(mols, etemp=ETEMP)
+    b.set_precision(args.precision)
     b.egrad()
     b.sync()
     stream = torch.cuda.ExternalStream(b.stream())
@@ -264,6 +265,7 @@ def run_gpu(args):
     prof = [b.profile_egrad() for _ in range(3)]
     scc_ms = statistics.median(p["scc"] for p in prof)
     iters = b.get()["iters"].astype(np.float64)
+    it64 = np.array([b.energy_terms(i)["iters_fp64"] for i in range(b.nmol)])
     act, _ = b.progress()
     flops = scc_flops(nao[act > 0], iters[act > 0])
     achieved = flops / (scc_ms * 1e-3) / 1e12
@@ -285,8 +287,9 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs, FP64, one CUDA graph "
                                    "per MD step", "ntraj_per_gpu": b.nmol, "atoms": [NMIN, NMAX],
-                       "etemp_K": ETEMP, "precision": "fp64", "l2": "flushed between timed steps (256 MiB write)",
+                       "etemp_K": ETEMP, "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)",
                        "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters)),
+                       "mean_scc_iters_fp64": float(np.mean(it64)),
                        "active_trajectories": int(np.sum(act))},
             "e2e": {"value": e2e, "unit": "trajectory-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -314,6 +317,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ntraj", type=int, default=None, help="smaller batch for profiling runs (default 256)")
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

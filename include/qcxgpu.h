@@ -97,7 +97,7 @@ int qcx_batch_get(qcx_batch* b, double* xyz, double* vel, double* grad, double* 
 
 /* Energy decomposition of molecule i: band, isotropic ES, third order,
  * anisotropic ES, multipole XC, dispersion, three-body, repulsion, -TS,
- * total, Fermi level (11 doubles). */
+ * total, Fermi level, number of FP64 SCC iterations (12 doubles). */
 int qcx_batch_get_energy_terms(qcx_batch* b, int i, double* terms);
 
 /* Dense matrices of molecule i for inspection: which = 0 S, 1 H0, 8 P,

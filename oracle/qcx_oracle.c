@@ -841,7 +841,8 @@ static double atm_energy_grad(const mol_t* m, const es_t* e, double* grad, doubl
 }
 
 /* ------------------------------------------------------------------------ */
-/* modified Broyden mixing (D. D. Johnson, PRB 38, 12807 (1988))              */
+/* modified Broyden mixing (D. D. Johnson, PRB 38, 12807 (1988)) over a      */
+/* sliding window of the last QCX_BROYDEN_WINDOW iterations                   */
 /* ------------------------------------------------------------------------ */
 typedef struct {
   int len, maxit, it;
@@ -890,7 +891,8 @@ static void broyden_step(broyden_t* b, double* x, const double* xout) {
   if (it == 0) {
     for (int i = 0; i < len; ++i) { b->xlast[i] = x[i]; b->flast[i] = f[i]; x[i] += b->alpha * f[i]; }
   } else {
-    int m = it - 1; /* new history index */
+    int m = (it - 1) % b->maxit; /* history slot (sliding window of maxit entries) */
+    int k = it < b->maxit ? it : b->maxit; /* valid slots */
     double* dfm = b->df + (size_t)m * len;
     double* um = b->u + (size_t)m * len;
     double nrm = 0.0;
@@ -901,13 +903,12 @@ static void broyden_step(broyden_t* b, double* x, const double* xout) {
       dfm[i] /= nrm;
       um[i] = b->alpha * dfm[i] + (x[i] - b->xlast[i]) / nrm;
     }
-    for (int j = 0; j <= m; ++j) {
+    for (int j = 0; j < k; ++j) {
       double s = 0.0;
       const double* dfj = b->df + (size_t)j * len;
       for (int i = 0; i < len; ++i) s += dfj[i] * dfm[i];
       b->a[j * b->maxit + m] = s; b->a[m * b->maxit + j] = s;
     }
-    int k = m + 1;
     double* M = malloc(sizeof(double) * k * k);
     double* c = malloc(sizeof(double) * k);
     for (int i = 0; i < k; ++i) {
@@ -1025,7 +1026,7 @@ static int run_scc(int nat, const int* Z, const double* xyz, double charge, doub
   double* V = malloc(sizeof(double) * nn);
   double* C = malloc(sizeof(double) * nn);
   broyden_t br;
-  broyden_init(&br, len, o->max_iter, o->broyden_alpha);
+  broyden_init(&br, len, QCX_BROYDEN_WINDOW, o->broyden_alpha);
   double eprev = 0.0;
   c->converged = 0;
   int it;

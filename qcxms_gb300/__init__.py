@@ -181,9 +181,9 @@ class Batch:
                 "status": status, "iters": iters}
 
     def energy_terms(self, i):
-        t = np.zeros(11)
+        t = np.zeros(12)
         self._check(self._lib.qcx_batch_get_energy_terms(self._h, int(i), _dp(t)), "energy_terms")
-        names = ["band", "ies", "e3", "aes", "axc", "disp", "atm", "rep", "ts", "total", "efermi"]
+        names = ["band", "ies", "e3", "aes", "axc", "disp", "atm", "rep", "ts", "total", "efermi", "iters_fp64"]
         return dict(zip(names, t))
 
     def matrix(self, i, which):

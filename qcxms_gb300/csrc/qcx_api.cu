@@ -170,7 +170,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
     md.nsh = (int)sh_atom.size() - md.sh_off;
     md.nao = nao;
     md.len = md.nsh + 9 * md.nat;
-    md.nmem = QCX_SCC_MAXITER;
+    md.nmem = QCX_BROYDEN_WINDOW;
     md.nel = nel;
     md.kT = etemp[m] * QCX_KTOAU;
     md.charge = charge[m];

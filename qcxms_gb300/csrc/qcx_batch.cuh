@@ -22,7 +22,7 @@ enum MatSlot {
 
 // per-molecule energy terms
 enum EnergySlot {
-  kEBand = 0, kEIes, kE3, kEAes, kEAxc, kEDisp, kEAtm, kERep, kETs, kETotal, kEFermi, kNumEnergy
+  kEBand = 0, kEIes, kE3, kEAes, kEAxc, kEDisp, kEAtm, kERep, kETs, kETotal, kEFermi, kIters64, kNumEnergy
 };
 
 // per-molecule status bits

@@ -19,6 +19,8 @@
 #define QCX_SCC_PCONV 1.0e-6
 #define QCX_BROYDEN_ALPHA 0.4
 #define QCX_BROYDEN_W0 0.01
+/* Broyden history: the last QCX_BROYDEN_WINDOW iterations */
+#define QCX_BROYDEN_WINDOW 24
 
 /* Fermi level bisection: fixed iteration count for reproducibility */
 #define QCX_FERMI_ITERS 200

@@ -436,8 +436,9 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
     __syncthreads();
     return;
   }
-  int m = it - 1;
-  if (m >= nmem) m = nmem - 1;  // history full: overwrite the newest slot
+  // sliding window: slot of this update, number of valid slots
+  int m = (it - 1) % nmem;
+  int k = it < nmem ? it : nmem;
   double* dfm = df + (long long)m * len;
   double* um = u + (long long)m * len;
   double nrm[1] = {0.0};
@@ -455,7 +456,6 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
     um[i] = alpha * dfm[i] + (x[i] - xl[i]) / nr;
   }
   __syncthreads();
-  int k = m + 1;
   // a[j][m] = df_j . df_m ; c_j = df_j . f   (one warp per j)
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = w; j < k; j += kWarps) {
@@ -546,6 +546,84 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 }
 
 // ---------------------------------------------------------------------------
+// GEMM-form FP64 eigenvector refinement in a nearly diagonal basis.
+//
+// JA holds B = C^T F C (ld np) for the current coefficient rows JV (= C^T,
+// S-orthonormal). First-order perturbation theory gives the eigenvectors of
+// B as I + K with K_ij = B_ij / (B_jj - B_ii), so C^T <- (I + K^T) C^T, and
+// the eigenvalues as B_jj + sum_i B_ij K_ij. Each pass leaves an error of
+// order max|K|^2; passes repeat (recomputing B) until max|K| < 1e-7, i.e. the
+// eigenvectors are exact to ~1e-14. Returns false (nothing changed) when the
+// basis is too far from diagonal (max|K| > 1e-2); the caller then uses Jacobi.
+// On success JA's diagonal holds the eigenvalues.
+// ---------------------------------------------------------------------------
+__device__ bool refine64(double* JA, double* JV, const double* F, const double* S, double* T, double* C, double* tmp,
+                         int n, SccShared& sh) {
+  const int np = n + (n & 1);
+  for (int pass = 0; pass < 3; ++pass) {
+    if (pass > 0) {
+      // recompute B for the updated basis
+      cta_gemm<double, double, double, double>(n, n, n, F, n, false, JV, np, true, T, n);
+      __syncthreads();
+      cta_gemm<double, double, double, double>(n, n, n, JV, np, false, T, n, false, JA, np);
+      __syncthreads();
+    }
+    // K^T[j][i] = K_ij = B_ij / (B_jj - B_ii) into T (ld n)
+    double kmax = 0.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      int j = e / n, i = e - j * n;
+      double k = 0.0;
+      if (i != j) {
+        double b = 0.5 * (JA[i * np + j] + JA[j * np + i]);
+        double d = JA[j * np + j] - JA[i * np + i];
+        if (b != 0.0) k = (fabs(d) > 1e-300) ? b / d : 1e300;
+      }
+      T[e] = k;
+      kmax = fmax(kmax, fabs(k));
+    }
+    kmax = cta_max(kmax, sh.red);
+    if (kmax > 1e-2) {
+      if (pass == 0) return false;
+      break;  // should not happen after a successful first pass; caller's Jacobi would be needed
+    }
+    // second-order eigenvalues into tmp, then onto the diagonal of B
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      double lam = JA[j * np + j];
+      for (int i = 0; i < n; ++i)
+        if (i != j) lam += 0.5 * (JA[i * np + j] + JA[j * np + i]) * T[(long long)j * n + i];
+      tmp[j] = lam;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x) JA[j * np + j] = tmp[j];
+    if (kmax == 0.0) return true;
+    // C^T <- C^T + K^T C^T
+    cta_gemm<double, double, double, double>(n, n, n, T, n, false, JV, np, false, C, n);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] += C[e];
+    __syncthreads();
+    if (kmax > 1e-7) {
+      // restore S-orthonormality: C^T <- (3I - C^T S C)/2 C^T
+      cta_gemm<double, double, double, double>(n, n, n, S, n, false, JV, np, true, T, n);
+      __syncthreads();
+      cta_gemm<double, double, double, double>(n, n, n, JV, np, false, T, n, false, C, n);
+      __syncthreads();
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        int i = e / n, j = e % n;
+        C[e] = (i == j ? 1.5 : 0.0) - 0.5 * C[e];
+      }
+      __syncthreads();
+      cta_gemm<double, double, double, double>(n, n, n, C, n, false, JV, np, false, T, n);
+      __syncthreads();
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = T[e];
+      __syncthreads();
+    } else {
+      return true;
+    }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // the SCC kernel
 //
 // MIXED = 0: every iteration in FP64.
@@ -555,7 +633,24 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 //   from the FP32 eigenvectors after one Newton-Schulz re-orthonormalisation.
 //   Potentials, Fermi level, moments, Broyden and energies are FP64 always.
 // ---------------------------------------------------------------------------
-constexpr double kMixedSwitch = 3e-5;
+constexpr double kMixedSwitch = 1e-4;
+
+// Optional per-phase cycle counters (diagnostic builds only: -DQCX_SCC_PHASE_TIMING).
+#ifdef QCX_SCC_PHASE_TIMING
+__device__ unsigned long long g_phase_cycles[16];
+#define PHASE_BEGIN() long long _pt = clock64()
+#define PHASE_MARK(i)                                                 \
+  do {                                                                \
+    if (threadIdx.x == 0) {                                           \
+      long long _n = clock64();                                       \
+      atomicAdd(&g_phase_cycles[i], (unsigned long long)(_n - _pt)); \
+      _pt = _n;                                                       \
+    }                                                                 \
+  } while (0)
+#else
+#define PHASE_BEGIN()
+#define PHASE_MARK(i)
+#endif
 
 template <int MIXED>
 __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
@@ -602,7 +697,6 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
   float* JV32 = (float*)JA + (long long)np * np;
   float* T32 = (float*)T;
   float* X32 = (float*)Wm;
-  float* C32 = (float*)C;
 
   // --- per-AO maps -------------------------------------------------------
   const int* sh_atom = bt.sh_atom + md.sh_off;
@@ -711,8 +805,15 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
   bool fp32_phase = MIXED != 0 && bt.max_iter > 8;
   bool have64 = false;  // JV holds an orthonormal FP64 basis from a previous iteration
   bool have32 = false;  // JV32 holds FP32 eigenvectors from a previous iteration
+  int bro_it = 0;       // Broyden updates since the last (re)start of the mixer
+  double best32 = 1e300;  // best residual seen in the FP32 phase
+  int stall32 = 0;
+  int n64 = 0;          // FP64 iterations done
+  PHASE_BEGIN();
   for (it = 1; it <= bt.max_iter; ++it) {
+    PHASE_MARK(15);
     potentials(mv, xin, en, sh.red);
+    PHASE_MARK(0);
     // Fock matrix
     {
       const double* vsh = vec + mv.vl.vsh;
@@ -731,16 +832,21 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       }
     }
     __syncthreads();
+    PHASE_MARK(1);
     int nocc = 0;
+    // JV / JV32 hold C^T: row k is the AO coefficient vector of MO k
+    // (S-orthonormal). After the first iteration the Fock matrix is expressed
+    // in the previous MO basis, B = C^T F C, which is nearly diagonal, and the
+    // Jacobi rotations update C^T in place.
     if (fp32_phase) {
       // ---- FP32 iteration ----
-      cta_gemm<double, float, float, float>(n, n, n, F, n, false, X32, n, false, T32, n);
-      __syncthreads();
-      cta_gemm<float, float, float, float>(n, n, n, X32, n, true, T32, n, false, JA32, np);
-      __syncthreads();
-      if (have32) {
-        // B = V A V^T in the previous eigenvector basis
-        cta_gemm<float, float, float, float>(n, n, n, JA32, np, false, JV32, np, true, T32, n);
+      if (!have32) {
+        cta_gemm<double, float, float, float>(n, n, n, F, n, false, X32, n, false, T32, n);
+        __syncthreads();
+        cta_gemm<float, float, float, float>(n, n, n, X32, n, true, T32, n, false, JA32, np);
+        __syncthreads();
+      } else {
+        cta_gemm<double, float, float, float>(n, n, n, F, n, false, JV32, np, true, T32, n);
         __syncthreads();
         cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, T32, n, false, JA32, np);
         __syncthreads();
@@ -754,8 +860,16 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
         }
       }
       __syncthreads();
-      jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, 30);
-      have32 = true;
+      PHASE_MARK(2);
+      jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? 8 : 30);
+      PHASE_MARK(3);
+      if (!have32) {
+        // eigenvectors of X^T F X -> C^T = V X^T
+        cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, X32, n, true, T32, n);
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV32[(e / n) * np + (e % n)] = T32[e];
+        have32 = true;
+      }
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         float di = JA32[i * np + i];
         int rank = 0;
@@ -767,35 +881,40 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
         eps[rank] = (double)di;
       }
       __syncthreads();
-      // C32 = X32 V32^T (columns in Jacobi order)
-      cta_gemm<float, float, float, float>(n, n, n, X32, n, false, JV32, np, true, C32, n);
     } else {
       // ---- FP64 iteration ----
-      if (MIXED && !have64 && have32) {
-        // FP32 eigenvectors -> FP64 basis with one Newton-Schulz step
-        // V <- (3I - V V^T) V / 2. This runs before A is formed because the
-        // FP32 matrices live inside the FP64 A storage.
-        for (long long e = threadIdx.x; e < (long long)np * np; e += blockDim.x) JV[e] = (double)JV32[e];
-        __syncthreads();
-        cta_gemm<double, double, double, double>(n, n, n, JV, np, false, JV, np, true, T, n);
-        __syncthreads();
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-          int i = e / n, j = e % n;
-          T[e] = (i == j ? 1.5 : 0.0) - 0.5 * T[e];
+      bool cold = false;
+      if (!have64) {
+        if (MIXED && have32) {
+          // FP32 coefficients -> FP64, re-orthonormalised in the S metric with
+          // one Newton-Schulz step C^T <- (3I - C^T S C)/2 C^T. The FP32
+          // matrices live inside the FP64 A storage, so this precedes any use of A.
+          for (long long e = threadIdx.x; e < (long long)np * np; e += blockDim.x) JV[e] = (double)JV32[e];
+          __syncthreads();
+          cta_gemm<double, double, double, double>(n, n, n, S, n, false, JV, np, true, T, n);
+          __syncthreads();
+          cta_gemm<double, double, double, double>(n, n, n, JV, np, false, T, n, false, C, n);
+          __syncthreads();
+          for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            int i = e / n, j = e % n;
+            C[e] = (i == j ? 1.5 : 0.0) - 0.5 * C[e];
+          }
+          __syncthreads();
+          cta_gemm<double, double, double, double>(n, n, n, C, n, false, JV, np, false, T, n);
+          __syncthreads();
+          for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = T[e];
+          __syncthreads();
+        } else {
+          cold = true;
         }
-        __syncthreads();
-        cta_gemm<double, double, double, double>(n, n, n, T, n, false, JV, np, false, C, n);
-        __syncthreads();
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = C[e];
-        __syncthreads();
-        have64 = true;
       }
-      cta_gemm<double, double, double, double>(n, n, n, F, n, false, X, n, false, T, n);
-      __syncthreads();
-      cta_gemm<double, double, double, double>(n, n, n, X, n, true, T, n, false, JA, np);
-      __syncthreads();
-      if (have64) {
-        cta_gemm<double, double, double, double>(n, n, n, JA, np, false, JV, np, true, T, n);
+      if (cold) {
+        cta_gemm<double, double, double, double>(n, n, n, F, n, false, X, n, false, T, n);
+        __syncthreads();
+        cta_gemm<double, double, double, double>(n, n, n, X, n, true, T, n, false, JA, np);
+        __syncthreads();
+      } else {
+        cta_gemm<double, double, double, double>(n, n, n, F, n, false, JV, np, true, T, n);
         __syncthreads();
         cta_gemm<double, double, double, double>(n, n, n, JV, np, false, T, n, false, JA, np);
         __syncthreads();
@@ -809,8 +928,18 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
         }
       }
       __syncthreads();
-      int sweeps = jacobi<double>(JA, JV, n, have64, 1e-12, sh, 50);
-      if (sweeps < 0) eig_fail = 1;
+      PHASE_MARK(4);
+      bool refined = !cold && refine64(JA, JV, F, S, T, C, eps, n, sh);
+      if (!refined) {
+        int sweeps = jacobi<double>(JA, JV, n, !cold, 1e-12, sh, cold ? 50 : 20);
+        if (sweeps < 0) eig_fail = 1;
+      }
+      PHASE_MARK(5);
+      if (cold) {
+        cta_gemm<double, double, double, double>(n, n, n, JV, np, false, X, n, true, T, n);
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = T[e];
+      }
       have64 = true;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double di = JA[i * np + i];
@@ -823,9 +952,8 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
         eps[rank] = di;
       }
       __syncthreads();
-      // C = X V^T (columns in Jacobi order)
-      cta_gemm<double, double, double, double>(n, n, n, X, n, false, JV, np, true, C, n);
     }
+    PHASE_MARK(6);
     if (threadIdx.x < 32) {
       double ef;
       double ts = fermi_warp(n, eps, nel, md.kT, focc, &ef);
@@ -839,26 +967,30 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     efermi = sh.scal[1];
     for (int k = 0; k < n; ++k)
       if (focc[k] > 0.0) nocc = k + 1;
+    PHASE_MARK(7);
     // P = C f C^T over the occupied (sorted) orbitals
     for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
       int i = (int)(e / n), j = (int)(e % n);
       if (j < i) continue;
       double p = 0.0;
       if (fp32_phase) {
+        float pf = 0.0f;
         for (int k = 0; k < nocc; ++k) {
           int c = sh.perm[k];
-          p += focc[k] * (double)(C32[(long long)i * n + c] * C32[(long long)j * n + c]);
+          pf += (float)focc[k] * JV32[(long long)c * np + i] * JV32[(long long)c * np + j];
         }
+        p = (double)pf;
       } else {
         for (int k = 0; k < nocc; ++k) {
           int c = sh.perm[k];
-          p += focc[k] * C[(long long)i * n + c] * C[(long long)j * n + c];
+          p += focc[k] * JV[(long long)c * np + i] * JV[(long long)c * np + j];
         }
       }
       Pm[(long long)i * n + j] = p;
       Pm[(long long)j * n + i] = p;
     }
     __syncthreads();
+    PHASE_MARK(8);
     // moments: per-AO rows (one warp per row)
     {
       int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -896,7 +1028,9 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       }
       __syncthreads();
     }
+    PHASE_MARK(9);
     potentials(mv, xout, en, sh.red);
+    PHASE_MARK(10);
     bool stop = false;
     {
       double acc[2] = {0.0, 0.0};
@@ -912,16 +1046,31 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       double de = fabs(eel - eprev);
       eprev = eel;
       if (fp32_phase) {
-        // hand over to FP64 once the FP32 iterations reach their noise floor
-        if (it > 1 && res < kMixedSwitch) fp32_phase = false;
-        if (it >= bt.max_iter - 8) fp32_phase = false;
-      } else if (it > 1 && de < bt.econv && res < bt.pconv) {
-        converged = 1;
-        stop = true;
+        // hand over to FP64 once the FP32 iterations reach their noise floor;
+        // the FP64 iterations restart the Broyden mixer from the current point
+        // (or once the FP32 residual has stopped improving below 1e-3)
+        if (res < 0.9 * best32) {
+          best32 = res;
+          stall32 = 0;
+        } else {
+          ++stall32;
+        }
+        if ((it > 1 && res < kMixedSwitch) || (stall32 >= 4 && res < 1e-3) || it >= bt.max_iter - 12)
+          fp32_phase = false;
+      } else {
+        ++n64;
+        // convergence needs two FP64 iterations so that dE compares FP64 energies
+        if (it > 1 && (n64 >= 2 || !MIXED) && de < bt.econv && res < bt.pconv) {
+          converged = 1;
+          stop = true;
+        }
       }
     }
+    PHASE_MARK(11);
     if (stop || it == bt.max_iter) break;
-    broyden(mv, xin, xout, it - 1, bt.mix_alpha, sh);
+    broyden(mv, xin, xout, bro_it, bt.mix_alpha, sh);
+    ++bro_it;
+    PHASE_MARK(12);
   }
   if (it > bt.max_iter) it = bt.max_iter;
   // energy-weighted density W = C f e C^T (FP64 coefficients of the last iteration)
@@ -934,7 +1083,7 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     double w = 0.0;
     for (int k = 0; k < nocc; ++k) {
       int c = sh.perm[k];
-      w += focc[k] * eps[k] * C[(long long)i * n + c] * C[(long long)j * n + c];
+      w += focc[k] * eps[k] * JV[(long long)c * np + i] * JV[(long long)c * np + j];
     }
     Wm[(long long)i * n + j] = w;
     Wm[(long long)j * n + i] = w;
@@ -951,6 +1100,7 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     E[kEDisp] = en[4];
     E[kETs] = ets;
     E[kEFermi] = efermi;
+    E[kIters64] = (double)(MIXED ? n64 : it);
     E[kETotal] = eel;  // electronic part; three-body and repulsion added by the gradient kernel
     int st = 0;
     if (!converged) st |= kSccNotConverged;
@@ -960,6 +1110,19 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     bt.iters[mol] = it;
   }
 }
+
+#ifdef QCX_SCC_PHASE_TIMING
+}  // namespace qcx
+extern "C" int qcx_debug_phase_cycles(unsigned long long* out, int reset) {
+  if (cudaMemcpyFromSymbol(out, qcx::g_phase_cycles, sizeof(unsigned long long) * 16) != cudaSuccess) return -1;
+  if (reset) {
+    unsigned long long z[16] = {0};
+    cudaMemcpyToSymbol(qcx::g_phase_cycles, z, sizeof(z));
+  }
+  return 0;
+}
+namespace qcx {
+#endif
 
 void launch_scc(const DevBatch& bt, int precision, cudaStream_t st) {
   static int configured = 0;

@@ -143,11 +143,12 @@ def test_gradient_central_differences(oracle_lib, name):
 
 def test_translation_rotation_invariance(oracle_lib):
     Z, xyz, charge = molecules.c6h12o2()
-    rc, e, g, q, _ = oracle_lib.egrad(Z, xyz, charge)
+    o = oracle_lib.default_opts(**TIGHT)
+    rc, e, g, q, _ = oracle_lib.egrad(Z, xyz, charge, opts=o)
     assert np.abs(g.sum(0)).max() < 1e-10
     th = 0.7
     R = np.array([[math.cos(th), -math.sin(th), 0], [math.sin(th), math.cos(th), 0], [0, 0, 1]])
-    rc2, e2, g2, q2, _ = oracle_lib.egrad(Z, xyz @ R.T + np.array([1.0, -2.0, 0.5]), charge)
+    rc2, e2, g2, q2, _ = oracle_lib.egrad(Z, xyz @ R.T + np.array([1.0, -2.0, 0.5]), charge, opts=o)
     assert abs(e - e2) < 1e-8
     assert np.abs(g @ R.T - g2).max() < 1e-6
     assert abs(q.sum() - charge) < 1e-10
