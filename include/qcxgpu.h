@@ -130,6 +130,26 @@ int qcx_batch_profile_egrad(qcx_batch* b, float* ms);
  * used to count algorithmic work. */
 int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat);
 
+/*
+ * Allocation-free variant of qcx_egrad for callers that cannot call
+ * cudaMalloc (for example a host program whose device memory belongs to
+ * another runtime's capped pool, or a path that must not trigger the device
+ * synchronisation an allocation implies). It has no counterpart in the
+ * reference. Same arguments, meaning and return codes as qcx_egrad, but all
+ * device scratch is one static __device__ array of about 5 MB that every
+ * GPU loading the library keeps until the process exits; nothing is
+ * allocated on the device or the host heap. Limits: QCX_NOALLOC_MAX_ATOMS
+ * atoms and QCX_NOALLOC_MAX_NAO atomic orbitals; larger inputs return -1
+ * with the reason on stderr. The first call on a device looks up the array's
+ * device address and uploads the parameters; make that first call before
+ * any stream capture. Calls share the array: calls that overlap on the GPU
+ * race (one process serialises its own calls on the host).
+ */
+#define QCX_NOALLOC_MAX_ATOMS 64
+#define QCX_NOALLOC_MAX_NAO 160
+int qcx_egrad_noalloc(int method, int nat, const int32_t* num, const double* xyz, int charge, int multiplicity,
+                      double etemp, double* energy, double* grad, double* qat);
+
 #ifdef __cplusplus
 }
 #endif
