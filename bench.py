@@ -150,6 +150,32 @@ def cpu_sample(mols, seconds, nthreads):
     return done / el, steps, el
 
 
+def plain_fp64_single(qg, constants, nsteps=6):
+    """Plain FP64 single-trajectory path: one C6H12O2 radical cation (20 atoms,
+    charge +1, etemp 300 K), 500 K Maxwell-Boltzmann velocities, 0.5 fs steps."""
+    import torch
+    from qcxms_gb300 import molgen
+    Z, xyz = molgen.c6h12o2()
+    m = {"Z": Z, "xyz": xyz, "vel": molgen.maxwell_boltzmann(Z, 500.0, 1234), "mass": molgen.masses(Z), "charge": 1}
+    b = qg.Batch([m], etemp=ETEMP)
+    b.set_precision("fp64")
+    b.egrad()
+    dt = DT_FS * constants.FSTOAU
+    b.step(2, dt)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream())
+    _, s0 = b.progress()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    b.step(nsteps, dt)
+    e.record(stream)
+    e.synchronize()
+    _, s1 = b.progress()
+    done = float(np.sum(s1 - s0))
+    b.close()
+    return done / (s.elapsed_time(e) * 1e-3)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -270,6 +296,7 @@ def run_gpu(args):
     flops = scc_flops(nao[act > 0], iters[act > 0])
     achieved = flops / (scc_ms * 1e-3) / 1e12
     peak64 = measured_fp64_peak(torch)
+    plain = plain_fp64_single(qg, constants) if rank == 0 and not args.no_plain else None
 
     if rank == 0:
         cpu = None
@@ -304,6 +331,9 @@ def run_gpu(args):
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if plain:
+            line["config"]["plain_fp64_single_trajectory_steps_per_s"] = plain
+            line["config"]["speedup_vs_plain_fp64_single_trajectory"] = value / plain
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -318,6 +348,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ntraj", type=int, default=None, help="smaller batch for profiling runs (default 256)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the single-trajectory FP64 reference leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

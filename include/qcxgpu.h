@@ -64,13 +64,13 @@ qcx_batch* qcx_batch_create(int nmol, const int32_t* nat, const int32_t* num, co
                             const double* etemp);
 void qcx_batch_destroy(qcx_batch* b);
 
-/* SCC controls (defaults: 100, 1e-7 Eh, 1e-6, 0.4). max_iter <= 100. */
+/* SCC controls (defaults: 100, 1e-7 Eh, 1e-6, 0.25). max_iter <= 100. */
 int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, double mixing);
 
 /* Arithmetic of the SCC loop: 0 = FP64 throughout (default); 1 = mixed:
- * FP32 transforms, Jacobi eigensolve and density until the charge residual
- * reaches 3e-5, then FP64 iterations warm-started from the FP32 eigenvectors
- * to the same convergence thresholds. Integrals, potentials, Fermi level,
+ * FP32 transforms, eigensolve and density until the moment residual drops
+ * below 1e-4 (or stops improving below 1e-3), then FP64 iterations
+ * warm-started from the FP32 eigenvectors to the same convergence thresholds. Integrals, potentials, Fermi level,
  * Broyden mixing, energies and the gradient are FP64 in both modes. */
 #define QCX_PRECISION_FP64 0
 #define QCX_PRECISION_MIXED 1

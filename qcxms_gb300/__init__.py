@@ -147,7 +147,7 @@ class Batch:
         if rc != 0:
             raise RuntimeError("%s failed: %s" % (what, _err(self._lib)))
 
-    def set_scc(self, max_iter=100, econv=1e-7, pconv=1e-6, mixing=0.4):
+    def set_scc(self, max_iter=100, econv=1e-7, pconv=1e-6, mixing=0.25):
         self._check(self._lib.qcx_batch_set_scc(self._h, int(max_iter), float(econv), float(pconv), float(mixing)),
                     "set_scc")
 

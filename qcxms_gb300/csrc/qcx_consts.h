@@ -17,7 +17,7 @@
 #define QCX_SCC_MAXITER 100
 #define QCX_SCC_ECONV 1.0e-7
 #define QCX_SCC_PCONV 1.0e-6
-#define QCX_BROYDEN_ALPHA 0.4
+#define QCX_BROYDEN_ALPHA 0.25
 #define QCX_BROYDEN_W0 0.01
 /* Broyden history: the last QCX_BROYDEN_WINDOW iterations */
 #define QCX_BROYDEN_WINDOW 24

