@@ -2,6 +2,7 @@
 // capture of one MD step, and the C ABI declared in include/qcxgpu.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -96,7 +97,7 @@ struct qcx_batch {
   double *d_cn = nullptr, *d_cnd = nullptr, *d_dedcn = nullptr, *d_dedcnd = nullptr, *d_mrad = nullptr,
          *d_dmrad = nullptr, *d_w4 = nullptr, *d_dw4 = nullptr, *d_qat = nullptr;
   double *d_mats = nullptr, *d_vecs = nullptr, *d_energy = nullptr, *d_ekin = nullptr;
-  int *d_status = nullptr, *d_iters = nullptr, *d_active = nullptr;
+  int *d_status = nullptr, *d_iters = nullptr, *d_active = nullptr, *d_order = nullptr;
   long long* d_steps = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -126,7 +127,7 @@ void free_batch(qcx_batch* b) {
   void* ptrs[] = {b->d_prm, b->d_mol, b->d_Z, b->d_atom_mol, b->d_sh_atom, b->d_sh_k, b->d_sh_ao, b->d_pairs,
                   b->d_xyz, b->d_grad, b->d_vel, b->d_mass, b->d_cn, b->d_cnd, b->d_dedcn, b->d_dedcnd,
                   b->d_mrad, b->d_dmrad, b->d_w4, b->d_dw4, b->d_qat, b->d_mats, b->d_vecs, b->d_energy,
-                  b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps};
+                  b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps, b->d_order};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -199,8 +200,16 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
       dalloc(&b->d_w4, (size_t)na * kMaxRef) || dalloc(&b->d_dw4, (size_t)na * kMaxRef) || dalloc(&b->d_qat, na) ||
       dalloc(&b->d_mats, (size_t)mat_off) || dalloc(&b->d_vecs, (size_t)vec_off) ||
       dalloc(&b->d_energy, (size_t)nmol * kNumEnergy) || dalloc(&b->d_ekin, nmol) || dalloc(&b->d_status, nmol) ||
-      dalloc(&b->d_iters, nmol) || dalloc(&b->d_active, nmol) || dalloc(&b->d_steps, nmol))
+      dalloc(&b->d_iters, nmol) || dalloc(&b->d_active, nmol) || dalloc(&b->d_steps, nmol) ||
+      dalloc(&b->d_order, nmol))
     return -1;
+  {
+    // launch order of the per-molecule kernels: decreasing nao^3 (work of the SCC)
+    std::vector<int> order(nmol);
+    for (int m = 0; m < nmol; ++m) order[m] = m;
+    std::stable_sort(order.begin(), order.end(), [b](int x, int y) { return b->mol[x].nao > b->mol[y].nao; });
+    CK(cudaMemcpy(b->d_order, order.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
+  }
   b->bytes = sizeof(double) * ((size_t)mat_off + (size_t)vec_off);
   CK(cudaMemcpy(b->d_prm, &hp, sizeof(Params), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b->d_mol, b->mol.data(), sizeof(MolDesc) * nmol, cudaMemcpyHostToDevice));
@@ -259,6 +268,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   d.ekin = b->d_ekin;
   d.active = b->d_active;
   d.steps_done = b->d_steps;
+  d.order = b->d_order;
   d.max_nao = b->max_nao;
   d.smem_bytes = (int)scc_smem_bytes(b->max_nao, 0);
   d.max_iter = QCX_SCC_MAXITER;

@@ -75,7 +75,7 @@ __device__ inline double block_sum(double v, double* red) {
 
 __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
   extern __shared__ __align__(16) double sm[];
-  const int mol = blockIdx.x;
+  const int mol = bt.order ? bt.order[blockIdx.x] : blockIdx.x;
   const MolDesc md = bt.mol[mol];
   if (!bt.active[mol]) return;
   if (bt.status[mol] & kCholeskyFailed) {
@@ -206,18 +206,19 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
     dcnd[a] += dcda;
   }
   __syncthreads();
-  // (b) three-body dispersion, one thread per ordered triple a > b > c
+  // (b) three-body dispersion, one thread per ordered triple a > b > c. The term is
+  // small (~1e-3 Eh); it is evaluated in FP32 (relative error ~1e-7) and summed in FP64.
   double eatm = 0.0;
   long long ntrip = (long long)nat * nat * nat;
   for (long long t = threadIdx.x; t < ntrip; t += blockDim.x) {
     int a = (int)(t / ((long long)nat * nat)), b = (int)((t / nat) % nat), c = (int)(t % nat);
     if (!(a > b && b > c)) continue;
     int za = Z[a], zb = Z[b], zc = Z[c];
-    double rab[3], rbc[3], rca[3], x = 0, y = 0, z = 0;
+    float rab[3], rbc[3], rca[3], x = 0, y = 0, z = 0;
     for (int k = 0; k < 3; ++k) {
-      rab[k] = xyz[3 * a + k] - xyz[3 * b + k];
-      rbc[k] = xyz[3 * b + k] - xyz[3 * c + k];
-      rca[k] = xyz[3 * c + k] - xyz[3 * a + k];
+      rab[k] = (float)(xyz[3 * a + k] - xyz[3 * b + k]);
+      rbc[k] = (float)(xyz[3 * b + k] - xyz[3 * c + k]);
+      rca[k] = (float)(xyz[3 * c + k] - xyz[3 * a + k]);
       x += rab[k] * rab[k];
       y += rbc[k] * rbc[k];
       z += rca[k] * rca[k];
@@ -228,57 +229,58 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
                            bt.dw4 + (long long)(off + c) * kMaxRef};
     int zs[3] = {za, zb, zc};
     // C6 of the three pairs and their CN' derivatives: pair (i,j) for (0,1),(1,2),(2,0)
-    double c6p[3], dc6[3][2];
+    float c6p[3], dc6[3][2];
     const int pi[3] = {0, 1, 2}, pj[3] = {1, 2, 0};
     for (int pr = 0; pr < 3; ++pr) {
       int i0 = pi[pr], j0 = pj[pr];
-      double s = 0.0, di = 0.0, dj = 0.0;
+      float s = 0.0f, di = 0.0f, dj = 0.0f;
       for (int ii = 0; ii < P.d4_nref[zs[i0]]; ++ii)
         for (int jj = 0; jj < P.d4_nref[zs[j0]]; ++jj) {
-          double cr = c6ref(P, zs[i0], ii, zs[j0], jj);
-          s += w[i0][ii] * w[j0][jj] * cr;
-          di += dw[i0][ii] * w[j0][jj] * cr;
-          dj += w[i0][ii] * dw[j0][jj] * cr;
+          float cr = (float)c6ref(P, zs[i0], ii, zs[j0], jj);
+          float wi = (float)w[i0][ii], wj = (float)w[j0][jj];
+          s += wi * wj * cr;
+          di += (float)dw[i0][ii] * wj * cr;
+          dj += wi * (float)dw[j0][jj] * cr;
         }
       c6p[pr] = s;
       dc6[pr][0] = di;
       dc6[pr][1] = dj;
     }
-    double c9 = QCX_D4_S9 * sqrt(c6p[0] * c6p[1] * c6p[2]);
-    double r0 = cbrt(bj_radius(P, za, zb) * bj_radius(P, zb, zc) * bj_radius(P, zc, za));
-    double rrr = sqrt(x) * sqrt(y) * sqrt(z);
-    double rbar = cbrt(rrr);
-    double alp3 = QCX_ATM_ALP / 3.0;
-    double tt = 6.0 * pow(r0 / rbar, alp3);
-    double fd = 1.0 / (1.0 + tt);
-    double u1 = x + z - y, u2 = x + y - z, u3 = y + z - x;
-    double num = u1 * u2 * u3;
-    double den = 8.0 * x * y * z;
-    double ang = 3.0 * num / den + 1.0;
-    double r3 = rrr * rrr * rrr;
-    double h = fd / r3;
-    double en = c9 * ang * h;
-    eatm += en;
-    double dnx = u2 * u3 + u1 * u3 - u1 * u2;
-    double dny = -u2 * u3 + u1 * u3 + u1 * u2;
-    double dnz = u2 * u3 - u1 * u3 + u1 * u2;
-    double dlnh = fd * tt * alp3 - 9.0;
-    double ex = c9 * (3.0 * (dnx / den - num / (den * x)) * h + ang * h * dlnh / (6.0 * x));
-    double ey = c9 * (3.0 * (dny / den - num / (den * y)) * h + ang * h * dlnh / (6.0 * y));
-    double ez = c9 * (3.0 * (dnz / den - num / (den * z)) * h + ang * h * dlnh / (6.0 * z));
+    float c9 = (float)QCX_D4_S9 * sqrtf(c6p[0] * c6p[1] * c6p[2]);
+    float r0 = cbrtf((float)(bj_radius(P, za, zb) * bj_radius(P, zb, zc) * bj_radius(P, zc, za)));
+    float rrr = sqrtf(x) * sqrtf(y) * sqrtf(z);
+    float rbar = cbrtf(rrr);
+    const float alp3 = (float)(QCX_ATM_ALP / 3.0);
+    float tt = 6.0f * powf(r0 / rbar, alp3);
+    float fd = 1.0f / (1.0f + tt);
+    float u1 = x + z - y, u2 = x + y - z, u3 = y + z - x;
+    float num = u1 * u2 * u3;
+    float den = 8.0f * x * y * z;
+    float ang = 3.0f * num / den + 1.0f;
+    float r3 = rrr * rrr * rrr;
+    float h = fd / r3;
+    float en = c9 * ang * h;
+    eatm += (double)en;
+    float dnx = u2 * u3 + u1 * u3 - u1 * u2;
+    float dny = -u2 * u3 + u1 * u3 + u1 * u2;
+    float dnz = u2 * u3 - u1 * u3 + u1 * u2;
+    float dlnh = fd * tt * alp3 - 9.0f;
+    float ex = c9 * (3.0f * (dnx / den - num / (den * x)) * h + ang * h * dlnh / (6.0f * x));
+    float ey = c9 * (3.0f * (dny / den - num / (den * y)) * h + ang * h * dlnh / (6.0f * y));
+    float ez = c9 * (3.0f * (dnz / den - num / (den * z)) * h + ang * h * dlnh / (6.0f * z));
     for (int k = 0; k < 3; ++k) {
-      double gx = 2.0 * ex * rab[k], gy = 2.0 * ey * rbc[k], gz = 2.0 * ez * rca[k];
-      atomicAdd(&g[3 * a + k], gx - gz);
-      atomicAdd(&g[3 * b + k], -gx + gy);
-      atomicAdd(&g[3 * c + k], -gy + gz);
+      float gx = 2.0f * ex * rab[k], gy = 2.0f * ey * rbc[k], gz = 2.0f * ez * rca[k];
+      atomicAdd(&g[3 * a + k], (double)(gx - gz));
+      atomicAdd(&g[3 * b + k], (double)(-gx + gy));
+      atomicAdd(&g[3 * c + k], (double)(-gy + gz));
     }
     // d ln C9 / d CN'_p = 1/2 sum over the two pairs containing p of dC6/C6
-    double da = 0.5 * (dc6[0][0] / c6p[0] + dc6[2][1] / c6p[2]);
-    double db = 0.5 * (dc6[0][1] / c6p[0] + dc6[1][0] / c6p[1]);
-    double dc = 0.5 * (dc6[1][1] / c6p[1] + dc6[2][0] / c6p[2]);
-    atomicAdd(&dcnd[a], en * da);
-    atomicAdd(&dcnd[b], en * db);
-    atomicAdd(&dcnd[c], en * dc);
+    float da = 0.5f * (dc6[0][0] / c6p[0] + dc6[2][1] / c6p[2]);
+    float db = 0.5f * (dc6[0][1] / c6p[0] + dc6[1][0] / c6p[1]);
+    float dc = 0.5f * (dc6[1][1] / c6p[1] + dc6[2][0] / c6p[2]);
+    atomicAdd(&dcnd[a], (double)(en * da));
+    atomicAdd(&dcnd[b], (double)(en * db));
+    atomicAdd(&dcnd[c], (double)(en * dc));
   }
   __syncthreads();
   // dedcn from the shell-pair kernel

@@ -127,6 +127,7 @@ struct DevBatch {
   double* ekin;    // [nmol]
   int* active;     // [nmol] 1 while the trajectory runs; 0 after a failed evaluation
   long long* steps_done;  // [nmol] successful energy+gradient evaluations
+  const int* order;  // [nmol] molecules by decreasing size: CTA b of a per-molecule kernel takes order[b]
   int max_nao;
   int smem_bytes;  // dynamic shared memory granted to the SCC kernel
   // SCC controls

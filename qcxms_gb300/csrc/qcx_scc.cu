@@ -227,49 +227,48 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
   }
   __syncthreads();
   double e[5] = {0, 0, 0, 0, 0};
-  // atom-resolved terms: multipoles, XC kernels, dispersion
+  // atom-resolved terms. First the on-atom multipole XC kernels (which also
+  // initialise the potentials), then the pair terms spread over all threads
+  // (atom pairs b-major, so that consecutive threads add into different atoms).
   for (int a = threadIdx.x; a < nat; a += blockDim.x) {
-    double va = 0.0, vd[3] = {0, 0, 0}, vq[6] = {0, 0, 0, 0, 0, 0};
     const double* ma = dp + 3 * a;
     const double* ta = qp + 6 * a;
-    double eaes = 0.0, sdisp = 0.0;
-    for (int b = 0; b < nat; ++b) {
-      if (b == a) continue;
-      double r[3] = {mv.xyz[3 * a] - mv.xyz[3 * b], mv.xyz[3 * a + 1] - mv.xyz[3 * b + 1],
-                     mv.xyz[3 * a + 2] - mv.xyz[3 * b + 2]};
-      double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-      double f3 = f3m[a * nat + b], f5 = f5m[a * nat + b];
-      const double* mb = dp + 3 * b;
-      const double* tb = qp + 6 * b;
-      double mar = ma[0] * r[0] + ma[1] * r[1] + ma[2] * r[2];
-      double mbr = mb[0] * r[0] + mb[1] * r[1] + mb[2] * r[2];
-      double mab = ma[0] * mb[0] + ma[1] * mb[1] + ma[2] * mb[2];
-      double rr[6] = {r[0] * r[0], r[1] * r[1], r[2] * r[2], 2 * r[0] * r[1], 2 * r[0] * r[2], 2 * r[1] * r[2]};
-      double rta = 0, rtb = 0;
-      for (int q = 0; q < 6; ++q) {
-        rta += ta[q] * rr[q];
-        rtb += tb[q] * rr[q];
-      }
-      eaes += f3 * (qat[a] * mbr - qat[b] * mar) + f5 * (qat[a] * rtb + qat[b] * rta + mab * r2 - 3.0 * mar * mbr);
-      va += f3 * mbr + f5 * rtb;
-      for (int k = 0; k < 3; ++k) vd[k] += -f3 * qat[b] * r[k] + f5 * (mb[k] * r2 - 3.0 * mbr * r[k]);
-      for (int q = 0; q < 6; ++q) vq[q] += f5 * qat[b] * rr[q];
-      sdisp += zeta[b] * c6g[a * nat + b];
-    }
     int z = mv.Z[a];
     double fd = P.aes_dk[z], fq = P.aes_qk[z];
-    double eaxc = fd * (ma[0] * ma[0] + ma[1] * ma[1] + ma[2] * ma[2]) +
-                  fq * (ta[0] * ta[0] + ta[1] * ta[1] + ta[2] * ta[2] + 2.0 * (ta[3] * ta[3] + ta[4] * ta[4] + ta[5] * ta[5]));
-    for (int k = 0; k < 3; ++k) vd[k] += 2.0 * fd * ma[k];
-    for (int q = 0; q < 3; ++q) vq[q] += 2.0 * fq * ta[q];
-    for (int q = 3; q < 6; ++q) vq[q] += 4.0 * fq * ta[q];
-    va += -dzeta[a] * sdisp;
-    vat[a] = va;
-    for (int k = 0; k < 3; ++k) vdp[3 * a + k] = vd[k];
-    for (int q = 0; q < 6; ++q) vqp[6 * a + q] = vq[q];
-    e[2] += 0.5 * eaes;
-    e[3] += eaxc;
-    e[4] += -0.5 * zeta[a] * sdisp;
+    e[3] += fd * (ma[0] * ma[0] + ma[1] * ma[1] + ma[2] * ma[2]) +
+            fq * (ta[0] * ta[0] + ta[1] * ta[1] + ta[2] * ta[2] + 2.0 * (ta[3] * ta[3] + ta[4] * ta[4] + ta[5] * ta[5]));
+    vat[a] = 0.0;
+    for (int k = 0; k < 3; ++k) vdp[3 * a + k] = 2.0 * fd * ma[k];
+    for (int q = 0; q < 3; ++q) vqp[6 * a + q] = 2.0 * fq * ta[q];
+    for (int q = 3; q < 6; ++q) vqp[6 * a + q] = 4.0 * fq * ta[q];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < nat * nat; idx += blockDim.x) {
+    int b = idx / nat, a = idx - b * nat;
+    if (b == a) continue;
+    const double* ma = dp + 3 * a;
+    const double* ta = qp + 6 * a;
+    double r[3] = {mv.xyz[3 * a] - mv.xyz[3 * b], mv.xyz[3 * a + 1] - mv.xyz[3 * b + 1],
+                   mv.xyz[3 * a + 2] - mv.xyz[3 * b + 2]};
+    double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    double f3 = f3m[a * nat + b], f5 = f5m[a * nat + b];
+    const double* mb = dp + 3 * b;
+    const double* tb = qp + 6 * b;
+    double mar = ma[0] * r[0] + ma[1] * r[1] + ma[2] * r[2];
+    double mbr = mb[0] * r[0] + mb[1] * r[1] + mb[2] * r[2];
+    double mab = ma[0] * mb[0] + ma[1] * mb[1] + ma[2] * mb[2];
+    double rr[6] = {r[0] * r[0], r[1] * r[1], r[2] * r[2], 2 * r[0] * r[1], 2 * r[0] * r[2], 2 * r[1] * r[2]};
+    double rta = 0, rtb = 0;
+    for (int q = 0; q < 6; ++q) {
+      rta += ta[q] * rr[q];
+      rtb += tb[q] * rr[q];
+    }
+    double cg = c6g[a * nat + b];
+    e[2] += 0.5 * (f3 * (qat[a] * mbr - qat[b] * mar) + f5 * (qat[a] * rtb + qat[b] * rta + mab * r2 - 3.0 * mar * mbr));
+    e[4] += -0.5 * zeta[a] * zeta[b] * cg;
+    atomicAdd(&vat[a], f3 * mbr + f5 * rtb - dzeta[a] * zeta[b] * cg);
+    for (int k = 0; k < 3; ++k) atomicAdd(&vdp[3 * a + k], -f3 * qat[b] * r[k] + f5 * (mb[k] * r2 - 3.0 * mbr * r[k]));
+    for (int q = 0; q < 6; ++q) atomicAdd(&vqp[6 * a + q], f5 * qat[b] * rr[q]);
   }
   __syncthreads();
   // shell-resolved isotropic electrostatics and third order
@@ -347,29 +346,37 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
         ((T*)sh.rs)[k] = s;
       }
       __syncthreads();
-      // rows of A and of Vt
-      for (int i = threadIdx.x; i < half * np; i += blockDim.x) {
-        int k = i / np, j = i - k * np;
-        if (sh.rskip[k]) continue;
-        T c = ((T*)sh.rc)[k], s = ((T*)sh.rs)[k];
-        int p = sh.rp[k], q = sh.rq[k];
-        T ap = A[p * np + j], aq = A[q * np + j];
-        A[p * np + j] = c * ap - s * aq;
-        A[q * np + j] = s * ap + c * aq;
-        T vp = Vt[p * np + j], vq = Vt[q * np + j];
-        Vt[p * np + j] = c * vp - s * vq;
-        Vt[q * np + j] = s * vp + c * vq;
-      }
-      __syncthreads();
-      // columns of A
-      for (int i = threadIdx.x; i < half * np; i += blockDim.x) {
-        int j = i / half, k = i - j * half;
-        if (sh.rskip[k]) continue;
-        T c = ((T*)sh.rc)[k], s = ((T*)sh.rs)[k];
-        int p = sh.rp[k], q = sh.rq[k];
-        T ap = A[j * np + p], aq = A[j * np + q];
-        A[j * np + p] = c * ap - s * aq;
-        A[j * np + q] = s * ap + c * aq;
+      // One fused phase per round: every 2x2 block A[{p1,q1}][{p2,q2}] of a pair
+      // of pairs becomes R1 * block * R2^T (each element belongs to exactly one
+      // block), and the rows p,q of Vt are rotated by R.
+      const int nblk = half * half;
+      for (int i = threadIdx.x; i < nblk + half * np; i += blockDim.x) {
+        if (i < nblk) {
+          int k1 = i / half, k2 = i - k1 * half;
+          int sk1 = sh.rskip[k1], sk2 = sh.rskip[k2];
+          if (sk1 && sk2) continue;
+          T c1 = ((T*)sh.rc)[k1], s1 = ((T*)sh.rs)[k1];
+          T c2 = ((T*)sh.rc)[k2], s2 = ((T*)sh.rs)[k2];
+          int p1 = sh.rp[k1], q1 = sh.rq[k1], p2 = sh.rp[k2], q2 = sh.rq[k2];
+          T a = A[p1 * np + p2], b = A[p1 * np + q2], c = A[q1 * np + p2], d = A[q1 * np + q2];
+          // rows: R1 = [[c1,-s1],[s1,c1]]
+          T ra = c1 * a - s1 * c, rb = c1 * b - s1 * d;
+          T rc = s1 * a + c1 * c, rd = s1 * b + c1 * d;
+          // columns: multiply by R2^T
+          A[p1 * np + p2] = c2 * ra - s2 * rb;
+          A[p1 * np + q2] = s2 * ra + c2 * rb;
+          A[q1 * np + p2] = c2 * rc - s2 * rd;
+          A[q1 * np + q2] = s2 * rc + c2 * rd;
+        } else {
+          int e = i - nblk;
+          int k = e / np, j = e - k * np;
+          if (sh.rskip[k]) continue;
+          T c = ((T*)sh.rc)[k], s = ((T*)sh.rs)[k];
+          int p = sh.rp[k], q = sh.rq[k];
+          T vp = Vt[p * np + j], vq = Vt[q * np + j];
+          Vt[p * np + j] = c * vp - s * vq;
+          Vt[q * np + j] = s * vp + c * vq;
+        }
       }
       __syncthreads();
     }
@@ -383,7 +390,7 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
 // Fermi level by safeguarded Newton/bisection (one warp); returns -T S.
 // ---------------------------------------------------------------------------
 __device__ double fermi_warp(int n, const double* eps, double nel, double kT, double* focc, double* efermi,
-                             double rtol = 1e-13) {
+                             double rtol = 1e-13, double mu_guess = 0.0, bool have_guess = false) {
   int lane = threadIdx.x & 31;
   if (nel <= 0.0) {
     for (int i = lane; i < n; i += 32) focc[i] = 0.0;
@@ -400,6 +407,7 @@ __device__ double fermi_warp(int n, const double* eps, double nel, double kT, do
   int lu = ho + 1 < n ? ho + 1 : n - 1;
   double lo = eps[0] - 1.0, hi = eps[n - 1] + 1.0;
   double mu = 0.5 * (eps[ho] + eps[lu]);
+  if (have_guess && mu_guess > lo && mu_guess < hi) mu = mu_guess;  // Fermi level of the previous iteration
   for (int it = 0; it < QCX_FERMI_ITERS; ++it) {
     double N = 0.0, dN = 0.0;
     for (int i = lane; i < n; i += 32) {
@@ -428,6 +436,64 @@ __device__ double fermi_warp(int n, const double* eps, double nel, double kT, do
   ts = warp_sum(ts);
   *efermi = mu;
   return ts;
+}
+
+// FP32 Fermi level for the FP32 SCC iterations (one warp). Orbital energies
+// are shifted by the starting guess once in FP64; the Newton/bisection runs in
+// FP32 on the shifted values held in registers (n <= 512), to an electron-count
+// accuracy of 1e-6 * nel. Returns -T S.
+__device__ double fermi_warp32(int n, const double* eps, double nel, double kT, double* focc, double* efermi,
+                               double mu_guess, bool have_guess) {
+  int lane = threadIdx.x & 31;
+  if (nel <= 0.0 || nel >= 2.0 * n || n > 512)
+    return fermi_warp(n, eps, nel, kT, focc, efermi, 1e-13, mu_guess, have_guess);
+  int ho = (int)ceil(nel / 2.0) - 1;
+  if (ho < 0) ho = 0;
+  int lu = ho + 1 < n ? ho + 1 : n - 1;
+  double mu0 = 0.5 * (eps[ho] + eps[lu]);
+  if (have_guess && mu_guess > eps[0] - 1.0 && mu_guess < eps[n - 1] + 1.0) mu0 = mu_guess;
+  float d[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    int i = lane + 32 * k;
+    d[k] = i < n ? (float)(eps[i] - mu0) : 1e30f;
+  }
+  const float ikT = (float)(1.0 / kT);
+  const float fnel = (float)nel;
+  float lo = (float)(eps[0] - mu0) - 1.0f, hi = (float)(eps[n - 1] - mu0) + 1.0f, mu = 0.0f;
+  for (int it = 0; it < QCX_FERMI_ITERS; ++it) {
+    float N = 0.0f, dN = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      float f = 1.0f / (1.0f + expf((d[k] - mu) * ikT));
+      N += 2.0f * f;
+      dN += 2.0f * f * (1.0f - f) * ikT;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      N += __shfl_xor_sync(0xffffffffu, N, o);
+      dN += __shfl_xor_sync(0xffffffffu, dN, o);
+    }
+    float r = N - fnel;
+    if (fabsf(r) < 1e-6f * (fnel > 1.0f ? fnel : 1.0f)) break;
+    if (r < 0.0f) lo = mu;
+    else hi = mu;
+    float mn = (dN > 1e-30f) ? mu - r / dN : 0.5f * (lo + hi);
+    if (!(mn > lo && mn < hi)) mn = 0.5f * (lo + hi);
+    mu = mn;
+  }
+  float ts = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    int i = lane + 32 * k;
+    if (i >= n) continue;
+    float x = (d[k] - mu) * ikT, ax = fabsf(x);
+    float fs = 1.0f / (1.0f + expf(ax));
+    ts += -(fs * ax + log1pf(expf(-ax)));
+    focc[i] = (double)(2.0f / (1.0f + expf(x)));
+  }
+  for (int o = 16; o > 0; o >>= 1) ts += __shfl_xor_sync(0xffffffffu, ts, o);
+  *efermi = mu0 + (double)mu;
+  return 2.0 * kT * (double)ts;
 }
 
 // ---------------------------------------------------------------------------
@@ -578,12 +644,12 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 // diagonal holds the eigenvalues.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ bool refine(T* JA, T* JV, const double* F, const double* S, T* Tm, T* Cm, double* tmp, int n,
+__device__ bool refine(T* JA, T* JV, const T* F, const double* S, T* Tm, T* Cm, double* tmp, int n,
                        double kfail, double ktol, int max_pass, SccShared& sh) {
   const int np = n + (n & 1);
   for (int pass = 0; pass < max_pass; ++pass) {
     if (pass > 0) {
-      cta_gemm<double, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
+      cta_gemm<T, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
       __syncthreads();
       cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, JA, np);
       __syncthreads();
@@ -649,7 +715,7 @@ __device__ bool refine(T* JA, T* JV, const double* F, const double* S, T* Tm, T*
     if (kmax < ktol) return true;
   }
   // passes exhausted: recompute B in the final basis for the caller's Jacobi
-  cta_gemm<double, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
+  cta_gemm<T, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
   __syncthreads();
   cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, JA, np);
   __syncthreads();
@@ -680,6 +746,7 @@ constexpr double kMixedSwitch = 1e-4;
 // Optional per-phase cycle counters (diagnostic builds only: -DQCX_SCC_PHASE_TIMING).
 #ifdef QCX_SCC_PHASE_TIMING
 __device__ unsigned long long g_phase_cycles[16];
+__device__ unsigned long long g_mol_cycles[4096];
 #define PHASE_BEGIN() long long _pt = clock64()
 #define PHASE_MARK(i)                                                 \
   do {                                                                \
@@ -697,7 +764,8 @@ __device__ unsigned long long g_phase_cycles[16];
 template <int MIXED>
 __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch bt) {
   extern __shared__ __align__(16) char smem_raw[];
-  const int mol = blockIdx.x;
+  // largest molecules first, so that the longest CTAs start in the first wave
+  const int mol = bt.order ? bt.order[blockIdx.x] : blockIdx.x;
   if (!bt.active[mol]) return;
   MolView mv;
   mv.bt = &bt;
@@ -852,6 +920,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   int stall32 = 0;
   int n64 = 0;          // FP64 iterations done
   PHASE_BEGIN();
+#ifdef QCX_SCC_PHASE_TIMING
+  long long _t_start = clock64();
+#endif
   for (it = 1; it <= bt.max_iter; ++it) {
     PHASE_MARK(15);
     potentials(mv, xin, en, sh.red);
@@ -861,16 +932,34 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       const double* vsh = vec + mv.vl.vsh;
       const double* vdp = vec + mv.vl.vdp;
       const double* vqp = vec + mv.vl.vqp;
-      for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-        int i = (int)(e / n), j = (int)(e % n);
-        int A = sh.ao_at[i], B = sh.ao_at[j];
-        long long ji = (long long)j * n + i;
-        double f = H0[e] - 0.5 * S[e] * (vsh[sh.ao_sh[i]] + vsh[sh.ao_sh[j]]);
+      if (fp32_phase) {
+        // FP32 iterations: the Fock matrix only feeds FP32 products
+        float* F32 = (float*)F;
+        for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+          int i = (int)(e / n), j = (int)(e % n);
+          int A = sh.ao_at[i], B = sh.ao_at[j];
+          long long ji = (long long)j * n + i;
+          float f = (float)H0[e] - 0.5f * (float)S[e] * (float)(vsh[sh.ao_sh[i]] + vsh[sh.ao_sh[j]]);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f -= 0.5 * (vdp[3 * A + c] * Dm[c * nn + e] + vdp[3 * B + c] * Dm[c * nn + ji]);
+          for (int c = 0; c < 3; ++c)
+            f -= 0.5f * ((float)vdp[3 * A + c] * (float)Dm[c * nn + e] + (float)vdp[3 * B + c] * (float)Dm[c * nn + ji]);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) f -= 0.5 * (vqp[6 * A + c] * Qm[c * nn + e] + vqp[6 * B + c] * Qm[c * nn + ji]);
-        F[e] = f;
+          for (int c = 0; c < 6; ++c)
+            f -= 0.5f * ((float)vqp[6 * A + c] * (float)Qm[c * nn + e] + (float)vqp[6 * B + c] * (float)Qm[c * nn + ji]);
+          F32[e] = f;
+        }
+      } else {
+        for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+          int i = (int)(e / n), j = (int)(e % n);
+          int A = sh.ao_at[i], B = sh.ao_at[j];
+          long long ji = (long long)j * n + i;
+          double f = H0[e] - 0.5 * S[e] * (vsh[sh.ao_sh[i]] + vsh[sh.ao_sh[j]]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) f -= 0.5 * (vdp[3 * A + c] * Dm[c * nn + e] + vdp[3 * B + c] * Dm[c * nn + ji]);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) f -= 0.5 * (vqp[6 * A + c] * Qm[c * nn + e] + vqp[6 * B + c] * Qm[c * nn + ji]);
+          F[e] = f;
+        }
       }
     }
     __syncthreads();
@@ -883,12 +972,12 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     if (fp32_phase) {
       // ---- FP32 iteration ----
       if (!have32) {
-        cta_gemm<double, float, float, float>(n, n, n, F, n, false, X32, n, false, T32, n);
+        cta_gemm<float, float, float, float>(n, n, n, (const float*)F, n, false, X32, n, false, T32, n);
         __syncthreads();
         cta_gemm<float, float, float, float>(n, n, n, X32, n, true, T32, n, false, JA32, np);
         __syncthreads();
       } else {
-        cta_gemm<double, float, float, float>(n, n, n, F, n, false, JV32, np, true, T32, n);
+        cta_gemm<float, float, float, float>(n, n, n, (const float*)F, n, false, JV32, np, true, T32, n);
         __syncthreads();
         cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, T32, n, false, JA32, np);
         __syncthreads();
@@ -904,7 +993,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       __syncthreads();
       PHASE_MARK(2);
       bool ok32 = have32 && QCX_REFINE32_PASSES > 0 &&
-                  refine<float>(JA32, JV32, F, S, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, 1e-3,
+                  refine<float>(JA32, JV32, (const float*)F, S, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, 1e-3,
                                 QCX_REFINE32_PASSES, sh);
       if (!ok32) jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? 8 : 30);
       PHASE_MARK(3);
@@ -1001,7 +1090,8 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     PHASE_MARK(6);
     if (threadIdx.x < 32) {
       double ef;
-      double ts = fermi_warp(n, eps, nel, md.kT, focc, &ef, fp32_phase ? 1e-9 : 1e-13);
+      double ts = fp32_phase ? fermi_warp32(n, eps, nel, md.kT, focc, &ef, efermi, it > 1)
+                             : fermi_warp(n, eps, nel, md.kT, focc, &ef, 1e-13, efermi, it > 1);
       if (threadIdx.x == 0) {
         sh.scal[0] = ts;
         sh.scal[1] = ef;
@@ -1040,20 +1130,38 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     {
       int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
       for (int i = w; i < n; i += kWarps) {
-        double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int j = lane; j < n; j += 32) {
-          long long e = (long long)i * n + j;
-          double p = Pm[e];
-          acc[0] += p * S[e];
+        if (fp32_phase) {
+          float acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+          for (int j = lane; j < n; j += 32) {
+            long long e = (long long)i * n + j;
+            float p = (float)Pm[e];
+            acc[0] += p * (float)S[e];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) acc[1 + c] += p * Dm[c * nn + e];
+            for (int c = 0; c < 3; ++c) acc[1 + c] += p * (float)Dm[c * nn + e];
 #pragma unroll
-          for (int c = 0; c < 6; ++c) acc[4 + c] += p * Qm[c * nn + e];
+            for (int c = 0; c < 6; ++c) acc[4 + c] += p * (float)Qm[c * nn + e];
+          }
+#pragma unroll
+          for (int c = 0; c < 10; ++c)
+            for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+          if (lane == 0)
+            for (int c = 0; c < 10; ++c) sh.mom[c * n + i] = (double)acc[c];
+        } else {
+          double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+          for (int j = lane; j < n; j += 32) {
+            long long e = (long long)i * n + j;
+            double p = Pm[e];
+            acc[0] += p * S[e];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc[1 + c] += p * Dm[c * nn + e];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[4 + c] += p * Qm[c * nn + e];
+          }
+#pragma unroll
+          for (int c = 0; c < 10; ++c) acc[c] = warp_sum(acc[c]);
+          if (lane == 0)
+            for (int c = 0; c < 10; ++c) sh.mom[c * n + i] = acc[c];
         }
-#pragma unroll
-        for (int c = 0; c < 10; ++c) acc[c] = warp_sum(acc[c]);
-        if (lane == 0)
-          for (int c = 0; c < 10; ++c) sh.mom[c * n + i] = acc[c];
       }
       __syncthreads();
       for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
@@ -1120,6 +1228,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     PHASE_MARK(12);
   }
   if (it > bt.max_iter) it = bt.max_iter;
+#ifdef QCX_SCC_PHASE_TIMING
+  if (threadIdx.x == 0 && mol < 4096) g_mol_cycles[mol] = (unsigned long long)(clock64() - _t_start);
+#endif
   // energy-weighted density W = C f e C^T (FP64 coefficients of the last iteration)
   int nocc = 0;
   for (int k = 0; k < n; ++k)
@@ -1160,6 +1271,10 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
 
 #ifdef QCX_SCC_PHASE_TIMING
 }  // namespace qcx
+extern "C" int qcx_debug_mol_cycles(unsigned long long* out, int n) {
+  return cudaMemcpyFromSymbol(out, qcx::g_mol_cycles, sizeof(unsigned long long) * (n < 4096 ? n : 4096)) ==
+                 cudaSuccess ? 0 : -1;
+}
 extern "C" int qcx_debug_phase_cycles(unsigned long long* out, int reset) {
   if (cudaMemcpyFromSymbol(out, qcx::g_phase_cycles, sizeof(unsigned long long) * 16) != cudaSuccess) return -1;
   if (reset) {
