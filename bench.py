@@ -30,6 +30,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "GFN2-xTB trajectory-steps/s"
+# DRAM bytes of one k_scc launch per molecule, from an ncu capture of 16 molecules
+# (6.65 MB; profiles/k_scc_mixed_16traj_full.md); a launch touches each molecule's own data only.
+SCC_DRAM_BYTES_PER_MOLECULE = 6.65e6 / 16
 NTRAJ, NMIN, NMAX = 256, 5, 40
 DT_FS = 0.5
 ETEMP = 300.0
@@ -322,7 +325,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                         "frac": achieved / peak64, "traffic": None, "kernel": "k_scc",
+                         "frac": achieved / peak64, "traffic": SCC_DRAM_BYTES_PER_MOLECULE * b.nmol, "kernel": "k_scc",
                          "peak_source": "measured in this run: cuBLAS FP64 GEMM 4096^3 (MEASURED_PEAKS.json holds "
                                         "only HBM and bf16 peaks)",
                          "flops_convention": "per molecule: iters*(9n^3+2n^3)+2n^3"},
