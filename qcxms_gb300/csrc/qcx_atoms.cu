@@ -122,29 +122,38 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
     dcnd[a] = 0.0;
   }
   __syncthreads();
-  // (a) pair terms, one thread per atom, all partners (each pair visited twice)
+  // (a) pair terms over all ordered atom pairs (b-major, so that consecutive
+  // threads add into different atoms); each pair is visited from both ends
+  int* at_sh0 = (int*)(red + 32);  // [nat] first shell of each atom
+  int* at_nsh = at_sh0 + nat;      // [nat] shell count
+  for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
+    int at = sh_atom[s] - off;
+    if (s == 0 || sh_atom[s - 1] - off != at) at_sh0[at] = s;
+    if (s == nsh - 1 || sh_atom[s + 1] - off != at) at_nsh[at] = s + 1;  // one past the last, fixed below
+  }
+  __syncthreads();
+  for (int x = threadIdx.x; x < nat; x += blockDim.x) at_nsh[x] -= at_sh0[x];
+  __syncthreads();
   double erep = 0.0;
-  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+  for (int idx = threadIdx.x; idx < nat * nat; idx += blockDim.x) {
+    int b = idx / nat, a = idx - b * nat;
+    if (b == a) continue;
     double ga[3] = {0, 0, 0}, dca = 0.0, dcda = 0.0;
     int za = Z[a];
     const double* ma = dp + 3 * a;
     const double* ta = qp + 6 * a;
-    for (int b = 0; b < nat; ++b) {
-      if (b == a) continue;
+    {
       int zb = Z[b];
       double r[3] = {xyz[3 * a] - xyz[3 * b], xyz[3 * a + 1] - xyz[3 * b + 1], xyz[3 * a + 2] - xyz[3 * b + 2]};
       double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
       double R = sqrt(r2);
       double dEdR = 0.0;
       // isotropic electrostatics
-      for (int s = 0; s < nsh; ++s) {
-        if (sh_atom[s] - off != a) continue;
-        for (int t = 0; t < nsh; ++t) {
-          if (sh_atom[t] - off != b) continue;
+      for (int s = at_sh0[a]; s < at_sh0[a] + at_nsh[a]; ++s)
+        for (int t = at_sh0[b]; t < at_sh0[b] + at_nsh[b]; ++t) {
           double gm = gam[s * nsh + t];
           dEdR += qsh[s] * qsh[t] * (-R * gm * gm * gm);
         }
-      }
       // dispersion (two-body): E = -zeta_a zeta_b C6_ab g_ab
       double gd, dgd;
       bj_kernel(P, za, zb, R, gd, dgd);
@@ -199,11 +208,11 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
       }
       dca += (d3r0 * s1 + d5r0 * s2) * 0.5 * bt.dmrad[off + a];
     }
-    g[3 * a] += ga[0];
-    g[3 * a + 1] += ga[1];
-    g[3 * a + 2] += ga[2];
-    dcn[a] += dca;
-    dcnd[a] += dcda;
+    atomicAdd(&g[3 * a], ga[0]);
+    atomicAdd(&g[3 * a + 1], ga[1]);
+    atomicAdd(&g[3 * a + 2], ga[2]);
+    atomicAdd(&dcn[a], dca);
+    atomicAdd(&dcnd[a], dcda);
   }
   __syncthreads();
   // (b) three-body dispersion, one thread per ordered triple a > b > c. The term is
@@ -286,21 +295,21 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
   // dedcn from the shell-pair kernel
   for (int a = threadIdx.x; a < nat; a += blockDim.x) dcn[a] += bt.dedcn[off + a];
   __syncthreads();
-  // (c) coordination-number chain rule
-  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
-    double ga[3] = {0, 0, 0};
-    for (int b = 0; b < nat; ++b) {
-      if (b == a) continue;
-      double r[3] = {xyz[3 * a] - xyz[3 * b], xyz[3 * a + 1] - xyz[3 * b + 1], xyz[3 * a + 2] - xyz[3 * b + 2]};
-      double R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-      double rc = P.rcov[Z[a]] + P.rcov[Z[b]], f, df1, df2;
-      cn_exp_pair(R, rc, f, df1);
-      cn_erf_pair(R, rc, f, df2);
-      double s = (dcn[a] + dcn[b]) * df1 + (dcnd[a] + dcnd[b]) * df2;
-      for (int k = 0; k < 3; ++k) ga[k] += s * r[k] / R;
-    }
-    for (int k = 0; k < 3; ++k) bt.grad[3LL * (off + a) + k] += g[3 * a + k] + ga[k];
+  // (c) coordination-number chain rule, over ordered pairs into the smem gradient
+  for (int idx = threadIdx.x; idx < nat * nat; idx += blockDim.x) {
+    int b = idx / nat, a = idx - b * nat;
+    if (b == a) continue;
+    double r[3] = {xyz[3 * a] - xyz[3 * b], xyz[3 * a + 1] - xyz[3 * b + 1], xyz[3 * a + 2] - xyz[3 * b + 2]};
+    double R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    double rc = P.rcov[Z[a]] + P.rcov[Z[b]], f, df1, df2;
+    cn_exp_pair(R, rc, f, df1);
+    cn_erf_pair(R, rc, f, df2);
+    double s = (dcn[a] + dcn[b]) * df1 + (dcnd[a] + dcnd[b]) * df2;
+    for (int k = 0; k < 3; ++k) atomicAdd(&g[3 * a + k], s * r[k] / R);
   }
+  __syncthreads();
+  for (int a = threadIdx.x; a < nat; a += blockDim.x)
+    for (int k = 0; k < 3; ++k) bt.grad[3LL * (off + a) + k] += g[3 * a + k];
   erep = block_sum(erep, red);
   eatm = block_sum(eatm, red);
   if (threadIdx.x == 0) {
@@ -317,8 +326,8 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
 }
 
 void launch_grad_atoms(const DevBatch& bt, cudaStream_t st) {
-  // largest molecule bounds the shared memory: 5 nat + 32 doubles
-  size_t smem = sizeof(double) * (5 * (size_t)bt.max_nao + 64);
+  // largest molecule bounds the shared memory: 5 nat + 32 doubles + 2 nat ints
+  size_t smem = sizeof(double) * (6 * (size_t)bt.max_nao + 64);
   k_grad_atoms<<<bt.nmol, kAtomThreads, smem, st>>>(bt);
 }
 
