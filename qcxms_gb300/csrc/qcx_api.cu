@@ -105,20 +105,24 @@ struct qcx_batch {
   long long launches = 0;
   size_t bytes = 0;
   int precision = 0;
+  int step_launches = 0;
 };
 
 namespace {
 
-void enqueue_egrad(qcx_batch* b) {
+// returns the number of kernels launched
+int enqueue_egrad(qcx_batch* b) {
   const DevBatch& d = b->dev;
+  int n = 0;
   launch_cn(d, b->stream);
-  launch_integrals(d, b->stream);
+  n += 1 + launch_integrals(d, b->stream);
   launch_scc(d, b->precision, b->stream);
   launch_zero_grad(d, b->stream);
-  launch_grad_pairs(d, b->stream);
+  n += 2 + launch_grad_pairs(d, b->stream);
   launch_grad_atoms(d, b->stream);
+  return n + 1;
 }
-constexpr int kEgradLaunches = 6;
+constexpr int kEgradPhases = 6;
 
 void free_batch(qcx_batch* b) {
   if (!b) return;
@@ -179,14 +183,26 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
     mat_off += (long long)kNumMat * slot_size(nao);
     md.vec_off = vec_off;
     vec_off += VecLayout::make(md.nat, md.nsh, nao, md.len, md.nmem).total;
-    for (int s = 0; s < md.nsh; ++s)
-      for (int t = 0; t < md.nsh; ++t) pairs.push_back({md.sh_off + s, md.sh_off + t});
     b->mol.push_back(md);
     b->max_nao = nao > b->max_nao ? nao : b->max_nao;
     aoff += nat[m];
   }
   b->natom = aoff;
   b->nshell = (int)sh_atom.size();
+  // ordered shell pairs of every molecule, grouped by angular-momentum class
+  int pair_off[10] = {0};
+  {
+    std::vector<int> sh_l(sh_atom.size());
+    for (size_t s = 0; s < sh_atom.size(); ++s) sh_l[s] = qcx_sh_l[b->Z[sh_atom[s]]][sh_k[s]];
+    for (int c = 0; c < 9; ++c) {
+      pair_off[c] = (int)pairs.size();
+      for (const MolDesc& md : b->mol)
+        for (int s = md.sh_off; s < md.sh_off + md.nsh; ++s)
+          for (int t = md.sh_off; t < md.sh_off + md.nsh; ++t)
+            if (sh_l[s] * 3 + sh_l[t] == c) pairs.push_back({s, t});
+    }
+    pair_off[9] = (int)pairs.size();
+  }
   b->npair = (int)pairs.size();
   CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   Params hp;
@@ -239,6 +255,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   d.natom = na;
   d.nshell = b->nshell;
   d.npair = b->npair;
+  for (int c = 0; c < 10; ++c) d.pair_off[c] = pair_off[c];
   d.prm = b->d_prm;
   d.mol = b->d_mol;
   d.Z = b->d_Z;
@@ -361,8 +378,7 @@ int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, cons
 
 int qcx_batch_egrad(qcx_batch* b) {
   if (!b) return -1;
-  enqueue_egrad(b);
-  b->launches = kEgradLaunches;
+  b->launches = enqueue_egrad(b);
   return check_launch();
 }
 
@@ -377,13 +393,13 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
     }
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     launch_leapfrog(b->dev, tstep, b->stream);
-    enqueue_egrad(b);
+    b->step_launches = 1 + enqueue_egrad(b);
     CK(cudaStreamEndCapture(b->stream, &b->graph));
     CK(cudaGraphInstantiate(&b->graph_exec, b->graph, 0));
     b->graph_tstep = tstep;
   }
   for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(b->graph_exec, b->stream));
-  b->launches = (long long)nsteps * (kEgradLaunches + 1);
+  b->launches = (long long)nsteps * b->step_launches;
   return check_launch();
 }
 
@@ -446,26 +462,26 @@ void* qcx_batch_stream(qcx_batch* b) { return b ? (void*)b->stream : nullptr; }
 
 int qcx_batch_profile_egrad(qcx_batch* b, float* ms) {
   if (!b || !ms) return -1;
-  cudaEvent_t ev[kEgradLaunches + 1];
+  cudaEvent_t ev[kEgradPhases + 1];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   const DevBatch& d = b->dev;
   CK(cudaEventRecord(ev[0], b->stream));
   launch_cn(d, b->stream);
   CK(cudaEventRecord(ev[1], b->stream));
-  launch_integrals(d, b->stream);
+  int nl = 3 + launch_integrals(d, b->stream);
   CK(cudaEventRecord(ev[2], b->stream));
   launch_scc(d, b->precision, b->stream);
   CK(cudaEventRecord(ev[3], b->stream));
   launch_zero_grad(d, b->stream);
   CK(cudaEventRecord(ev[4], b->stream));
-  launch_grad_pairs(d, b->stream);
+  nl += launch_grad_pairs(d, b->stream);
   CK(cudaEventRecord(ev[5], b->stream));
   launch_grad_atoms(d, b->stream);
   CK(cudaEventRecord(ev[6], b->stream));
   CK(cudaEventSynchronize(ev[6]));
-  for (int i = 0; i < kEgradLaunches; ++i) CK(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+  for (int i = 0; i < kEgradPhases; ++i) CK(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
-  b->launches = kEgradLaunches;
+  b->launches = nl;
   return check_launch();
 }
 

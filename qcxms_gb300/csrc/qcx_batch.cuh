@@ -117,7 +117,8 @@ struct DevBatch {
   const int* sh_k;     // shell index within the element
   const int* sh_ao;    // local AO offset within the molecule
   // shell pairs (ordered, both directions, same molecule)
-  const ShellPair* pairs;
+  const ShellPair* pairs;  // grouped by angular-momentum class l_a*3 + l_b
+  int pair_off[10];        // class c occupies pairs[pair_off[c] .. pair_off[c+1])
   // pools
   double* mats;
   double* vecs;

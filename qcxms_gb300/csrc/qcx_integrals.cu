@@ -184,26 +184,17 @@ __device__ void pair_integrals(const DevBatch& bt, const MolDesc& md, int s, int
     }
 }
 
+// one kernel per angular-momentum class, so that each gets its own register allocation
+template <int LA, int LB>
 __global__ void k_integrals(DevBatch bt) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= bt.npair) return;
+  constexpr int cls = LA * 3 + LB;
+  int idx = bt.pair_off[cls] + blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= bt.pair_off[cls + 1]) return;
   ShellPair sp = bt.pairs[idx];
   int A = bt.sh_atom[sp.s], B = bt.sh_atom[sp.t];
   if (!bt.active[bt.atom_mol[A]]) return;
   const MolDesc md = bt.mol[bt.atom_mol[A]];
-  const Params& P = *bt.prm;
-  int la = P.sh_l[bt.Z[A]][bt.sh_k[sp.s]], lb = P.sh_l[bt.Z[B]][bt.sh_k[sp.t]];
-  switch (la * 3 + lb) {
-    case 0: pair_integrals<0, 0>(bt, md, sp.s, sp.t, A, B); break;
-    case 1: pair_integrals<0, 1>(bt, md, sp.s, sp.t, A, B); break;
-    case 2: pair_integrals<0, 2>(bt, md, sp.s, sp.t, A, B); break;
-    case 3: pair_integrals<1, 0>(bt, md, sp.s, sp.t, A, B); break;
-    case 4: pair_integrals<1, 1>(bt, md, sp.s, sp.t, A, B); break;
-    case 5: pair_integrals<1, 2>(bt, md, sp.s, sp.t, A, B); break;
-    case 6: pair_integrals<2, 0>(bt, md, sp.s, sp.t, A, B); break;
-    case 7: pair_integrals<2, 1>(bt, md, sp.s, sp.t, A, B); break;
-    default: pair_integrals<2, 2>(bt, md, sp.s, sp.t, A, B); break;
-  }
+  pair_integrals<LA, LB>(bt, md, sp.s, sp.t, A, B);
 }
 
 // ---------------------------------------------------------------------------
@@ -326,39 +317,41 @@ __device__ void pair_gradient(const DevBatch& bt, const MolDesc& md, int s, int 
   atomicAdd(&bt.dedcn[A], P.kcn[za][ka] * kxyp * gS);
 }
 
+template <int LA, int LB>
 __global__ void k_grad_pairs(DevBatch bt) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= bt.npair) return;
+  constexpr int cls = LA * 3 + LB;
+  int idx = bt.pair_off[cls] + blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= bt.pair_off[cls + 1]) return;
   ShellPair sp = bt.pairs[idx];
   int A = bt.sh_atom[sp.s], B = bt.sh_atom[sp.t];
   if (A == B) return;
   if (!bt.active[bt.atom_mol[A]]) return;
   const MolDesc md = bt.mol[bt.atom_mol[A]];
-  const Params& P = *bt.prm;
-  int la = P.sh_l[bt.Z[A]][bt.sh_k[sp.s]], lb = P.sh_l[bt.Z[B]][bt.sh_k[sp.t]];
-  switch (la * 3 + lb) {
-    case 0: pair_gradient<0, 0>(bt, md, sp.s, sp.t, A, B); break;
-    case 1: pair_gradient<0, 1>(bt, md, sp.s, sp.t, A, B); break;
-    case 2: pair_gradient<0, 2>(bt, md, sp.s, sp.t, A, B); break;
-    case 3: pair_gradient<1, 0>(bt, md, sp.s, sp.t, A, B); break;
-    case 4: pair_gradient<1, 1>(bt, md, sp.s, sp.t, A, B); break;
-    case 5: pair_gradient<1, 2>(bt, md, sp.s, sp.t, A, B); break;
-    case 6: pair_gradient<2, 0>(bt, md, sp.s, sp.t, A, B); break;
-    case 7: pair_gradient<2, 1>(bt, md, sp.s, sp.t, A, B); break;
-    default: pair_gradient<2, 2>(bt, md, sp.s, sp.t, A, B); break;
+  pair_gradient<LA, LB>(bt, md, sp.s, sp.t, A, B);
+}
+
+#define QCX_CLASS_KERNELS(KERNEL)                                                                   \
+  static void (*const KERNEL##_table[9])(DevBatch) = {                                              \
+      KERNEL<0, 0>, KERNEL<0, 1>, KERNEL<0, 2>, KERNEL<1, 0>, KERNEL<1, 1>, KERNEL<1, 2>,             \
+      KERNEL<2, 0>, KERNEL<2, 1>, KERNEL<2, 2>};
+
+QCX_CLASS_KERNELS(k_integrals)
+QCX_CLASS_KERNELS(k_grad_pairs)
+
+static int launch_classes(void (*const table[9])(DevBatch), const DevBatch& bt, cudaStream_t st) {
+  int n = 0;
+  const int threads = 128;
+  for (int c = 0; c < 9; ++c) {
+    int cnt = bt.pair_off[c + 1] - bt.pair_off[c];
+    if (cnt <= 0) continue;
+    table[c]<<<(cnt + threads - 1) / threads, threads, 0, st>>>(bt);
+    ++n;
   }
+  return n;
 }
 
-void launch_integrals(const DevBatch& bt, cudaStream_t st) {
-  if (bt.npair == 0) return;
-  int threads = 128;
-  k_integrals<<<(bt.npair + threads - 1) / threads, threads, 0, st>>>(bt);
-}
+int launch_integrals(const DevBatch& bt, cudaStream_t st) { return launch_classes(k_integrals_table, bt, st); }
 
-void launch_grad_pairs(const DevBatch& bt, cudaStream_t st) {
-  if (bt.npair == 0) return;
-  int threads = 128;
-  k_grad_pairs<<<(bt.npair + threads - 1) / threads, threads, 0, st>>>(bt);
-}
+int launch_grad_pairs(const DevBatch& bt, cudaStream_t st) { return launch_classes(k_grad_pairs_table, bt, st); }
 
 }  // namespace qcx

@@ -7,9 +7,11 @@
 namespace qcx {
 
 void launch_cn(const DevBatch& bt, cudaStream_t st);
-void launch_integrals(const DevBatch& bt, cudaStream_t st);
+// The shell-pair kernels launch one specialised kernel per angular-momentum
+// class; they return the number of kernels launched.
+int launch_integrals(const DevBatch& bt, cudaStream_t st);
 void launch_scc(const DevBatch& bt, int precision, cudaStream_t st);
-void launch_grad_pairs(const DevBatch& bt, cudaStream_t st);
+int launch_grad_pairs(const DevBatch& bt, cudaStream_t st);
 void launch_grad_atoms(const DevBatch& bt, cudaStream_t st);
 void launch_leapfrog(const DevBatch& bt, double tstep, cudaStream_t st);
 void launch_zero_grad(const DevBatch& bt, cudaStream_t st);

@@ -230,9 +230,17 @@ extern "C" int qcx_egrad_noalloc(int method, int nat, const int32_t* num, const 
                   kStaticMaxNao);
     return fail(msg);
   }
+  // ordered shell pairs grouped by angular-momentum class
   int npair = 0;
-  for (int s = 0; s < nsh; ++s)
-    for (int t = 0; t < nsh; ++t) h_pairs[npair++] = ShellPair{s, t};
+  int pair_off[10];
+  for (int c = 0; c < 9; ++c) {
+    pair_off[c] = npair;
+    for (int s = 0; s < nsh; ++s)
+      for (int t = 0; t < nsh; ++t)
+        if (qcx_sh_l[h_Z[h_sh_atom[s]]][h_sh_k[s]] * 3 + qcx_sh_l[h_Z[h_sh_atom[t]]][h_sh_k[t]] == c)
+          h_pairs[npair++] = ShellPair{s, t};
+  }
+  pair_off[9] = npair;
   std::memset(&h_mol, 0, sizeof(h_mol));
   h_mol.nat = nat;
   h_mol.nsh = nsh;
@@ -271,6 +279,7 @@ extern "C" int qcx_egrad_noalloc(int method, int nat, const int32_t* num, const 
   d.natom = nat;
   d.nshell = nsh;
   d.npair = npair;
+  for (int c = 0; c < 10; ++c) d.pair_off[c] = pair_off[c];
   d.prm = (const Params*)(base + L.prm);
   d.mol = (const MolDesc*)(base + L.mol);
   d.Z = (const int*)(base + L.Z);
