@@ -14,6 +14,12 @@
 
 namespace qcx {
 
+#ifndef QCX_JAC32_WARM_SWEEPS
+#define QCX_JAC32_WARM_SWEEPS 1
+#endif
+#ifndef QCX_MIXED_SWITCH
+#define QCX_MIXED_SWITCH 1e-4
+#endif
 #ifndef QCX_SCC_THREADS
 #define QCX_SCC_THREADS 512
 #endif
@@ -763,12 +769,13 @@ __device__ bool refine(T* JA, T* JV, const T* F, const double* S, T* Tm, T* Cm, 
 //   from the FP32 eigenvectors after one Newton-Schulz re-orthonormalisation.
 //   Potentials, Fermi level, moments, Broyden and energies are FP64 always.
 // ---------------------------------------------------------------------------
-constexpr double kMixedSwitch = 1e-4;
+constexpr double kMixedSwitch = QCX_MIXED_SWITCH;
 
 // Optional per-phase cycle counters (diagnostic builds only: -DQCX_SCC_PHASE_TIMING).
 #ifdef QCX_SCC_PHASE_TIMING
 __device__ unsigned long long g_phase_cycles[16];
 __device__ unsigned long long g_mol_cycles[4096];
+__device__ unsigned long long g_counts[8];  // refine64 ok, jacobi64 fallbacks
 #define PHASE_BEGIN() long long _pt = clock64()
 #define PHASE_MARK(i)                                                 \
   do {                                                                \
@@ -1017,7 +1024,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       bool ok32 = have32 && QCX_REFINE32_PASSES > 0 &&
                   refine<float>(JA32, JV32, (const float*)F, S, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, 1e-3,
                                 QCX_REFINE32_PASSES, 1e-3, sh, efermi, 25.0 * md.kT);
-      if (!ok32) jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? 8 : 30);
+      if (!ok32) jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? QCX_JAC32_WARM_SWEEPS : 30);
 #ifdef QCX_SCC_PHASE_TIMING
       if (threadIdx.x == 0) atomicAdd(&g_phase_cycles[ok32 ? 13 : 14], 1ull);
 #endif
@@ -1091,6 +1098,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       // FP64 mode: eigenvectors to ~1e-14 every iteration (the oracle's path);
       // mixed mode: one pass suffices once max|K| < 1e-4 (error < 1e-8)
       bool refined = !cold && refine<double>(JA, JV, F, S, T, C, eps, n, 0.2, MIXED ? 1e-4 : 1e-7, 6, 1e-5, sh);
+#ifdef QCX_SCC_PHASE_TIMING
+      if (threadIdx.x == 0 && !cold) atomicAdd(&g_counts[refined ? 0 : 1], 1ull);
+#endif
       if (!refined) {
         int sweeps = jacobi<double>(JA, JV, n, !cold, 1e-12, sh, cold ? 50 : 20);
         if (sweeps < 0) eig_fail = 1;
@@ -1298,6 +1308,14 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
 
 #ifdef QCX_SCC_PHASE_TIMING
 }  // namespace qcx
+extern "C" int qcx_debug_counts(unsigned long long* out, int reset) {
+  if (cudaMemcpyFromSymbol(out, qcx::g_counts, sizeof(unsigned long long) * 8) != cudaSuccess) return -1;
+  if (reset) {
+    unsigned long long z[8] = {0};
+    cudaMemcpyToSymbol(qcx::g_counts, z, sizeof(z));
+  }
+  return 0;
+}
 extern "C" int qcx_debug_mol_cycles(unsigned long long* out, int n) {
   return cudaMemcpyFromSymbol(out, qcx::g_mol_cycles, sizeof(unsigned long long) * (n < 4096 ? n : 4096)) ==
                  cudaSuccess ? 0 : -1;
