@@ -38,10 +38,20 @@ DT_FS = 0.5
 ETEMP = 300.0
 
 
-def workload(rank, ntraj=None):
+def workload(rank, ntraj=None, kind="batch"):
     from qcxms_gb300 import molgen
+    if kind == "cid":
+        n = ntraj or 4096
+        return molgen.cid_workload(n, 10, 80, seed0=rank * n)
     n = ntraj or NTRAJ
     return molgen.batch_workload(n, NMIN, NMAX, seed0=rank * NTRAJ)
+
+
+WORKLOAD_NAMES = {
+    "batch": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs, one CUDA graph per MD step",
+    "cid": "4096 C/H/N/O/S cations, 10-80 atoms, + Ar at 40 eV lab frame, b ~ U(0, 2 A), 0.5 fs, one CUDA graph "
+           "per MD step",
+}
 
 
 def dist_env():
@@ -218,7 +228,7 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     dt = DT_FS * constants.FSTOAU
-    mols = workload(rank, args.ntraj)
+    mols = workload(rank, args.ntraj, args.workload)
     b = qg.Batch(mols, etemp=ETEMP)
     b.set_precision(args.precision)
     b.egrad()
@@ -315,8 +325,8 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": "trajectory-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs, FP64, one CUDA graph "
-                                   "per MD step", "ntraj_per_gpu": b.nmol, "atoms": [NMIN, NMAX],
+            "config": {"workload": WORKLOAD_NAMES[args.workload], "ntraj_per_gpu": b.nmol,
+                       "atoms": [NMIN, NMAX] if args.workload == "batch" else [10, 81],
                        "etemp_K": ETEMP, "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)",
                        "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters)),
                        "mean_scc_iters_fp64": float(np.mean(it64)),
@@ -351,6 +361,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ntraj", type=int, default=None, help="smaller batch for profiling runs (default 256)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "cid"])
     ap.add_argument("--no-plain", action="store_true", help="skip the single-trajectory FP64 reference leg")
     args = ap.parse_args()
     if args.impl == "reference":

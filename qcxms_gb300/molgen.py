@@ -98,3 +98,48 @@ def batch_workload(ntraj, nmin, nmax, seed0=0, tmin=1000.0, tmax=4000.0):
         vel = maxwell_boltzmann(Z, temp, seed0 + t)
         mols.append({"Z": Z, "xyz": xyz, "vel": vel, "mass": masses(Z), "charge": 1, "temp": temp})
     return mols
+
+
+def random_cho(nat, seed):
+    """Random C/H/O molecule (C 0.35, H 0.55, O 0.10) with ``nat`` atoms."""
+    return random_chno(nat, seed, fractions=((6, 0.35), (1, 0.55), (8, 0.10)))
+
+
+AR_Z = 18
+EVTOAU = 1.0 / 27.21138505  # src/xtb_mctc_convert.f90:28-29
+
+
+def cid_workload(ntraj, nmin=10, nmax=80, seed0=0, e_lab_ev=40.0, bmax_aa=2.0, temp=500.0, gap_aa=4.0):
+    """Collision-induced dissociation set-up: a C/H/N/O/S cation and one Ar atom.
+
+    The ion (internal Maxwell-Boltzmann velocities at ``temp``) moves with lab-frame
+    kinetic energy ``e_lab_ev`` towards an Ar atom at rest, offset sideways by an
+    impact parameter b ~ U(0, bmax). As in the reference collision set-up
+    (src/cid.f90:344-399, 512-620) the Ar atom is part of the electronic-structure
+    system, so each trajectory is one molecule of N+1 atoms with charge +1.
+    """
+    mols = []
+    for t in range(ntraj):
+        rng = np.random.default_rng(700000 + seed0 + t)
+        nat = int(rng.integers(nmin, nmax + 1))
+        Z, xyz = random_chno(nat, 50000 + seed0 + t,
+                             fractions=((6, 0.30), (1, 0.50), (7, 0.05), (8, 0.10), (16, 0.05)))
+        m = masses(Z)
+        com = (m[:, None] * xyz).sum(0) / m.sum()
+        xyz = xyz - com
+        rmax = np.linalg.norm(xyz, axis=1).max()
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        w = rng.normal(size=3)
+        w -= w.dot(u) * u
+        w /= np.linalg.norm(w)
+        b = rng.uniform(0.0, bmax_aa) * AATOAU
+        ar = (rmax + gap_aa * AATOAU) * u + b * w
+        vel = maxwell_boltzmann(Z, temp, seed0 + t)
+        vion = np.sqrt(2.0 * e_lab_ev * EVTOAU / m.sum())
+        vel = vel + vion * u
+        Zc = np.concatenate([Z, [AR_Z]]).astype(np.int32)
+        mols.append({"Z": Zc, "xyz": np.vstack([xyz, ar]), "vel": np.vstack([vel, np.zeros(3)]),
+                     "mass": np.concatenate([m, [MASS_AU[AR_Z]]]), "charge": 1, "temp": temp,
+                     "impact_parameter": b})
+    return mols

@@ -1,0 +1,92 @@
+"""GPU checks of the remaining workload configurations.
+
+- differentiation: analytic gradient of 30-atom C/H/O cations against central
+  finite differences (h = 1e-4 Bohr), and torch.autograd.gradcheck through the
+  adjoint;
+- precision: mixed versus FP64 on 60-atom C/H/N/O molecules;
+- collision-induced dissociation: molecule + Ar at 40 eV, parity of the first
+  evaluation with the oracle (includes S d shells and Ar) and a short MD run.
+"""
+import numpy as np
+import pytest
+
+import qcxms_gb300 as qg
+from qcxms_gb300 import constants, molgen, precision_check
+
+pytestmark = pytest.mark.gpu
+KT = 300.0 * constants.KB_AU
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_fd_gradient_30_atom_cations(gpu, seed):
+    Z, xyz = molgen.random_cho(30, 3000 + seed)
+    b = qg.Batch([{"Z": Z, "xyz": xyz, "charge": 1}])
+    b.set_scc(100, 1e-10, 1e-8, 0.25)
+    b.egrad()
+    r = b.get()
+    assert r["status"][0] == 0
+    g = r["grad"]
+    rng = np.random.default_rng(seed)
+    h = 1e-4
+    for _ in range(6):
+        a, k = int(rng.integers(0, len(Z))), int(rng.integers(0, 3))
+        e = []
+        for sgn in (1, -1):
+            x = xyz.copy()
+            x[a, k] += sgn * h
+            b.set_state(xyz=x)
+            b.egrad()
+            rr = b.get()
+            assert rr["status"][0] == 0
+            e.append(rr["energy"][0])
+        assert abs((e[0] - e[1]) / (2 * h) - g[a, k]) < 1e-5
+
+
+def test_autograd_gradcheck(gpu):
+    torch = pytest.importorskip("torch")
+    from qcxms_gb300 import autograd
+    Z = np.array([16, 1, 6, 1])
+    xyz = torch.tensor([[0, 0, 0], [0, 2.4, 0.8], [3.2, -0.4, 0.4], [4.0, 1.4, 0.3]], dtype=torch.float64,
+                       requires_grad=True)
+    f = autograd.energy_function(Z, charge=1)
+    assert torch.autograd.gradcheck(f, (xyz,), eps=1e-4, atol=1e-5, rtol=1e-4, fast_mode=False)
+
+
+def test_precision_60_atoms(gpu):
+    res = precision_check.run(ntraj=4, natoms=60)
+    assert res["both_converged"] >= 3
+    assert res["max_abs_dE"] <= 1e-6
+    assert res["max_abs_dg"] <= 1e-5
+
+
+def test_cid_first_evaluation_matches_oracle(gpu, oracle_lib):
+    mols = molgen.cid_workload(3, nmin=10, nmax=18, seed0=11)
+    b = qg.Batch(mols)
+    b.set_scc(100, 1e-10, 1e-8, 0.25)
+    b.egrad()
+    r = b.get()
+    g = b.split(r["grad"])
+    for i, m in enumerate(mols):
+        rc, e, gref, q, info = oracle_lib.egrad(m["Z"], m["xyz"], 1, kT=KT,
+                                                opts=oracle_lib.default_opts(econv=1e-10, pconv=1e-8))
+        # both sides agree on whether the SCC converges (one of these systems does not)
+        assert (r["status"][i] == 0) == (rc == 0)
+        if rc != 0:
+            continue
+        assert abs(r["energy"][i] - e) < 1e-8
+        assert np.abs(g[i] - gref).max() < 1e-6
+
+
+def test_cid_md_mixed_vs_fp64(gpu):
+    mols = molgen.cid_workload(3, nmin=10, nmax=20, seed0=21)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        b = qg.Batch(mols)
+        b.set_precision(prec)
+        b.egrad()
+        b.step(20, 0.5 * constants.FSTOAU)
+        out[prec] = b.get()
+    ok = (out["fp64"]["status"] == 0) & (out["mixed"]["status"] == 0)
+    assert ok.sum() >= 2
+    assert np.all(np.isfinite(out["mixed"]["energy"]))
+    assert np.abs(out["fp64"]["energy"] - out["mixed"]["energy"])[ok].max() < 1e-5
