@@ -136,7 +136,7 @@ int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat);
  * another runtime's capped pool, or a path that must not trigger the device
  * synchronisation an allocation implies). It has no counterpart in the
  * reference. Same arguments, meaning and return codes as qcx_egrad, but all
- * device scratch is one static __device__ array of about 5 MB that every
+ * device scratch is one static __device__ array of about 6 MB that every
  * GPU loading the library keeps until the process exits; nothing is
  * allocated on the device or the host heap. Limits: QCX_NOALLOC_MAX_ATOMS
  * atoms and QCX_NOALLOC_MAX_NAO atomic orbitals; larger inputs return -1

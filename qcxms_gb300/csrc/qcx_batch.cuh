@@ -12,11 +12,16 @@
 
 namespace qcx {
 
-// matrix slots inside a molecule's matrix block (each n*n doubles)
+// matrix slots inside a molecule's matrix block (each np*np doubles).
+// kS32 holds FP32 copies of S (first n*n floats) and H0 (next n*n floats);
+// kD32 the three dipole and kQ32 the six quadrupole matrices in FP32 (n*n
+// floats each, spanning the slots that follow them). The FP32 SCC iterations
+// read these instead of converting the FP64 matrices element by element.
 enum MatSlot {
   kS = 0, kH0, kX, kF, kT, kA, kV, kC, kP, kW,
   kDm0, kDm1, kDm2,
   kQm0, kQm1, kQm2, kQm3, kQm4, kQm5,
+  kS32, kD32, kD32b, kQ32, kQ32b, kQ32c,
   kNumMat
 };
 

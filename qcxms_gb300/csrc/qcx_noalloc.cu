@@ -11,7 +11,7 @@
 // uses file-scope host buffers, inputs and outputs are plain host pointers.
 //
 // Limits: at most QCX_NOALLOC_MAX_ATOMS atoms and QCX_NOALLOC_MAX_NAO atomic
-// orbitals (64 and 160; about 5 MB of device memory).
+// orbitals (64 and 160; about 6 MB of device memory).
 // The array is held by every GPU that loads the library until the process
 // exits. All calls share it: calls that overlap on the GPU race on it (within
 // one process the host side serialises calls with a mutex, so only work the

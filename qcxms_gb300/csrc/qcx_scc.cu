@@ -8,6 +8,7 @@
 // geometry), X = L^-T, A = X^T F X, cyclic parallel Jacobi on A (round-robin
 // pair ordering, n/2 disjoint rotations per round), C = X V.
 #include <cfloat>
+#include <type_traits>
 
 #include "qcx_batch.cuh"
 #include "qcx_kernels.h"
@@ -34,6 +35,14 @@ namespace qcx {
 #endif
 #ifndef QCX_REFINE32_PASSES
 #define QCX_REFINE32_PASSES 2
+#endif
+#ifndef QCX_REFINE32_KTOL
+#define QCX_REFINE32_KTOL 1e-3
+#endif
+// rounds of exact rotations on the pairs that first-order refinement cannot
+// handle, before the refinement gives up and a Jacobi sweep takes over
+#ifndef QCX_HARD_ROUNDS
+#define QCX_HARD_ROUNDS 6
 #endif
 constexpr int kSccThreads = QCX_SCC_THREADS;
 constexpr int kWarps = kSccThreads / 32;
@@ -321,6 +330,18 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
   // more sweep reaches tol, so that sweep is the last and needs no check sweep
   const double last_below = sqrt(reltol) * fmax(1.0, amax);
   bool last = false;
+  // rotation table of a round: (p, q) pairs and (c, s), s == 0 for a skipped
+  // rotation (rp/rq and rc/rs are contiguous, so they hold half int2 / T2)
+  using T2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+  int2* pq = (int2*)sh.rp;
+  T2* csr = (T2*)sh.rc;
+  const int nblk = half * half;
+  // per-thread start of the block items (k1, k2) and of the row items (k, j);
+  // items advance by blockDim.x, i.e. by (dk1, dk2) and (dk, dj)
+  const int b1 = threadIdx.x / half, b2 = threadIdx.x - b1 * half;
+  const int db1 = blockDim.x / half, db2 = blockDim.x - db1 * half;
+  const int v1 = threadIdx.x / np, v2 = threadIdx.x - v1 * np;
+  const int dv1 = blockDim.x / np, dv2 = blockDim.x - dv1 * np;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     T offmax = 0;
     for (int r = 0; r < m; ++r) {
@@ -330,8 +351,10 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
           p = m;
           q = r;
         } else {
-          p = (r + k) % m;
-          q = (r - k + m) % m;
+          p = r + k;
+          if (p >= m) p -= m;
+          q = r - k;
+          if (q < 0) q += m;
         }
         if (p > q) {
           int t = p;
@@ -341,9 +364,8 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
         T apq = A[p * np + q];
         T aa = apq < T(0) ? -apq : apq;
         offmax = aa > offmax ? aa : offmax;
-        int skip = !(aa > tiny);
         T c = 1, s = 0;
-        if (!skip) {
+        if (aa > tiny) {
           T app = A[p * np + p], aqq = A[q * np + q];
           T theta = (aqq - app) / (T(2) * apq);
           T at = theta < T(0) ? -theta : theta;
@@ -351,43 +373,52 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
           c = T(1) / sqrt(T(1) + t * t);
           s = t * c;
         }
-        sh.rp[k] = p;
-        sh.rq[k] = q;
-        sh.rskip[k] = skip;
-        ((T*)sh.rc)[k] = c;
-        ((T*)sh.rs)[k] = s;
+        pq[k] = make_int2(p, q);
+        T2 cs;
+        cs.x = c;
+        cs.y = s;
+        csr[k] = cs;
       }
       __syncthreads();
       // One fused phase per round: every 2x2 block A[{p1,q1}][{p2,q2}] of a pair
       // of pairs becomes R1 * block * R2^T (each element belongs to exactly one
       // block), and the rows p,q of Vt are rotated by R.
-      const int nblk = half * half;
-      for (int i = threadIdx.x; i < nblk + half * np; i += blockDim.x) {
-        if (i < nblk) {
-          int k1 = i / half, k2 = i - k1 * half;
-          int sk1 = sh.rskip[k1], sk2 = sh.rskip[k2];
-          if (sk1 && sk2) continue;
-          T c1 = ((T*)sh.rc)[k1], s1 = ((T*)sh.rs)[k1];
-          T c2 = ((T*)sh.rc)[k2], s2 = ((T*)sh.rs)[k2];
-          int p1 = sh.rp[k1], q1 = sh.rq[k1], p2 = sh.rp[k2], q2 = sh.rq[k2];
-          T a = A[p1 * np + p2], b = A[p1 * np + q2], c = A[q1 * np + p2], d = A[q1 * np + q2];
+      for (int k1 = b1, k2 = b2; k1 < half;) {
+        T2 r1 = csr[k1], r2 = csr[k2];
+        if (r1.y != T(0) || r2.y != T(0)) {
+          int2 e1 = pq[k1], e2 = pq[k2];
+          T* row_p = A + e1.x * np;
+          T* row_q = A + e1.y * np;
+          T a = row_p[e2.x], b = row_p[e2.y], c = row_q[e2.x], d = row_q[e2.y];
           // rows: R1 = [[c1,-s1],[s1,c1]]
-          T ra = c1 * a - s1 * c, rb = c1 * b - s1 * d;
-          T rc = s1 * a + c1 * c, rd = s1 * b + c1 * d;
+          T ra = r1.x * a - r1.y * c, rb = r1.x * b - r1.y * d;
+          T rc = r1.y * a + r1.x * c, rd = r1.y * b + r1.x * d;
           // columns: multiply by R2^T
-          A[p1 * np + p2] = c2 * ra - s2 * rb;
-          A[p1 * np + q2] = s2 * ra + c2 * rb;
-          A[q1 * np + p2] = c2 * rc - s2 * rd;
-          A[q1 * np + q2] = s2 * rc + c2 * rd;
-        } else {
-          int e = i - nblk;
-          int k = e / np, j = e - k * np;
-          if (sh.rskip[k]) continue;
-          T c = ((T*)sh.rc)[k], s = ((T*)sh.rs)[k];
-          int p = sh.rp[k], q = sh.rq[k];
-          T vp = Vt[p * np + j], vq = Vt[q * np + j];
-          Vt[p * np + j] = c * vp - s * vq;
-          Vt[q * np + j] = s * vp + c * vq;
+          row_p[e2.x] = r2.x * ra - r2.y * rb;
+          row_p[e2.y] = r2.y * ra + r2.x * rb;
+          row_q[e2.x] = r2.x * rc - r2.y * rd;
+          row_q[e2.y] = r2.y * rc + r2.x * rd;
+        }
+        k1 += db1;
+        k2 += db2;
+        if (k2 >= half) {
+          k2 -= half;
+          ++k1;
+        }
+      }
+      for (int k = v1, j = v2; k < half;) {
+        T2 rr = csr[k];
+        if (rr.y != T(0)) {
+          int2 e = pq[k];
+          T vp = Vt[e.x * np + j], vq = Vt[e.y * np + j];
+          Vt[e.x * np + j] = rr.x * vp - rr.y * vq;
+          Vt[e.y * np + j] = rr.y * vp + rr.x * vq;
+        }
+        k += dv1;
+        j += dv2;
+        if (j >= np) {
+          j -= np;
+          ++k;
         }
       }
       __syncthreads();
@@ -641,6 +672,95 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 }
 
 // ---------------------------------------------------------------------------
+// Exact Jacobi rotations on the pairs that are too far from diagonal for the
+// first-order refinement: Km (ld n) holds the first-order coefficients, row i
+// picks its partner j with the largest |K_ij| above khard, and thread 0 keeps
+// a set of disjoint pairs (rows in index order, so the choice is
+// deterministic). Each kept pair (p, q) gets the rotation that zeroes B_pq; B
+// is rotated on both sides (all rows first, then all columns, which is
+// R B R^T for commuting disjoint rotations) and so are the coefficient rows,
+// with the conventions of jacobi(). Returns the number of rotations.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ int rotate_hard_pairs(T* JA, T* JV, const T* Km, int n, T khard, SccShared& sh) {
+  const int np = n + (n & 1);
+  int* best = sh.perm;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    T bk = khard;
+    int bj = -1;
+    for (int j = 0; j < n; ++j) {
+      T k = Km[(long long)i * n + j];
+      k = k < T(0) ? -k : k;
+      if (k > bk) {
+        bk = k;
+        bj = j;
+      }
+    }
+    best[i] = bj;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned* used = (unsigned*)sh.red;  // one bit per orbital: 16 kWarps doubles hold 1024 kWarps bits
+    const int words = (n + 31) >> 5;
+    for (int w = 0; w < words; ++w) used[w] = 0u;
+    int cnt = 0;
+    for (int i = 0; i < n; ++i) {
+      int j = best[i];
+      if (j < 0) continue;
+      if (((used[i >> 5] >> (i & 31)) | (used[j >> 5] >> (j & 31))) & 1u) continue;
+      used[i >> 5] |= 1u << (i & 31);
+      used[j >> 5] |= 1u << (j & 31);
+      sh.rp[cnt] = i < j ? i : j;
+      sh.rq[cnt] = i < j ? j : i;
+      ++cnt;
+    }
+    sh.rskip[0] = cnt;
+  }
+  __syncthreads();
+  const int cnt = sh.rskip[0];
+  T* rc = (T*)sh.rc;
+  T* rs = (T*)sh.rs;
+  for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+    int p = sh.rp[k], q = sh.rq[k];
+    T apq = T(0.5) * (JA[p * np + q] + JA[q * np + p]);
+    T app = JA[p * np + p], aqq = JA[q * np + q];
+    T c = 1, s = 0;
+    if (apq != T(0)) {
+      T theta = (aqq - app) / (T(2) * apq);
+      T at = theta < T(0) ? -theta : theta;
+      T t = (theta >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + theta * theta));
+      c = T(1) / sqrt(T(1) + t * t);
+      s = t * c;
+    }
+    rc[k] = c;
+    rs[k] = s;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < cnt * n; e += blockDim.x) {
+    int k = e / n, j = e - k * n;
+    int p = sh.rp[k], q = sh.rq[k];
+    T c = rc[k], s = rs[k];
+    T ap = JA[p * np + j], aq = JA[q * np + j];
+    JA[p * np + j] = c * ap - s * aq;
+    JA[q * np + j] = s * ap + c * aq;
+    T vp = JV[p * np + j], vq = JV[q * np + j];
+    JV[p * np + j] = c * vp - s * vq;
+    JV[q * np + j] = s * vp + c * vq;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < cnt * n; e += blockDim.x) {
+    int k = e / n, i = e - k * n;
+    int p = sh.rp[k], q = sh.rq[k];
+    T c = rc[k], s = rs[k];
+    T ap = JA[i * np + p], aq = JA[i * np + q];
+    JA[i * np + p] = c * ap - s * aq;
+    JA[i * np + q] = s * ap + c * aq;
+  }
+  __syncthreads();
+  return cnt;
+}
+
+// ---------------------------------------------------------------------------
 // GEMM-form eigenvector refinement in a nearly diagonal basis (T = float or
 // double).
 //
@@ -650,26 +770,32 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
 // followed by one Newton-Schulz step that restores S-orthonormality, and the
 // eigenvalues as B_jj + sum_i B_ij K_ij. A pass leaves an error of order
 // max|K|^2; passes repeat (recomputing B) until the max|K| of a pass is below
-// ktol (the remaining error is then below ktol^2). Returns false
-// without touching JV when the basis is too far from diagonal (max|K| > kfail
-// on the first pass) or the passes do not reach ktol; the caller then runs
-// Jacobi on the current B (which JA holds in that case). On success JA's
-// diagonal holds the eigenvalues.
+// ktol (the remaining error is then below ktol^2). In FP32, pairs with
+// |K| > kfail are first rotated exactly (rotate_hard_pairs, up to
+// QCX_HARD_ROUNDS rounds per call).
+// Returns false when the basis stays too far from diagonal or the passes do
+// not reach ktol; JA then holds B for the current rows of JV and the caller
+// runs Jacobi on it. On success JA's diagonal holds the eigenvalues.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ bool refine(T* JA, T* JV, const T* F, const double* S, T* Tm, T* Cm, double* tmp, int n,
+__device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, double* tmp, int n,
                        double kfail, double ktol, int max_pass, double ns_min, SccShared& sh,
                        double mu = 0.0, double occ_gap = -1.0) {
   const int np = n + (n & 1);
+  int hard = 0;       // rounds of exact rotations so far
+  bool fresh = true;  // JA holds B for the current rows of JV
   for (int pass = 0; pass < max_pass; ++pass) {
-    if (pass > 0) {
+    if (pass > 0 && !fresh) {
       cta_gemm<T, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
       __syncthreads();
       cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, JA, np);
       __syncthreads();
     }
-    // K^T[j][i] = K_ij = B_ij / (B_jj - B_ii) into Tm (ld n)
-    double kmax = 0.0;
+    fresh = false;
+    // K^T[j][i] = K_ij = B_ij / (B_jj - B_ii) into Tm (ld n). All arithmetic
+    // in T: FP64 instructions inside the FP32 iterations cost the FP64 rate.
+    T kmax_t = T(0);
+    const T mu_t = (T)mu, gap_t = (T)occ_gap;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
       int j = e / n, i = e - j * n;
       T k = T(0);
@@ -680,17 +806,26 @@ __device__ bool refine(T* JA, T* JV, const T* F, const double* S, T* Tm, T* Cm, 
         // empty (further than occ_gap from mu, same side) leaves the density
         // unchanged, so such pairs are not rotated
         bool same = false;
-        if (occ_gap > 0.0) {
-          double ei = (double)JA[i * np + i] - mu, ej = (double)JA[j * np + j] - mu;
-          same = (ei > occ_gap && ej > occ_gap) || (ei < -occ_gap && ej < -occ_gap);
+        if (gap_t > T(0)) {
+          T ei = JA[i * np + i] - mu_t, ej = JA[j * np + j] - mu_t;
+          same = (ei > gap_t && ej > gap_t) || (ei < -gap_t && ej < -gap_t);
         }
         if (b != T(0) && !same) k = (d > T(1e-30) || d < T(-1e-30)) ? b / d : T(1e30);
       }
       Tm[e] = k;
-      kmax = fmax(kmax, fabs((double)k));
+      T ka = k < T(0) ? -k : k;
+      kmax_t = ka > kmax_t ? ka : kmax_t;
     }
-    kmax = cta_max(kmax, sh.red);
+    double kmax = cta_max((double)kmax_t, sh.red);
     if (kmax > kfail) {
+      // rotate the offending pairs exactly (B stays expressed in the rotated
+      // basis, so no recomputation) and look again
+      if (sizeof(T) == 4 && hard < QCX_HARD_ROUNDS && rotate_hard_pairs<T>(JA, JV, Tm, n, (T)kfail, sh) > 0) {
+        ++hard;
+        --pass;
+        fresh = true;
+        continue;
+      }
       if (pass == 0) return false;
       // the basis moved but did not converge: give the current B to Jacobi
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -705,14 +840,15 @@ __device__ bool refine(T* JA, T* JV, const T* F, const double* S, T* Tm, T* Cm, 
       return false;
     }
     // second-order eigenvalues onto the diagonal of B
+    T* lamv = (T*)tmp;
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      double lam = (double)JA[j * np + j];
+      T lam = JA[j * np + j];
       for (int i = 0; i < n; ++i)
-        if (i != j) lam += 0.5 * (double)(JA[i * np + j] + JA[j * np + i]) * (double)Tm[(long long)j * n + i];
-      tmp[j] = lam;
+        if (i != j) lam += T(0.5) * (JA[i * np + j] + JA[j * np + i]) * Tm[(long long)j * n + i];
+      lamv[j] = lam;
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < n; j += blockDim.x) JA[j * np + j] = (T)tmp[j];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) JA[j * np + j] = lamv[j];
     if (kmax == 0.0) return true;
     // C^T <- C^T + K^T C^T
     cta_gemm<T, T, T, T>(n, n, n, Tm, n, false, JV, np, false, Cm, n);
@@ -726,19 +862,32 @@ __device__ bool refine(T* JA, T* JV, const T* F, const double* S, T* Tm, T* Cm, 
       if (kmax < ktol) return true;
       continue;
     }
-    cta_gemm<double, T, T, T>(n, n, n, S, n, false, JV, np, true, Tm, n);
-    __syncthreads();
-    cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, Cm, n);
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-      int i = e / n, j = e % n;
-      Cm[e] = (i == j ? T(1.5) : T(0)) - T(0.5) * Cm[e];
+    // FP64: one step (later passes and iterations remove what is left). FP32:
+    // the exact rotations let first-order steps of up to kfail through, whose
+    // O(K^2) defect one step does not remove, so steps repeat until the defect
+    // predicted from the measured one (3/4 n E^2) is at FP32 rounding level.
+    const int ns_steps = sizeof(T) == 4 ? 3 : 1;
+    for (int st = 0; st < ns_steps; ++st) {
+      cta_gemm<T, T, T, T>(n, n, n, S, n, false, JV, np, true, Tm, n);
+      __syncthreads();
+      cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, Cm, n);
+      __syncthreads();
+      T emax_t = T(0);
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        int i = e / n, j = e % n;
+        T d = Cm[e] - (i == j ? T(1) : T(0));
+        T ad = d < T(0) ? -d : d;
+        emax_t = ad > emax_t ? ad : emax_t;
+        Cm[e] = (i == j ? T(1) : T(0)) - T(0.5) * d;
+      }
+      double emax = ns_steps > 1 ? cta_max((double)emax_t, sh.red) : 0.0;
+      __syncthreads();
+      cta_gemm<T, T, T, T>(n, n, n, Cm, n, false, JV, np, false, Tm, n);
+      __syncthreads();
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = Tm[e];
+      __syncthreads();
+      if (0.75 * n * emax * emax < 1e-9) break;
     }
-    __syncthreads();
-    cta_gemm<T, T, T, T>(n, n, n, Cm, n, false, JV, np, false, Tm, n);
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = Tm[e];
-    __syncthreads();
     // the remaining off-diagonal is of order kmax^2: stop once that is below ktol^2
     if (kmax < ktol) return true;
   }
@@ -757,6 +906,235 @@ __device__ bool refine(T* JA, T* JV, const T* F, const double* S, T* Tm, T* Cm, 
   }
   __syncthreads();
   return false;
+}
+
+// ---------------------------------------------------------------------------
+// Double-float arithmetic for the finishing iterations of mixed mode.
+//
+// A value is held as an unevaluated sum hi + lo of two FP32 numbers (Dekker
+// 1971; the "double-single" or "df64" representation), about 48 significant
+// bits. Products use the exact FMA splitting of hi*hi and sums use Knuth's
+// two-sum, so a dot product of length n carries a relative error of order
+// n 2^-46 while running on the FP32 pipes, which GB300 executes at 58 times
+// the FP64 rate. All steps use explicitly rounded intrinsics so that the
+// compiler cannot contract or reorder them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void dd_split(double x, float& hi, float& lo) {
+  hi = __double2float_rn(x);
+  lo = __double2float_rn(x - (double)hi);
+}
+
+// (sh, sl) += (ah + al) (bh + bl), dropping al*bl
+__device__ __forceinline__ void dd_fma(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  float p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  float s = __fadd_rn(sh, p);
+  float v = __fsub_rn(s, sh);
+  float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(p, v));
+  sl = __fadd_rn(sl, __fadd_rn(t, e));
+  sh = s;
+}
+
+// renormalise so that |lo| <= ulp(hi) / 2 (fast two-sum; |hi| >= |lo| holds)
+__device__ __forceinline__ void dd_norm(float& hi, float& lo) {
+  float s = __fadd_rn(hi, lo);
+  lo = __fsub_rn(lo, __fsub_rn(s, hi));
+  hi = s;
+}
+
+// (h, l) += d
+__device__ __forceinline__ void dd_add(float& h, float& l, float d) {
+  float s = __fadd_rn(h, d);
+  float v = __fsub_rn(s, h);
+  float t = __fadd_rn(__fsub_rn(h, __fsub_rn(s, v)), __fsub_rn(d, v));
+  l = __fadd_rn(l, t);
+  h = s;
+  dd_norm(h, l);
+}
+
+// C = op(A) op(B) in double-float, with the index conventions of cta_gemm
+// (ta: A stored K x M; tb: B stored N x K). Each operand is a pair of planes
+// (hi, lo) with the same leading dimension. The result goes to the planes
+// (Ch, Cl), or, when Cd is given, to Cd as FP64.
+__device__ void cta_gemm_dd(int M, int N, int K, const float* Ah, const float* Al, int lda, bool ta, const float* Bh,
+                            const float* Bl, int ldb, bool tb, float* Ch, float* Cl, double* Cd, int ldc) {
+  int tilesM = (M + 1) / 2, tilesN = (N + 1) / 2;
+  for (int t = threadIdx.x; t < tilesM * tilesN; t += blockDim.x) {
+    int i0 = (t / tilesN) * 2, j0 = (t % tilesN) * 2;
+    bool i1ok = i0 + 1 < M, j1ok = j0 + 1 < N;
+    int i1 = i1ok ? i0 + 1 : i0, j1 = j1ok ? j0 + 1 : j0;
+    float h00 = 0.f, l00 = 0.f, h01 = 0.f, l01 = 0.f, h10 = 0.f, l10 = 0.f, h11 = 0.f, l11 = 0.f;
+    for (int k = 0; k < K; ++k) {
+      long long a0 = ta ? (long long)k * lda + i0 : (long long)i0 * lda + k;
+      long long a1 = ta ? (long long)k * lda + i1 : (long long)i1 * lda + k;
+      long long b0 = tb ? (long long)j0 * ldb + k : (long long)k * ldb + j0;
+      long long b1 = tb ? (long long)j1 * ldb + k : (long long)k * ldb + j1;
+      float a0h = Ah[a0], a0l = Al[a0], a1h = Ah[a1], a1l = Al[a1];
+      float b0h = Bh[b0], b0l = Bl[b0], b1h = Bh[b1], b1l = Bl[b1];
+      dd_fma(h00, l00, a0h, a0l, b0h, b0l);
+      dd_fma(h01, l01, a0h, a0l, b1h, b1l);
+      dd_fma(h10, l10, a1h, a1l, b0h, b0l);
+      dd_fma(h11, l11, a1h, a1l, b1h, b1l);
+    }
+    dd_norm(h00, l00);
+    dd_norm(h01, l01);
+    dd_norm(h10, l10);
+    dd_norm(h11, l11);
+    auto put = [&](int i, int j, float h, float l) {
+      long long c = (long long)i * ldc + j;
+      if (Cd) {
+        Cd[c] = (double)h + (double)l;
+      } else {
+        Ch[c] = h;
+        Cl[c] = l;
+      }
+    };
+    put(i0, j0, h00, l00);
+    if (j1ok) put(i0, j1, h01, l01);
+    if (i1ok) {
+      put(i1, j0, h10, l10);
+      if (j1ok) put(i1, j1, h11, l11);
+    }
+  }
+}
+
+// Double-float coefficient rows and the matrices of one molecule's finishing
+// iterations (mixed mode). Planes: V (rows = MOs, ld np), B = V F V^T (ld np),
+// F and S (ld n), T and M scratch (ld n); Kf and dV are FP32 scratch (ld n).
+struct DDMats {
+  float *Vh, *Vl, *Bh, *Bl, *Fh, *Fl, *Sh, *Sl, *Th, *Tl, *Mh, *Ml, *Kf, *dV;
+};
+
+// V <- V + dV (dV FP32, ld n) in double-float
+__device__ void dd_add_rows(const DDMats& d, int n, int np) {
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int i = e / n, j = e - i * n;
+    long long x = (long long)i * np + j;
+    float h = d.Vh[x], l = d.Vl[x];
+    dd_add(h, l, d.dV[e]);
+    d.Vh[x] = h;
+    d.Vl[x] = l;
+  }
+  __syncthreads();
+}
+
+// B = V F V^T
+__device__ void dd_rotate_fock(const DDMats& d, int n, int np) {
+  cta_gemm_dd(n, n, n, d.Fh, d.Fl, n, false, d.Vh, d.Vl, np, true, d.Th, d.Tl, nullptr, n);
+  __syncthreads();
+  cta_gemm_dd(n, n, n, d.Vh, d.Vl, np, false, d.Th, d.Tl, n, false, d.Bh, d.Bl, nullptr, np);
+  __syncthreads();
+}
+
+// Newton-Schulz steps V <- (3I - V S V^T)/2 V: the overlap V S V^T in
+// double-float, the (small) correction -(V S V^T - I)/2 V in FP32. Returns the
+// largest |V S V^T - I| seen before the last step.
+__device__ double dd_orthonormalize(const DDMats& d, int n, int np, int steps, SccShared& sh) {
+  double emax = 0.0;
+  for (int st = 0; st < steps; ++st) {
+    cta_gemm_dd(n, n, n, d.Sh, d.Sl, n, false, d.Vh, d.Vl, np, true, d.Th, d.Tl, nullptr, n);
+    __syncthreads();
+    cta_gemm_dd(n, n, n, d.Vh, d.Vl, np, false, d.Th, d.Tl, n, false, d.Mh, d.Ml, nullptr, n);
+    __syncthreads();
+    float em = 0.f;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      int i = e / n, j = e - i * n;
+      float dev = __fadd_rn(__fsub_rn(d.Mh[e], i == j ? 1.f : 0.f), d.Ml[e]);
+      em = fmaxf(em, fabsf(dev));
+      d.Kf[e] = -0.5f * dev;
+    }
+    emax = cta_max((double)em, sh.red);
+    cta_gemm<float, float, float, float>(n, n, n, d.Kf, n, false, d.Vh, np, false, d.dV, n);
+    __syncthreads();
+    dd_add_rows(d, n, np);
+    // the defect left is about 3/4 n emax^2
+    if (0.75 * n * emax * emax < 1e-26) break;
+  }
+  return emax;
+}
+
+// First-order refinement of the double-float rows V against B = V F V^T (held
+// in d.B on entry), as refine() does in FP32/FP64: K_ij = B_ij / (B_jj - B_ii)
+// in FP32 from the double-float B, V <- V + K^T V with the product in FP32
+// (K is small, so its rounding is far below the double-float level of V), and
+// Newton-Schulz in double-float when max|K| >= ns_min. Eigenvalues (second
+// order) go to lam. Returns false if max|K| exceeds kfail or the passes do not
+// reach ktol; B then holds V F V^T for the current rows.
+__device__ bool refine_dd(const DDMats& d, int n, double* lam, double kfail, double ktol, int max_pass,
+                          double ns_min, SccShared& sh) {
+  const int np = n + (n & 1);
+  for (int pass = 0; pass < max_pass; ++pass) {
+    if (pass > 0) dd_rotate_fock(d, n, np);
+    // diagonal in FP64
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      long long x = (long long)i * np + i;
+      lam[i] = (double)d.Bh[x] + (double)d.Bl[x];
+    }
+    __syncthreads();
+    float km = 0.f;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      int j = e / n, i = e - j * n;
+      float k = 0.f;
+      if (i != j) {
+        float b = 0.5f * (d.Bh[(long long)i * np + j] + d.Bh[(long long)j * np + i]);
+        float dd = __double2float_rn(lam[j] - lam[i]);
+        if (b != 0.f) k = (dd > 1e-30f || dd < -1e-30f) ? b / dd : 1e30f;
+      }
+      d.Kf[e] = k;  // K^T[j][i] = K_ij
+      km = fmaxf(km, fabsf(k));
+    }
+    double kmax = cta_max((double)km, sh.red);
+    if (kmax > kfail) return false;
+    // second-order eigenvalues
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      float c = 0.f;
+      for (int i = 0; i < n; ++i)
+        if (i != j) c += 0.5f * (d.Bh[(long long)i * np + j] + d.Bh[(long long)j * np + i]) * d.Kf[(long long)j * n + i];
+      d.dV[j] = c;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x) lam[j] += (double)d.dV[j];
+    __syncthreads();
+    if (kmax == 0.0) return true;
+    cta_gemm<float, float, float, float>(n, n, n, d.Kf, n, false, d.Vh, np, false, d.dV, n);
+    __syncthreads();
+    dd_add_rows(d, n, np);
+    if (kmax >= ns_min) dd_orthonormalize(d, n, np, 1, sh);
+    if (kmax < ktol) return true;
+  }
+  dd_rotate_fock(d, n, np);
+  return false;
+}
+
+// Cd = sum_{k < nocc} w_k v_k^T v_k (FP64 result, ld n) for the double-float
+// rows v_k = V[perm[k]]: G_k = w_k v_k goes to the T planes, the rows in order
+// to the M planes, and one double-float product G^T V_occ forms the matrix.
+__device__ void dd_density(const DDMats& d, int n, int nocc, const int* perm, const double* w, double* Cd,
+                           SccShared& sh) {
+  const int np = n + (n & 1);
+  float* wh = (float*)sh.rc;  // np floats each: the rotation scratch is free here
+  float* wl = (float*)sh.rs;
+  for (int k = threadIdx.x; k < nocc; k += blockDim.x) dd_split(w[k], wh[k], wl[k]);
+  __syncthreads();
+  for (int e = threadIdx.x; e < nocc * n; e += blockDim.x) {
+    int k = e / n, j = e - k * n;
+    long long x = (long long)perm[k] * np + j;
+    float vh = d.Vh[x], vl = d.Vl[x];
+    float p = __fmul_rn(wh[k], vh);
+    float er = __fmaf_rn(wh[k], vh, -p);
+    er = __fmaf_rn(wh[k], vl, er);
+    er = __fmaf_rn(wl[k], vh, er);
+    dd_norm(p, er);
+    d.Th[e] = p;
+    d.Tl[e] = er;
+    d.Mh[e] = vh;
+    d.Ml[e] = vl;
+  }
+  __syncthreads();
+  cta_gemm_dd(n, n, nocc, d.Th, d.Tl, n, true, d.Mh, d.Ml, n, false, nullptr, nullptr, Cd, n);
+  __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -933,8 +1311,42 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     }
   }
   __syncthreads();
-  if (MIXED)
-    for (long long e = threadIdx.x; e < nn; e += blockDim.x) X32[e] = (float)X[e];
+  // FP32 copies of the fixed matrices for the FP32 iterations (conversions
+  // from FP64 run at the FP64 rate, so they are done once here)
+  float* S32 = (float*)mat_ptr(bt, md, kS32);
+  float* H032 = S32 + nn;
+  float* D32 = (float*)mat_ptr(bt, md, kD32);
+  float* Q32 = (float*)mat_ptr(bt, md, kQ32);
+  // double-float planes of the finishing iterations (mixed mode): V in the
+  // coefficient storage, B in the A storage, F in the F slot, S as the FP32
+  // copy plus a lo plane in the W slot (free until W is formed), scratch in
+  // the T, C and X slots (X is only needed without an FP32 phase)
+  DDMats dm;
+  dm.Vh = (float*)JV;
+  dm.Vl = dm.Vh + (long long)np * np;
+  dm.Bh = (float*)JA;
+  dm.Bl = dm.Bh + (long long)np * np;
+  dm.Fh = (float*)F;
+  dm.Fl = dm.Fh + nn;
+  dm.Sh = S32;
+  dm.Sl = (float*)Wm;
+  dm.Th = (float*)T;
+  dm.Tl = dm.Th + nn;
+  dm.Mh = (float*)C;
+  dm.Ml = dm.Mh + nn;
+  dm.Kf = (float*)X;
+  dm.dV = dm.Kf + nn;
+  if (MIXED) {
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+      X32[e] = (float)X[e];
+      S32[e] = (float)S[e];
+      H032[e] = (float)H0[e];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) D32[c * nn + e] = (float)Dm[c * nn + e];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) Q32[c * nn + e] = (float)Qm[c * nn + e];
+    }
+  }
   for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = 0.0;
   __syncthreads();
 
@@ -962,19 +1374,25 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       const double* vdp = vec + mv.vl.vdp;
       const double* vqp = vec + mv.vl.vqp;
       if (fp32_phase) {
-        // FP32 iterations: the Fock matrix only feeds FP32 products
+        // FP32 iterations: the Fock matrix only feeds FP32 products. The
+        // potentials go to shared memory as FP32 (the moment scratch is free
+        // until the moments are formed: nsh + 9 nat <= 10 n floats).
+        float* vs32 = (float*)sh.mom;
+        float* vd32 = vs32 + nsh;
+        float* vq32 = vd32 + 3 * nat;
+        for (int i = threadIdx.x; i < nsh + 9 * nat; i += blockDim.x)
+          vs32[i] = (float)(i < nsh ? vsh[i] : (i < nsh + 3 * nat ? vdp[i - nsh] : vqp[i - nsh - 3 * nat]));
+        __syncthreads();
         float* F32 = (float*)F;
         for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
           int i = (int)(e / n), j = (int)(e % n);
           int A = sh.ao_at[i], B = sh.ao_at[j];
           long long ji = (long long)j * n + i;
-          float f = (float)H0[e] - 0.5f * (float)S[e] * (float)(vsh[sh.ao_sh[i]] + vsh[sh.ao_sh[j]]);
+          float f = H032[e] - 0.5f * S32[e] * (vs32[sh.ao_sh[i]] + vs32[sh.ao_sh[j]]);
 #pragma unroll
-          for (int c = 0; c < 3; ++c)
-            f -= 0.5f * ((float)vdp[3 * A + c] * (float)Dm[c * nn + e] + (float)vdp[3 * B + c] * (float)Dm[c * nn + ji]);
+          for (int c = 0; c < 3; ++c) f -= 0.5f * (vd32[3 * A + c] * D32[c * nn + e] + vd32[3 * B + c] * D32[c * nn + ji]);
 #pragma unroll
-          for (int c = 0; c < 6; ++c)
-            f -= 0.5f * ((float)vqp[6 * A + c] * (float)Qm[c * nn + e] + (float)vqp[6 * B + c] * (float)Qm[c * nn + ji]);
+          for (int c = 0; c < 6; ++c) f -= 0.5f * (vq32[6 * A + c] * Q32[c * nn + e] + vq32[6 * B + c] * Q32[c * nn + ji]);
           F32[e] = f;
         }
       } else {
@@ -987,7 +1405,8 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
           for (int c = 0; c < 3; ++c) f -= 0.5 * (vdp[3 * A + c] * Dm[c * nn + e] + vdp[3 * B + c] * Dm[c * nn + ji]);
 #pragma unroll
           for (int c = 0; c < 6; ++c) f -= 0.5 * (vqp[6 * A + c] * Qm[c * nn + e] + vqp[6 * B + c] * Qm[c * nn + ji]);
-          F[e] = f;
+          if (MIXED && have32) dd_split(f, dm.Fh[e], dm.Fl[e]);  // double-float finishing iterations
+          else F[e] = f;
         }
       }
     }
@@ -1022,7 +1441,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       __syncthreads();
       PHASE_MARK(2);
       bool ok32 = have32 && QCX_REFINE32_PASSES > 0 &&
-                  refine<float>(JA32, JV32, (const float*)F, S, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, 1e-3,
+                  refine<float>(JA32, JV32, (const float*)F, S32, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, QCX_REFINE32_KTOL,
                                 QCX_REFINE32_PASSES, 1e-3, sh, efermi, 25.0 * md.kT);
       if (!ok32) jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? QCX_JAC32_WARM_SWEEPS : 30);
 #ifdef QCX_SCC_PHASE_TIMING
@@ -1045,6 +1464,74 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         }
         sh.perm[rank] = i;
         eps[rank] = (double)di;
+      }
+      __syncthreads();
+    } else if (MIXED && have32) {
+      // ---- finishing iteration of mixed mode, in double-float ----
+      double* lam = sh.mom;  // n eigenvalues (the moment scratch is free here)
+      if (!have64) {
+        // FP32 coefficients -> double-float rows, re-orthonormalised in the S
+        // metric (the FP32 rows live in the lo plane of B, so this precedes B)
+        for (long long e = threadIdx.x; e < (long long)np * np; e += blockDim.x) {
+          dm.Vh[e] = JV32[e];
+          dm.Vl[e] = 0.f;
+        }
+        for (long long e = threadIdx.x; e < nn; e += blockDim.x) dm.Sl[e] = __double2float_rn(S[e] - (double)S32[e]);
+        __syncthreads();
+        dd_orthonormalize(dm, n, np, 2, sh);
+      }
+      dd_rotate_fock(dm, n, np);
+      PHASE_MARK(4);
+      bool refined = refine_dd(dm, n, lam, 0.2, 1e-4, 6, 1e-5, sh);
+#ifdef QCX_SCC_PHASE_TIMING
+      if (threadIdx.x == 0) atomicAdd(&g_counts[refined ? 0 : 1], 1ull);
+#endif
+      if (!refined) {
+        // FP64 Jacobi on B in the current basis: planes -> FP64 through the T
+        // and C slots, and the rotated rows back to double-float
+        float* tB = (float*)T;
+        float* tV = (float*)C;
+        const long long np2 = (long long)np * np;
+        for (long long e = threadIdx.x; e < np2; e += blockDim.x) {
+          tB[e] = dm.Bh[e];
+          tB[np2 + e] = dm.Bl[e];
+          tV[e] = dm.Vh[e];
+          tV[np2 + e] = dm.Vl[e];
+        }
+        __syncthreads();
+        for (long long e = threadIdx.x; e < np2; e += blockDim.x) {
+          JA[e] = (double)tB[e] + (double)tB[np2 + e];
+          JV[e] = (double)tV[e] + (double)tV[np2 + e];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+          int i = e / n, j = e % n;
+          if (j < i) {
+            double s = 0.5 * (JA[i * np + j] + JA[j * np + i]);
+            JA[i * np + j] = s;
+            JA[j * np + i] = s;
+          }
+        }
+        __syncthreads();
+        if (jacobi<double>(JA, JV, n, true, 1e-12, sh, 20) < 0) eig_fail = 1;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) lam[i] = JA[i * np + i];
+        double* tD = C;
+        for (long long e = threadIdx.x; e < np2; e += blockDim.x) tD[e] = JV[e];
+        __syncthreads();
+        for (long long e = threadIdx.x; e < np2; e += blockDim.x) dd_split(tD[e], dm.Vh[e], dm.Vl[e]);
+        __syncthreads();
+      }
+      PHASE_MARK(5);
+      have64 = true;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double di = lam[i];
+        int rank = 0;
+        for (int j = 0; j < n; ++j) {
+          double dj = lam[j];
+          rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
+        }
+        sh.perm[rank] = i;
+        eps[rank] = di;
       }
       __syncthreads();
     } else {
@@ -1137,29 +1624,42 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     __syncthreads();
     ets = sh.scal[0];
     efermi = sh.scal[1];
+    // occupations are >= 0, so focc > 0 is a test on the bit pattern (no FP64 compare)
     for (int k = 0; k < n; ++k)
-      if (focc[k] > 0.0) nocc = k + 1;
+      if (__double_as_longlong(focc[k]) > 0) nocc = k + 1;
     PHASE_MARK(7);
-    // P = C f C^T over the occupied (sorted) orbitals
-    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-      int i = (int)(e / n), j = (int)(e % n);
-      if (j < i) continue;
-      double p = 0.0;
-      if (fp32_phase) {
+    // P = C f C^T over the occupied (sorted) orbitals; the FP32 iterations keep
+    // P as FP32 (in the P slot) for the FP32 moments
+    if (fp32_phase) {
+      float* f32 = (float*)sh.rc;  // np floats; the rotation scratch is free after the eigensolve
+      for (int k = threadIdx.x; k < nocc; k += blockDim.x) f32[k] = (float)focc[k];
+      __syncthreads();
+      float* P32 = (float*)Pm;
+      for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+        int i = (int)(e / n), j = (int)(e % n);
+        if (j < i) continue;
         float pf = 0.0f;
         for (int k = 0; k < nocc; ++k) {
           int c = sh.perm[k];
-          pf += (float)focc[k] * JV32[(long long)c * np + i] * JV32[(long long)c * np + j];
+          pf += f32[k] * JV32[(long long)c * np + i] * JV32[(long long)c * np + j];
         }
-        p = (double)pf;
-      } else {
+        P32[(long long)i * n + j] = pf;
+        P32[(long long)j * n + i] = pf;
+      }
+    } else if (MIXED && have32) {
+      dd_density(dm, n, nocc, sh.perm, focc, Pm, sh);
+    } else {
+      for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+        int i = (int)(e / n), j = (int)(e % n);
+        if (j < i) continue;
+        double p = 0.0;
         for (int k = 0; k < nocc; ++k) {
           int c = sh.perm[k];
           p += focc[k] * JV[(long long)c * np + i] * JV[(long long)c * np + j];
         }
+        Pm[(long long)i * n + j] = p;
+        Pm[(long long)j * n + i] = p;
       }
-      Pm[(long long)i * n + j] = p;
-      Pm[(long long)j * n + i] = p;
     }
     __syncthreads();
     PHASE_MARK(8);
@@ -1168,15 +1668,16 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
       for (int i = w; i < n; i += kWarps) {
         if (fp32_phase) {
+          const float* P32 = (const float*)Pm;
           float acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
           for (int j = lane; j < n; j += 32) {
             long long e = (long long)i * n + j;
-            float p = (float)Pm[e];
-            acc[0] += p * (float)S[e];
+            float p = P32[e];
+            acc[0] += p * S32[e];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) acc[1 + c] += p * (float)Dm[c * nn + e];
+            for (int c = 0; c < 3; ++c) acc[1 + c] += p * D32[c * nn + e];
 #pragma unroll
-            for (int c = 0; c < 6; ++c) acc[4 + c] += p * (float)Qm[c * nn + e];
+            for (int c = 0; c < 6; ++c) acc[4 + c] += p * Q32[c * nn + e];
           }
 #pragma unroll
           for (int c = 0; c < 10; ++c)
@@ -1226,7 +1727,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     bool stop = false;
     {
       double acc[2] = {0.0, 0.0};
-      for (long long e = threadIdx.x; e < nn; e += blockDim.x) acc[0] += Pm[e] * H0[e];
+      // the band energy only enters the FP64 convergence test
+      if (!fp32_phase)
+        for (long long e = threadIdx.x; e < nn; e += blockDim.x) acc[0] += Pm[e] * H0[e];
       for (int i = threadIdx.x; i < len; i += blockDim.x) {
         double d = xout[i] - xin[i];
         acc[1] += d * d;
@@ -1268,20 +1771,27 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
 #ifdef QCX_SCC_PHASE_TIMING
   if (threadIdx.x == 0 && mol < 4096) g_mol_cycles[mol] = (unsigned long long)(clock64() - _t_start);
 #endif
-  // energy-weighted density W = C f e C^T (FP64 coefficients of the last iteration)
+  // energy-weighted density W = C f e C^T (coefficients of the last iteration)
   int nocc = 0;
   for (int k = 0; k < n; ++k)
     if (focc[k] > 0.0) nocc = k + 1;
-  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-    int i = (int)(e / n), j = (int)(e % n);
-    if (j < i) continue;
-    double w = 0.0;
-    for (int k = 0; k < nocc; ++k) {
-      int c = sh.perm[k];
-      w += focc[k] * eps[k] * JV[(long long)c * np + i] * JV[(long long)c * np + j];
+  if (MIXED && have32) {
+    double* w = sh.mom;
+    for (int k = threadIdx.x; k < nocc; k += blockDim.x) w[k] = focc[k] * eps[k];
+    __syncthreads();
+    dd_density(dm, n, nocc, sh.perm, w, Wm, sh);
+  } else {
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+      int i = (int)(e / n), j = (int)(e % n);
+      if (j < i) continue;
+      double w = 0.0;
+      for (int k = 0; k < nocc; ++k) {
+        int c = sh.perm[k];
+        w += focc[k] * eps[k] * JV[(long long)c * np + i] * JV[(long long)c * np + j];
+      }
+      Wm[(long long)i * n + j] = w;
+      Wm[(long long)j * n + i] = w;
     }
-    Wm[(long long)i * n + j] = w;
-    Wm[(long long)j * n + i] = w;
   }
   // outputs
   for (int a = threadIdx.x; a < nat; a += blockDim.x) bt.qat[md.atom_off + a] = vec[mv.vl.qat + a];
