@@ -36,6 +36,9 @@ namespace qcx {
 #ifndef QCX_REFINE32_PASSES
 #define QCX_REFINE32_PASSES 2
 #endif
+#ifndef QCX_REFINE32_BACKOFF
+#define QCX_REFINE32_BACKOFF 3
+#endif
 #ifndef QCX_REFINE32_KTOL
 #define QCX_REFINE32_KTOL 1e-3
 #endif
@@ -300,6 +303,11 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
   for (int k = 0; k < 5; ++k) en[k] = e[k];
 }
 
+// s != 0 for a rotation sine that is either exactly +0 (a skipped rotation)
+// or nonzero, tested on the bit pattern: an FP64 compare would run at the FP64 rate
+__device__ __forceinline__ bool nonzero(float s) { return __float_as_int(s) != 0; }
+__device__ __forceinline__ bool nonzero(double s) { return __double_as_longlong(s) != 0; }
+
 // ---------------------------------------------------------------------------
 // cyclic parallel Jacobi on the symmetric np x np matrix A (lda = np).
 // Vt (ld = np) holds eigenvectors as rows; with warm = false it starts as the
@@ -335,7 +343,6 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
   using T2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
   int2* pq = (int2*)sh.rp;
   T2* csr = (T2*)sh.rc;
-  const int nblk = half * half;
   // per-thread start of the block items (k1, k2) and of the row items (k, j);
   // items advance by blockDim.x, i.e. by (dk1, dk2) and (dk, dj)
   const int b1 = threadIdx.x / half, b2 = threadIdx.x - b1 * half;
@@ -385,7 +392,7 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
       // block), and the rows p,q of Vt are rotated by R.
       for (int k1 = b1, k2 = b2; k1 < half;) {
         T2 r1 = csr[k1], r2 = csr[k2];
-        if (r1.y != T(0) || r2.y != T(0)) {
+        if (nonzero(r1.y) || nonzero(r2.y)) {
           int2 e1 = pq[k1], e2 = pq[k2];
           T* row_p = A + e1.x * np;
           T* row_q = A + e1.y * np;
@@ -408,7 +415,7 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
       }
       for (int k = v1, j = v2; k < half;) {
         T2 rr = csr[k];
-        if (rr.y != T(0)) {
+        if (nonzero(rr.y)) {
           int2 e = pq[k];
           T vp = Vt[e.x * np + j], vq = Vt[e.y * np + j];
           Vt[e.x * np + j] = rr.x * vp - rr.y * vq;
@@ -541,6 +548,77 @@ __device__ double fermi_warp32(int n, const double* eps, double nel, double kT, 
 }
 
 // ---------------------------------------------------------------------------
+// Solves M x = b for a symmetric positive definite k x k matrix (k <= 32, row
+// major, FP64) with one warp: an FP32 Cholesky factor held one row per lane,
+// then two steps of iterative refinement with FP64 residuals (Wilkinson), which
+// recover the FP64 solution for condition numbers far below 1/eps_FP32^2. The
+// factorisation and triangular solves run on the FP32 pipes; a serial FP64
+// elimination on one warp is latency-bound at the FP64 rate.
+// ---------------------------------------------------------------------------
+// L L^T x = b with the Cholesky factor held one row per lane (row[c] = L[lane][c])
+// and the right-hand side held one element per lane
+template <int NM>
+__device__ __forceinline__ float chol_solve_lane(const float (&row)[NM], float b, int k) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < NM; ++j) {
+    if (j < k) {
+      float yj = __shfl_sync(full, b, j) / __shfl_sync(full, row[j], j);
+      if (lane == j) b = yj;
+      else if (lane > j) b = fmaf(-row[j], yj, b);
+    }
+  }
+#pragma unroll
+  for (int j = NM - 1; j >= 0; --j) {
+    if (j < k) {
+      float t = (lane > j && lane < k) ? row[j] * b : 0.f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(full, t, o);
+      float yj = __shfl_sync(full, b, j), ljj = __shfl_sync(full, row[j], j);
+      if (lane == j) b = (yj - t) / ljj;
+    }
+  }
+  return b;
+}
+
+template <int NM>
+__device__ void spd_solve_warp(const double* M, double* rhs, int k) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  float row[NM];
+#pragma unroll
+  for (int c = 0; c < NM; ++c) row[c] = (lane < k && c < k) ? (float)M[lane * k + c] : 0.f;
+#pragma unroll
+  for (int j = 0; j < NM; ++j) {
+    if (j < k) {
+      float ljj = sqrtf(fmaxf(__shfl_sync(full, row[j], j), 1e-30f));
+      float lj = lane > j ? row[j] / ljj : 0.f;
+      if (lane == j) row[j] = ljj;
+      else if (lane > j) row[j] = lj;
+#pragma unroll
+      for (int c = j + 1; c < NM; ++c) {
+        if (c < k) {
+          float lcj = __shfl_sync(full, lj, c);
+          if (lane >= c) row[c] = fmaf(-lj, lcj, row[c]);
+        }
+      }
+    }
+  }
+  const double bd = lane < k ? rhs[lane] : 0.0;
+  double xd = (double)chol_solve_lane<NM>(row, (float)bd, k);
+  for (int it = 0; it < 2; ++it) {
+    double r = bd;
+    for (int c = 0; c < k; ++c) {
+      double xc = __shfl_sync(full, xd, c);
+      if (lane < k) r -= M[lane * k + c] * xc;
+    }
+    xd += (double)chol_solve_lane<NM>(row, (float)r, k);
+  }
+  if (lane < k) rhs[lane] = xd;
+}
+
+// ---------------------------------------------------------------------------
 // modified Broyden update of x (len) given x_out; it = number of previous updates
 // ---------------------------------------------------------------------------
 __device__ void broyden(const MolView& mv, double* x, const double* xout, int it, double alpha, SccShared& sh) {
@@ -600,7 +678,9 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
     }
   }
   __syncthreads();
-  // solve (w0^2 I + a) gamma = c by Gaussian elimination with partial pivoting (one warp)
+  // solve (w0^2 I + a) gamma = c (symmetric positive definite): one warp, FP32
+  // Cholesky with FP64 refinement; Gaussian elimination with partial pivoting
+  // for histories longer than a warp
   double* Ms = vec + mv.vl.bm;
   double* rhs = Ms + k * k;
   for (int i = threadIdx.x; i < k * k; i += blockDim.x) {
@@ -609,7 +689,9 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
   }
   for (int i = threadIdx.x; i < k; i += blockDim.x) rhs[i] = cvec[i];
   __syncthreads();
-  if (w == 0) {
+  if (k <= 32 && QCX_BROYDEN_WINDOW <= 32) {
+    if (w == 0) spd_solve_warp<(QCX_BROYDEN_WINDOW < 32 ? QCX_BROYDEN_WINDOW : 32)>(Ms, rhs, k);
+  } else if (w == 0) {
     for (int col = 0; col < k; ++col) {
       // pivot search
       double best = -1.0;
@@ -1001,13 +1083,26 @@ __device__ void cta_gemm_dd(int M, int N, int K, const float* Ah, const float* A
 }
 
 // Double-float coefficient rows and the matrices of one molecule's finishing
-// iterations (mixed mode). Planes: V (rows = MOs, ld np), B = V F V^T (ld np),
-// F and S (ld n), T and M scratch (ld n); Kf and dV are FP32 scratch (ld n).
+// iterations (mixed mode). Planes: V (rows = MOs, ld np) and its transpose Vt
+// (ld n, kept in step with V so that the products with V^T read their operand
+// along rows), B = V F V^T (ld np), F and S (ld n), T and M scratch (ld n); Kf
+// and dV are FP32 scratch (ld n).
 struct DDMats {
-  float *Vh, *Vl, *Bh, *Bl, *Fh, *Fl, *Sh, *Sl, *Th, *Tl, *Mh, *Ml, *Kf, *dV;
+  float *Vh, *Vl, *Vth, *Vtl, *Bh, *Bl, *Fh, *Fl, *Sh, *Sl, *Th, *Tl, *Mh, *Ml, *Kf, *dV;
 };
 
-// V <- V + dV (dV FP32, ld n) in double-float
+// Vt = V^T
+__device__ void dd_transpose(const DDMats& d, int n, int np) {
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int k = e / n, j = e - k * n;
+    long long x = (long long)j * np + k;
+    d.Vth[e] = d.Vh[x];
+    d.Vtl[e] = d.Vl[x];
+  }
+  __syncthreads();
+}
+
+// V <- V + dV (dV FP32, ld n) in double-float, and the same into Vt
 __device__ void dd_add_rows(const DDMats& d, int n, int np) {
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int i = e / n, j = e - i * n;
@@ -1016,13 +1111,15 @@ __device__ void dd_add_rows(const DDMats& d, int n, int np) {
     dd_add(h, l, d.dV[e]);
     d.Vh[x] = h;
     d.Vl[x] = l;
+    d.Vth[(long long)j * n + i] = h;
+    d.Vtl[(long long)j * n + i] = l;
   }
   __syncthreads();
 }
 
 // B = V F V^T
 __device__ void dd_rotate_fock(const DDMats& d, int n, int np) {
-  cta_gemm_dd(n, n, n, d.Fh, d.Fl, n, false, d.Vh, d.Vl, np, true, d.Th, d.Tl, nullptr, n);
+  cta_gemm_dd(n, n, n, d.Fh, d.Fl, n, false, d.Vth, d.Vtl, n, false, d.Th, d.Tl, nullptr, n);
   __syncthreads();
   cta_gemm_dd(n, n, n, d.Vh, d.Vl, np, false, d.Th, d.Tl, n, false, d.Bh, d.Bl, nullptr, np);
   __syncthreads();
@@ -1034,7 +1131,7 @@ __device__ void dd_rotate_fock(const DDMats& d, int n, int np) {
 __device__ double dd_orthonormalize(const DDMats& d, int n, int np, int steps, SccShared& sh) {
   double emax = 0.0;
   for (int st = 0; st < steps; ++st) {
-    cta_gemm_dd(n, n, n, d.Sh, d.Sl, n, false, d.Vh, d.Vl, np, true, d.Th, d.Tl, nullptr, n);
+    cta_gemm_dd(n, n, n, d.Sh, d.Sl, n, false, d.Vth, d.Vtl, n, false, d.Th, d.Tl, nullptr, n);
     __syncthreads();
     cta_gemm_dd(n, n, n, d.Vh, d.Vl, np, false, d.Th, d.Tl, n, false, d.Mh, d.Ml, nullptr, n);
     __syncthreads();
@@ -1151,7 +1248,7 @@ constexpr double kMixedSwitch = QCX_MIXED_SWITCH;
 
 // Optional per-phase cycle counters (diagnostic builds only: -DQCX_SCC_PHASE_TIMING).
 #ifdef QCX_SCC_PHASE_TIMING
-__device__ unsigned long long g_phase_cycles[16];
+__device__ unsigned long long g_phase_cycles[24];
 __device__ unsigned long long g_mol_cycles[4096];
 __device__ unsigned long long g_counts[8];  // refine64 ok, jacobi64 fallbacks
 #define PHASE_BEGIN() long long _pt = clock64()
@@ -1324,6 +1421,8 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   DDMats dm;
   dm.Vh = (float*)JV;
   dm.Vl = dm.Vh + (long long)np * np;
+  dm.Vth = Q32;  // the FP32 quadrupoles are not needed after the FP32 iterations
+  dm.Vtl = dm.Vth + nn;
   dm.Bh = (float*)JA;
   dm.Bl = dm.Bh + (long long)np * np;
   dm.Fh = (float*)F;
@@ -1359,6 +1458,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   int bro_it = 0;       // Broyden updates since the last (re)start of the mixer
   double best32 = 1e300;  // best residual seen in the FP32 phase
   int stall32 = 0;
+  int backoff32 = 0;    // FP32 iterations left before the next refinement attempt
   int n64 = 0;          // FP64 iterations done
   PHASE_BEGIN();
 #ifdef QCX_SCC_PHASE_TIMING
@@ -1440,9 +1540,15 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       }
       __syncthreads();
       PHASE_MARK(2);
-      bool ok32 = have32 && QCX_REFINE32_PASSES > 0 &&
+      // a failed refinement costs about a Jacobi sweep, so after a failure the
+      // next QCX_REFINE32_BACKOFF iterations go straight to the sweep
+      bool try32 = have32 && QCX_REFINE32_PASSES > 0 && backoff32 == 0;
+      if (backoff32 > 0) --backoff32;
+      bool ok32 = try32 &&
                   refine<float>(JA32, JV32, (const float*)F, S32, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, QCX_REFINE32_KTOL,
                                 QCX_REFINE32_PASSES, 1e-3, sh, efermi, 25.0 * md.kT);
+      PHASE_MARK(16);
+      if (try32 && !ok32) backoff32 = QCX_REFINE32_BACKOFF;
       if (!ok32) jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? QCX_JAC32_WARM_SWEEPS : 30);
 #ifdef QCX_SCC_PHASE_TIMING
       if (threadIdx.x == 0) atomicAdd(&g_phase_cycles[ok32 ? 13 : 14], 1ull);
@@ -1478,6 +1584,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         }
         for (long long e = threadIdx.x; e < nn; e += blockDim.x) dm.Sl[e] = __double2float_rn(S[e] - (double)S32[e]);
         __syncthreads();
+        dd_transpose(dm, n, np);
         dd_orthonormalize(dm, n, np, 2, sh);
       }
       dd_rotate_fock(dm, n, np);
@@ -1520,6 +1627,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         __syncthreads();
         for (long long e = threadIdx.x; e < np2; e += blockDim.x) dd_split(tD[e], dm.Vh[e], dm.Vl[e]);
         __syncthreads();
+        dd_transpose(dm, n, np);
       }
       PHASE_MARK(5);
       have64 = true;
@@ -1831,9 +1939,9 @@ extern "C" int qcx_debug_mol_cycles(unsigned long long* out, int n) {
                  cudaSuccess ? 0 : -1;
 }
 extern "C" int qcx_debug_phase_cycles(unsigned long long* out, int reset) {
-  if (cudaMemcpyFromSymbol(out, qcx::g_phase_cycles, sizeof(unsigned long long) * 16) != cudaSuccess) return -1;
+  if (cudaMemcpyFromSymbol(out, qcx::g_phase_cycles, sizeof(unsigned long long) * 24) != cudaSuccess) return -1;
   if (reset) {
-    unsigned long long z[16] = {0};
+    unsigned long long z[24] = {0};
     cudaMemcpyToSymbol(qcx::g_phase_cycles, z, sizeof(z));
   }
   return 0;
