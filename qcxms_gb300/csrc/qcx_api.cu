@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -15,6 +16,11 @@
 #include "qcx_kernels.h"
 
 using namespace qcx;
+
+// number of molecule groups whose SCC and gradient kernels run on separate streams
+#ifndef QCX_MOL_GROUPS
+#define QCX_MOL_GROUPS 8
+#endif
 
 namespace {
 
@@ -106,21 +112,63 @@ struct qcx_batch {
   size_t bytes = 0;
   int precision = 0;
   int step_launches = 0;
+  // Molecule groups: contiguous chunks of the size order (largest first).
+  // After the batch-wide coordination numbers and integrals, each group runs
+  // its SCC and gradient kernels on its own stream, so that the gradients of
+  // groups that converge early overlap the SCC of the slowest molecules.
+  int ngroup = 1;
+  std::vector<int> g_start, g_count;      // range of each group in the size order
+  std::vector<int> g_pair_start;          // first pair of each group in d_gpairs
+  std::vector<std::array<int, 10>> g_pair_off;  // class offsets inside the group
+  ShellPair* d_gpairs = nullptr;          // shell pairs ordered by group, then class
+  std::vector<cudaStream_t> g_stream;     // g_stream[0] is the batch stream
+  std::vector<cudaEvent_t> g_join;
+  cudaEvent_t g_fork = nullptr;
 };
 
 namespace {
 
-// returns the number of kernels launched
+// the batch restricted to molecule group g (SCC and gradient kernels)
+DevBatch group_dev(const qcx_batch* b, int g) {
+  DevBatch d = b->dev;
+  d.nmol = b->g_count[g];
+  d.order = b->dev.order + b->g_start[g];
+  d.pairs = b->d_gpairs + b->g_pair_start[g];
+  for (int c = 0; c < 10; ++c) d.pair_off[c] = b->g_pair_off[g][c];
+  d.npair = d.pair_off[9];
+  return d;
+}
+
+// Enqueues one energy + gradient evaluation; returns the number of kernels
+// launched, or -1 on an error in the stream bookkeeping.
 int enqueue_egrad(qcx_batch* b) {
   const DevBatch& d = b->dev;
   int n = 0;
   launch_cn(d, b->stream);
   n += 1 + launch_integrals(d, b->stream);
-  launch_scc(d, b->precision, b->stream);
   launch_zero_grad(d, b->stream);
-  n += 2 + launch_grad_pairs(d, b->stream);
-  launch_grad_atoms(d, b->stream);
-  return n + 1;
+  ++n;
+  if (b->ngroup == 1) {
+    launch_scc(d, b->precision, b->stream);
+    n += 1 + launch_grad_pairs(d, b->stream);
+    launch_grad_atoms(d, b->stream);
+    return n + 1;
+  }
+  if (cudaEventRecord(b->g_fork, b->stream) != cudaSuccess) return -1;
+  for (int g = 0; g < b->ngroup; ++g) {
+    cudaStream_t st = b->g_stream[g];
+    if (g > 0 && cudaStreamWaitEvent(st, b->g_fork, 0) != cudaSuccess) return -1;
+    DevBatch gd = group_dev(b, g);
+    launch_scc(gd, b->precision, st);
+    n += 1 + launch_grad_pairs(gd, st);
+    launch_grad_atoms(gd, st);
+    ++n;
+    if (g > 0) {
+      if (cudaEventRecord(b->g_join[g], st) != cudaSuccess) return -1;
+      if (cudaStreamWaitEvent(b->stream, b->g_join[g], 0) != cudaSuccess) return -1;
+    }
+  }
+  return n;
 }
 constexpr int kEgradPhases = 6;
 
@@ -134,6 +182,12 @@ void free_batch(qcx_batch* b) {
                   b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps, b->d_order};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (b->d_gpairs) cudaFree(b->d_gpairs);
+  for (size_t g = 1; g < b->g_stream.size(); ++g)
+    if (b->g_stream[g]) cudaStreamDestroy(b->g_stream[g]);
+  for (cudaEvent_t e : b->g_join)
+    if (e) cudaEventDestroy(e);
+  if (b->g_fork) cudaEventDestroy(b->g_fork);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -225,6 +279,42 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
     for (int m = 0; m < nmol; ++m) order[m] = m;
     std::stable_sort(order.begin(), order.end(), [b](int x, int y) { return b->mol[x].nao > b->mol[y].nao; });
     CK(cudaMemcpy(b->d_order, order.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
+    // molecule groups (contiguous in the size order) and their shell pairs,
+    // ordered by group and then by angular-momentum class
+    const int G = nmol < QCX_MOL_GROUPS ? nmol : QCX_MOL_GROUPS;
+    b->ngroup = G;
+    std::vector<int> sh_l(sh_atom.size());
+    for (size_t sh = 0; sh < sh_atom.size(); ++sh) sh_l[sh] = qcx_sh_l[b->Z[sh_atom[sh]]][sh_k[sh]];
+    std::vector<ShellPair> gp;
+    gp.reserve(pairs.size());
+    for (int g = 0; g < G; ++g) {
+      const int k0 = (int)((long long)g * nmol / G), k1 = (int)((long long)(g + 1) * nmol / G);
+      b->g_start.push_back(k0);
+      b->g_count.push_back(k1 - k0);
+      b->g_pair_start.push_back((int)gp.size());
+      std::array<int, 10> off{};
+      for (int c = 0; c < 9; ++c) {
+        off[c] = (int)gp.size() - b->g_pair_start[g];
+        for (int k = k0; k < k1; ++k) {
+          const MolDesc& md = b->mol[order[k]];
+          for (int s = md.sh_off; s < md.sh_off + md.nsh; ++s)
+            for (int t = md.sh_off; t < md.sh_off + md.nsh; ++t)
+              if (sh_l[s] * 3 + sh_l[t] == c) gp.push_back({s, t});
+        }
+      }
+      off[9] = (int)gp.size() - b->g_pair_start[g];
+      b->g_pair_off.push_back(off);
+    }
+    if (dalloc(&b->d_gpairs, gp.size())) return -1;
+    CK(cudaMemcpy(b->d_gpairs, gp.data(), sizeof(ShellPair) * gp.size(), cudaMemcpyHostToDevice));
+    b->g_stream.assign(G, nullptr);
+    b->g_join.assign(G, nullptr);
+    b->g_stream[0] = b->stream;
+    for (int g = 1; g < G; ++g) {
+      CK(cudaStreamCreateWithFlags(&b->g_stream[g], cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&b->g_join[g], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&b->g_fork, cudaEventDisableTiming));
   }
   b->bytes = sizeof(double) * ((size_t)mat_off + (size_t)vec_off);
   CK(cudaMemcpy(b->d_prm, &hp, sizeof(Params), cudaMemcpyHostToDevice));
@@ -378,7 +468,12 @@ int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, cons
 
 int qcx_batch_egrad(qcx_batch* b) {
   if (!b) return -1;
-  b->launches = enqueue_egrad(b);
+  int n = enqueue_egrad(b);
+  if (n < 0) {
+    set_error("qcx_batch_egrad: stream synchronisation failed");
+    return -1;
+  }
+  b->launches = n;
   return check_launch();
 }
 
@@ -393,8 +488,15 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
     }
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     launch_leapfrog(b->dev, tstep, b->stream);
-    b->step_launches = 1 + enqueue_egrad(b);
-    CK(cudaStreamEndCapture(b->stream, &b->graph));
+    int n = enqueue_egrad(b);
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &b->graph);
+    if (n < 0 || ce != cudaSuccess) {
+      if (ce == cudaSuccess && b->graph) cudaGraphDestroy(b->graph);
+      b->graph = nullptr;
+      set_error(std::string("qcx_batch_step: graph capture failed: ") + cudaGetErrorString(ce));
+      return -1;
+    }
+    b->step_launches = 1 + n;
     CK(cudaGraphInstantiate(&b->graph_exec, b->graph, 0));
     b->graph_tstep = tstep;
   }

@@ -20,7 +20,9 @@
 #define QCX_BROYDEN_ALPHA 0.25
 #define QCX_BROYDEN_W0 0.01
 /* Broyden history: the last QCX_BROYDEN_WINDOW iterations */
+#ifndef QCX_BROYDEN_WINDOW
 #define QCX_BROYDEN_WINDOW 24
+#endif
 
 /* Fermi level bisection: fixed iteration count for reproducibility */
 #define QCX_FERMI_ITERS 200

@@ -37,13 +37,22 @@ namespace qcx {
 #define QCX_REFINE32_PASSES 2
 #endif
 #ifndef QCX_REFINE32_BACKOFF
-#define QCX_REFINE32_BACKOFF 3
+#define QCX_REFINE32_BACKOFF 6
 #endif
 #ifndef QCX_REFINE32_KTOL
 #define QCX_REFINE32_KTOL 1e-3
 #endif
 // rounds of exact rotations on the pairs that first-order refinement cannot
 // handle, before the refinement gives up and a Jacobi sweep takes over
+// items per batch of the Jacobi update loops, and whether the sweep is a
+// separate function (its own register allocation; the caller saves its live
+// registers around the call, once per sweep)
+#ifndef QCX_JAC_UNROLL
+#define QCX_JAC_UNROLL 4
+#endif
+#ifndef QCX_JAC_INLINE
+#define QCX_JAC_INLINE __noinline__
+#endif
 #ifndef QCX_HARD_ROUNDS
 #define QCX_HARD_ROUNDS 6
 #endif
@@ -317,7 +326,7 @@ __device__ __forceinline__ bool nonzero(double s) { return __double_as_longlong(
 // Returns the number of sweeps, or -1 if max_sweeps were not enough.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& sh, int max_sweeps) {
+__device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& sh, int max_sweeps) {
   const int np = n + (n & 1);
   const int half = np / 2;
   const int m = np - 1;
@@ -390,42 +399,97 @@ __device__ int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& s
       // One fused phase per round: every 2x2 block A[{p1,q1}][{p2,q2}] of a pair
       // of pairs becomes R1 * block * R2^T (each element belongs to exactly one
       // block), and the rows p,q of Vt are rotated by R.
+      // Items are taken U at a time with all their shared-memory loads issued
+      // before any use, so that the latencies overlap (a round is otherwise
+      // bound by one dependent load chain per item).
+      constexpr int U = sizeof(T) == 4 ? QCX_JAC_UNROLL : 2;
       for (int k1 = b1, k2 = b2; k1 < half;) {
-        T2 r1 = csr[k1], r2 = csr[k2];
-        if (nonzero(r1.y) || nonzero(r2.y)) {
-          int2 e1 = pq[k1], e2 = pq[k2];
-          T* row_p = A + e1.x * np;
-          T* row_q = A + e1.y * np;
-          T a = row_p[e2.x], b = row_p[e2.y], c = row_q[e2.x], d = row_q[e2.y];
-          // rows: R1 = [[c1,-s1],[s1,c1]]
-          T ra = r1.x * a - r1.y * c, rb = r1.x * b - r1.y * d;
-          T rc = r1.y * a + r1.x * c, rd = r1.y * b + r1.x * d;
-          // columns: multiply by R2^T
-          row_p[e2.x] = r2.x * ra - r2.y * rb;
-          row_p[e2.y] = r2.y * ra + r2.x * rb;
-          row_q[e2.x] = r2.x * rc - r2.y * rd;
-          row_q[e2.y] = r2.y * rc + r2.x * rd;
+        int ka[U], kb[U];
+        bool ok[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          ok[u] = k1 < half;
+          ka[u] = ok[u] ? k1 : 0;
+          kb[u] = k2;
+          k1 += db1;
+          k2 += db2;
+          if (k2 >= half) {
+            k2 -= half;
+            ++k1;
+          }
         }
-        k1 += db1;
-        k2 += db2;
-        if (k2 >= half) {
-          k2 -= half;
-          ++k1;
+        T2 r1[U], r2[U];
+        int2 e1[U], e2[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          r1[u] = csr[ka[u]];
+          r2[u] = csr[kb[u]];
+          e1[u] = pq[ka[u]];
+          e2[u] = pq[kb[u]];
+        }
+        T a[U], b[U], c[U], d[U];
+        bool act[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          act[u] = ok[u] && (nonzero(r1[u].y) || nonzero(r2[u].y));
+          if (act[u]) {
+            a[u] = A[e1[u].x * np + e2[u].x];
+            b[u] = A[e1[u].x * np + e2[u].y];
+            c[u] = A[e1[u].y * np + e2[u].x];
+            d[u] = A[e1[u].y * np + e2[u].y];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (act[u]) {
+            // rows: R1 = [[c1,-s1],[s1,c1]]; columns: multiply by R2^T
+            T ra = r1[u].x * a[u] - r1[u].y * c[u], rb = r1[u].x * b[u] - r1[u].y * d[u];
+            T rc = r1[u].y * a[u] + r1[u].x * c[u], rd = r1[u].y * b[u] + r1[u].x * d[u];
+            A[e1[u].x * np + e2[u].x] = r2[u].x * ra - r2[u].y * rb;
+            A[e1[u].x * np + e2[u].y] = r2[u].y * ra + r2[u].x * rb;
+            A[e1[u].y * np + e2[u].x] = r2[u].x * rc - r2[u].y * rd;
+            A[e1[u].y * np + e2[u].y] = r2[u].y * rc + r2[u].x * rd;
+          }
         }
       }
       for (int k = v1, j = v2; k < half;) {
-        T2 rr = csr[k];
-        if (nonzero(rr.y)) {
-          int2 e = pq[k];
-          T vp = Vt[e.x * np + j], vq = Vt[e.y * np + j];
-          Vt[e.x * np + j] = rr.x * vp - rr.y * vq;
-          Vt[e.y * np + j] = rr.y * vp + rr.x * vq;
+        int kk[U], jj[U];
+        bool ok[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          ok[u] = k < half;
+          kk[u] = ok[u] ? k : 0;
+          jj[u] = j;
+          k += dv1;
+          j += dv2;
+          if (j >= np) {
+            j -= np;
+            ++k;
+          }
         }
-        k += dv1;
-        j += dv2;
-        if (j >= np) {
-          j -= np;
-          ++k;
+        T2 rr[U];
+        int2 e[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          rr[u] = csr[kk[u]];
+          e[u] = pq[kk[u]];
+        }
+        T vp[U], vq[U];
+        bool act[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          act[u] = ok[u] && nonzero(rr[u].y);
+          if (act[u]) {
+            vp[u] = Vt[e[u].x * np + jj[u]];
+            vq[u] = Vt[e[u].y * np + jj[u]];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (act[u]) {
+            Vt[e[u].x * np + jj[u]] = rr[u].x * vp[u] - rr[u].y * vq[u];
+            Vt[e[u].y * np + jj[u]] = rr[u].y * vp[u] + rr[u].x * vq[u];
+          }
         }
       }
       __syncthreads();
@@ -1480,19 +1544,50 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         float* vs32 = (float*)sh.mom;
         float* vd32 = vs32 + nsh;
         float* vq32 = vd32 + 3 * nat;
-        for (int i = threadIdx.x; i < nsh + 9 * nat; i += blockDim.x)
-          vs32[i] = (float)(i < nsh ? vsh[i] : (i < nsh + 3 * nat ? vdp[i - nsh] : vqp[i - nsh - 3 * nat]));
+        float* r32 = vq32 + 6 * nat;  // atom positions (nsh + 12 nat <= 20 n floats)
+        for (int i = threadIdx.x; i < nsh + 12 * nat; i += blockDim.x) {
+          double v;
+          if (i < nsh) v = vsh[i];
+          else if (i < nsh + 3 * nat) v = vdp[i - nsh];
+          else if (i < nsh + 9 * nat) v = vqp[i - nsh - 3 * nat];
+          else v = mv.xyz[i - nsh - 9 * nat];
+          vs32[i] = (float)v;
+        }
         __syncthreads();
         float* F32 = (float*)F;
+        // The multipole operators are centred on the bra atom, so the (j,i)
+        // elements follow from the (i,j) ones by shifting the centre by
+        // d = R_A - R_B: D_ji = D_ij + d S_ij and, for the second moments,
+        // M_ji = M_ij + d D_ij^T + D_ij d^T + d d^T S_ij (then made traceless).
+        // This reads every matrix along rows only.
         for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
           int i = (int)(e / n), j = (int)(e % n);
           int A = sh.ao_at[i], B = sh.ao_at[j];
-          long long ji = (long long)j * n + i;
-          float f = H032[e] - 0.5f * S32[e] * (vs32[sh.ao_sh[i]] + vs32[sh.ao_sh[j]]);
+          const float s = S32[e];
+          float f = H032[e] - 0.5f * s * (vs32[sh.ao_sh[i]] + vs32[sh.ao_sh[j]]);
+          float d[3], D[3];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) f -= 0.5f * (vd32[3 * A + c] * D32[c * nn + e] + vd32[3 * B + c] * D32[c * nn + ji]);
+          for (int c = 0; c < 3; ++c) {
+            d[c] = r32[3 * A + c] - r32[3 * B + c];
+            D[c] = D32[c * nn + e];
+            f -= 0.5f * (vd32[3 * A + c] * D[c] + vd32[3 * B + c] * (D[c] + d[c] * s));
+          }
+          const float dD = d[0] * D[0] + d[1] * D[1] + d[2] * D[2];
+          const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
 #pragma unroll
-          for (int c = 0; c < 6; ++c) f -= 0.5f * (vq32[6 * A + c] * Q32[c * nn + e] + vq32[6 * B + c] * Q32[c * nn + ji]);
+          for (int c = 0; c < 3; ++c) {
+            float q = Q32[c * nn + e];
+            float qji = q + 3.f * d[c] * D[c] + 1.5f * d[c] * d[c] * s - dD - 0.5f * dd * s;
+            f -= 0.5f * (vq32[6 * A + c] * q + vq32[6 * B + c] * qji);
+          }
+          // off-diagonal components xy, xz, yz
+#pragma unroll
+          for (int c = 3; c < 6; ++c) {
+            const int a = c == 5 ? 1 : 0, b = c == 3 ? 1 : 2;
+            float q = Q32[c * nn + e];
+            float qji = q + 1.5f * (d[a] * D[b] + d[b] * D[a] + d[a] * d[b] * s);
+            f -= 0.5f * (vq32[6 * A + c] * q + vq32[6 * B + c] * qji);
+          }
           F32[e] = f;
         }
       } else {
@@ -1525,7 +1620,15 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         cta_gemm<float, float, float, float>(n, n, n, X32, n, true, T32, n, false, JA32, np);
         __syncthreads();
       } else {
-        cta_gemm<float, float, float, float>(n, n, n, (const float*)F, n, false, JV32, np, true, T32, n);
+        // B = V F V^T with V^T copied out first (the FP64 X slot is free in
+        // the FP32 iterations), so that both products read along rows
+        float* Vt32 = (float*)X;
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+          int k = e / n, j = e - k * n;
+          Vt32[e] = JV32[j * np + k];
+        }
+        __syncthreads();
+        cta_gemm<float, float, float, float>(n, n, n, (const float*)F, n, false, Vt32, n, false, T32, n);
         __syncthreads();
         cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, T32, n, false, JA32, np);
         __syncthreads();
@@ -1562,10 +1665,13 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         have32 = true;
       }
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        // a non-finite eigenvalue ranks as +inf, so that the ranks stay a permutation
         float di = JA32[i * np + i];
+        if (!(di <= FLT_MAX)) di = INFINITY;
         int rank = 0;
         for (int j = 0; j < n; ++j) {
           float dj = JA32[j * np + j];
+          if (!(dj <= FLT_MAX)) dj = INFINITY;
           rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
         }
         sh.perm[rank] = i;
@@ -1633,9 +1739,11 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       have64 = true;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double di = lam[i];
+        if (!(di <= DBL_MAX)) di = INFINITY;
         int rank = 0;
         for (int j = 0; j < n; ++j) {
           double dj = lam[j];
+          if (!(dj <= DBL_MAX)) dj = INFINITY;
           rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
         }
         sh.perm[rank] = i;
@@ -1709,9 +1817,11 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       have64 = true;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double di = JA[i * np + i];
+        if (!(di <= DBL_MAX)) di = INFINITY;
         int rank = 0;
         for (int j = 0; j < n; ++j) {
           double dj = JA[j * np + j];
+          if (!(dj <= DBL_MAX)) dj = INFINITY;
           rank += (dj < di || (dj == di && j < i)) ? 1 : 0;
         }
         sh.perm[rank] = i;
@@ -1742,18 +1852,18 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       float* f32 = (float*)sh.rc;  // np floats; the rotation scratch is free after the eigensolve
       for (int k = threadIdx.x; k < nocc; k += blockDim.x) f32[k] = (float)focc[k];
       __syncthreads();
+      // P = G^T V_occ with G_k = f_k v_k (rows in occupation order, in the T and C slots)
       float* P32 = (float*)Pm;
-      for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-        int i = (int)(e / n), j = (int)(e % n);
-        if (j < i) continue;
-        float pf = 0.0f;
-        for (int k = 0; k < nocc; ++k) {
-          int c = sh.perm[k];
-          pf += f32[k] * JV32[(long long)c * np + i] * JV32[(long long)c * np + j];
-        }
-        P32[(long long)i * n + j] = pf;
-        P32[(long long)j * n + i] = pf;
+      float* G32 = T32;
+      float* Vo32 = (float*)C;
+      for (int e = threadIdx.x; e < nocc * n; e += blockDim.x) {
+        int k = e / n, j = e - k * n;
+        float v = JV32[sh.perm[k] * np + j];
+        G32[e] = f32[k] * v;
+        Vo32[e] = v;
       }
+      __syncthreads();
+      cta_gemm<float, float, float, float>(n, n, nocc, G32, n, true, Vo32, n, false, P32, n);
     } else if (MIXED && have32) {
       dd_density(dm, n, nocc, sh.perm, focc, Pm, sh);
     } else {
