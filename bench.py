@@ -121,11 +121,13 @@ def scc_flops(nao, iters):
     return float(np.sum(iters * 11.0 * n3 + 2.0 * n3))
 
 
-def measured_fp64_peak(torch):
-    """Dense FP64 throughput of this GPU (cuBLAS DGEMM, best of 5), TFLOP/s."""
+def measured_peak(torch, dtype):
+    """Dense throughput of this GPU on CUDA cores (cuBLAS GEMM 4096^3 in dtype,
+    TF32 tensor cores off for FP32; best of 5), TFLOP/s."""
     n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
     for _ in range(2):
         torch.matmul(a, b)
     torch.cuda.synchronize()
@@ -308,7 +310,10 @@ def run_gpu(args):
     act, _ = b.progress()
     flops = scc_flops(nao[act > 0], iters[act > 0])
     achieved = flops / (scc_ms * 1e-3) / 1e12
-    peak64 = measured_fp64_peak(torch)
+    # The mixed kernel runs its O(n^3) work on the FP32 pipes (FP32 iterations and
+    # the double-float finishing iterations); the FP64 kernel on the FP64 pipe.
+    mixed = args.precision == "mixed"
+    peak = measured_peak(torch, torch.float32 if mixed else torch.float64)
     plain = plain_fp64_single(qg, constants) if rank == 0 and not args.no_plain else None
 
     if rank == 0:
@@ -334,11 +339,11 @@ def run_gpu(args):
             "e2e": {"value": e2e, "unit": "trajectory-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                         "frac": achieved / peak64, "traffic": SCC_DRAM_BYTES_PER_MOLECULE * b.nmol, "kernel": "k_scc",
-                         "peak_source": "measured in this run: cuBLAS FP64 GEMM 4096^3 (MEASURED_PEAKS.json holds "
-                                        "only HBM and bf16 peaks)",
-                         "flops_convention": "per molecule: iters*(9n^3+2n^3)+2n^3"},
+            "roofline": {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": SCC_DRAM_BYTES_PER_MOLECULE * b.nmol, "kernel": "k_scc",
+                         "peak_source": "measured in this run: cuBLAS %s GEMM 4096^3 on CUDA cores (MEASURED_PEAKS.json "
+                                        "holds only HBM and bf16 tensor peaks)" % ("FP32" if mixed else "FP64"),
+                         "flops_convention": "algorithmic, per molecule: iters*(9n^3+2n^3)+2n^3"},
             "kernel_ms": breakdown,
             "clocks": clk.summary(),
         }

@@ -48,7 +48,7 @@ namespace qcx {
 // separate function (its own register allocation; the caller saves its live
 // registers around the call, once per sweep)
 #ifndef QCX_JAC_UNROLL
-#define QCX_JAC_UNROLL 4
+#define QCX_JAC_UNROLL 1
 #endif
 #ifndef QCX_JAC_INLINE
 #define QCX_JAC_INLINE __noinline__
@@ -310,6 +310,94 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
   }
   cta_sum<5>(e, red);
   for (int k = 0; k < 5; ++k) en[k] = e[k];
+}
+
+// ---------------------------------------------------------------------------
+// FP32 potentials for the FP32 iterations: the potential terms of
+// potentials() (no energies, which only the FP64 convergence test uses), in
+// FP32, written to shared memory for the FP32 Fock build, with shared-memory
+// atomics for the pair sums. Layout of v32: shell potentials [nsh], dipole
+// [3 nat] and quadrupole [6 nat] potentials, atom positions [3 nat], then
+// scratch (dipoles, quadrupoles, charges, zeta, dzeta, atom potentials).
+// Returns false, writing nothing, when the scratch (nsh + 25 nat floats)
+// exceeds the 20 n floats available.
+// ---------------------------------------------------------------------------
+__device__ bool potentials32(const MolView& mv, const double* x, float* v32, int n) {
+  const Params& P = *mv.bt->prm;
+  const int nat = mv.md.nat, nsh = mv.md.nsh;
+  if (nsh + 25 * nat > 20 * n) return false;
+  float* vs32 = v32;
+  float* vd32 = vs32 + nsh;
+  float* vq32 = vd32 + 3 * nat;
+  float* r32 = vq32 + 6 * nat;
+  float* m32 = r32 + 3 * nat;
+  float* t32 = m32 + 3 * nat;
+  float* q32 = t32 + 6 * nat;
+  float* z32 = q32 + nat;
+  float* dz32 = z32 + nat;
+  float* va32 = dz32 + nat;
+  const double* qsh = x;
+  const double* dp = x + nsh;
+  const double* qp = x + nsh + 3 * nat;
+  const double* vec = mv.vec;
+  const double* gam = vec + mv.vl.gam;
+  const double* c6g = vec + mv.vl.c6g;
+  const double* f3m = vec + mv.vl.f3;
+  const double* f5m = vec + mv.vl.f5;
+  const int* sh_k = mv.bt->sh_k + mv.md.sh_off;
+  const int* sh_atom = mv.bt->sh_atom + mv.md.sh_off;
+  const int aoff = mv.md.atom_off;
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+    double q = 0.0;
+    for (int t = 0; t < nsh; ++t)
+      if (sh_atom[t] - aoff == a) q += qsh[t];
+    double zt, dzt;
+    d4_zeta(P, mv.Z[a], q, zt, dzt);
+    q32[a] = (float)q;
+    z32[a] = (float)zt;
+    dz32[a] = (float)dzt;
+    va32[a] = 0.f;
+    const float fd = (float)P.aes_dk[mv.Z[a]], fq = (float)P.aes_qk[mv.Z[a]];
+    for (int k = 0; k < 3; ++k) {
+      r32[3 * a + k] = (float)mv.xyz[3 * a + k];
+      m32[3 * a + k] = (float)dp[3 * a + k];
+      vd32[3 * a + k] = 2.f * fd * m32[3 * a + k];
+    }
+    for (int c = 0; c < 6; ++c) {
+      t32[6 * a + c] = (float)qp[6 * a + c];
+      vq32[6 * a + c] = (c < 3 ? 2.f : 4.f) * fq * t32[6 * a + c];
+    }
+  }
+  __syncthreads();
+  // pair terms (atom pairs b-major, so that consecutive threads add into different atoms)
+  for (int idx = threadIdx.x; idx < nat * nat; idx += blockDim.x) {
+    int b = idx / nat, a = idx - b * nat;
+    if (b == a) continue;
+    float r[3] = {r32[3 * a] - r32[3 * b], r32[3 * a + 1] - r32[3 * b + 1], r32[3 * a + 2] - r32[3 * b + 2]};
+    float r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    float f3 = (float)f3m[a * nat + b], f5 = (float)f5m[a * nat + b], cg = (float)c6g[a * nat + b];
+    const float* mb = m32 + 3 * b;
+    const float* tb = t32 + 6 * b;
+    float mbr = mb[0] * r[0] + mb[1] * r[1] + mb[2] * r[2];
+    float rr[6] = {r[0] * r[0], r[1] * r[1], r[2] * r[2], 2.f * r[0] * r[1], 2.f * r[0] * r[2], 2.f * r[1] * r[2]};
+    float rtb = 0.f;
+    for (int c = 0; c < 6; ++c) rtb += tb[c] * rr[c];
+    const float qb = q32[b];
+    atomicAdd(&va32[a], f3 * mbr + f5 * rtb - dz32[a] * z32[b] * cg);
+    for (int k = 0; k < 3; ++k) atomicAdd(&vd32[3 * a + k], -f3 * qb * r[k] + f5 * (mb[k] * r2 - 3.f * mbr * r[k]));
+    for (int c = 0; c < 6; ++c) atomicAdd(&vq32[6 * a + c], f5 * qb * rr[c]);
+  }
+  __syncthreads();
+  // shell-resolved isotropic electrostatics and third order
+  for (int t = threadIdx.x; t < nsh; t += blockDim.x) {
+    double v = 0.0;
+    for (int u = 0; u < nsh; ++u) v += gam[t * nsh + u] * qsh[u];
+    int a = sh_atom[t] - aoff;
+    double g3 = P.gamma3[mv.Z[a]][sh_k[t]];
+    vs32[t] = (float)(v + g3 * qsh[t] * qsh[t]) + va32[a];
+  }
+  __syncthreads();
+  return true;
 }
 
 // s != 0 for a rotation sine that is either exactly +0 (a skipped rotation)
@@ -1530,7 +1618,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
 #endif
   for (it = 1; it <= bt.max_iter; ++it) {
     PHASE_MARK(15);
-    potentials(mv, xin, en, sh.red);
+    // FP32 iterations take their potentials in FP32 straight into shared memory
+    const bool pot32 = fp32_phase && potentials32(mv, xin, (float*)sh.mom, n);
+    if (!pot32) potentials(mv, xin, en, sh.red);
     PHASE_MARK(0);
     // Fock matrix
     {
@@ -1545,15 +1635,17 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         float* vd32 = vs32 + nsh;
         float* vq32 = vd32 + 3 * nat;
         float* r32 = vq32 + 6 * nat;  // atom positions (nsh + 12 nat <= 20 n floats)
-        for (int i = threadIdx.x; i < nsh + 12 * nat; i += blockDim.x) {
-          double v;
-          if (i < nsh) v = vsh[i];
-          else if (i < nsh + 3 * nat) v = vdp[i - nsh];
-          else if (i < nsh + 9 * nat) v = vqp[i - nsh - 3 * nat];
-          else v = mv.xyz[i - nsh - 9 * nat];
-          vs32[i] = (float)v;
+        if (!pot32) {
+          for (int i = threadIdx.x; i < nsh + 12 * nat; i += blockDim.x) {
+            double v;
+            if (i < nsh) v = vsh[i];
+            else if (i < nsh + 3 * nat) v = vdp[i - nsh];
+            else if (i < nsh + 9 * nat) v = vqp[i - nsh - 3 * nat];
+            else v = mv.xyz[i - nsh - 9 * nat];
+            vs32[i] = (float)v;
+          }
+          __syncthreads();
         }
-        __syncthreads();
         float* F32 = (float*)F;
         // The multipole operators are centred on the bra atom, so the (j,i)
         // elements follow from the (i,j) ones by shifting the centre by
