@@ -30,9 +30,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "GFN2-xTB trajectory-steps/s"
-# DRAM bytes of one k_scc launch per molecule, from an ncu capture of 16 molecules
-# (6.65 MB; profiles/k_scc_mixed_16traj_full.md); a launch touches each molecule's own data only.
-SCC_DRAM_BYTES_PER_MOLECULE = 6.65e6 / 16
+# DRAM bytes of one k_scc launch per molecule, from an ncu capture of a launch over 8
+# molecules (5.37 MB; profiles/k_scc_mixed_64traj_group_full.md); a launch touches each
+# molecule's own data only.
+SCC_DRAM_BYTES_PER_MOLECULE = 5.37e6 / 8
 NTRAJ, NMIN, NMAX = 256, 5, 40
 DT_FS = 0.5
 ETEMP = 300.0

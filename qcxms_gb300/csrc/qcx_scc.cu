@@ -53,6 +53,10 @@ namespace qcx {
 #ifndef QCX_JAC_INLINE
 #define QCX_JAC_INLINE __noinline__
 #endif
+// rounds of the Jacobi sweep with compacted lists of active rotations
+#ifndef QCX_JAC_COMPACT
+#define QCX_JAC_COMPACT 1
+#endif
 #ifndef QCX_HARD_ROUNDS
 #define QCX_HARD_ROUNDS 6
 #endif
@@ -448,6 +452,116 @@ __device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double relto
   const int dv1 = blockDim.x / np, dv2 = blockDim.x - dv1 * np;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     T offmax = 0;
+#if QCX_JAC_COMPACT
+    if (half <= (int)blockDim.x) {
+      // Rounds with compacted rotation lists: the parameter phase also sorts the
+      // rotations into active (s != 0) and skipped ones (warp ballots and a
+      // prefix over the warps), and the update touches only the 2x2 blocks and
+      // coefficient rows that an active rotation changes.
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      int* act = sh.rskip;        // [half] active rotations of the round
+      int* inact = sh.perm;       // [half] skipped rotations
+      int* wcnt = (int*)sh.red;   // [2 kWarps] per-warp counts
+      for (int r = 0; r < m; ++r) {
+        bool on = false;
+        const int k = threadIdx.x;
+        if (k < half) {
+          int p, q;
+          if (k == 0) {
+            p = m;
+            q = r;
+          } else {
+            p = r + k;
+            if (p >= m) p -= m;
+            q = r - k;
+            if (q < 0) q += m;
+          }
+          if (p > q) {
+            int t = p;
+            p = q;
+            q = t;
+          }
+          T apq = A[p * np + q];
+          T aa = apq < T(0) ? -apq : apq;
+          offmax = aa > offmax ? aa : offmax;
+          T c = 1, s = 0;
+          if (aa > tiny) {
+            T app = A[p * np + p], aqq = A[q * np + q];
+            T theta = (aqq - app) / (T(2) * apq);
+            T at = theta < T(0) ? -theta : theta;
+            T t = (theta >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + theta * theta));
+            c = T(1) / sqrt(T(1) + t * t);
+            s = t * c;
+          }
+          pq[k] = make_int2(p, q);
+          T2 cs;
+          cs.x = c;
+          cs.y = s;
+          csr[k] = cs;
+          on = nonzero(s);
+        }
+        const unsigned ba = __ballot_sync(0xffffffffu, on);
+        const unsigned bi = __ballot_sync(0xffffffffu, !on && k < half);
+        if (lane == 0) {
+          wcnt[wid] = __popc(ba);
+          wcnt[kWarps + wid] = __popc(bi);
+        }
+        __syncthreads();
+        int offa = 0, offi = 0, na = 0, ni = 0;
+        for (int w2 = 0; w2 < kWarps; ++w2) {
+          const int ca = wcnt[w2], ci = wcnt[kWarps + w2];
+          if (w2 < wid) {
+            offa += ca;
+            offi += ci;
+          }
+          na += ca;
+          ni += ci;
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        if (on) act[offa + __popc(ba & lt)] = k;
+        else if (k < half) inact[offi + __popc(bi & lt)] = k;
+        __syncthreads();
+        if (na == 0) continue;  // nothing changes this round (uniform)
+        // blocks in the rows of an active rotation (all columns), then blocks in
+        // the rows of a skipped rotation and the columns of an active one
+        const int tot1 = na * half, tot2 = ni * na;
+        for (int e = threadIdx.x; e < tot1 + tot2; e += blockDim.x) {
+          int k1, k2;
+          if (e < tot1) {
+            const int a1 = e / half;
+            k1 = act[a1];
+            k2 = e - a1 * half;
+          } else {
+            const int f = e - tot1, i1 = f / na;
+            k1 = inact[i1];
+            k2 = act[f - i1 * na];
+          }
+          const T2 r1 = csr[k1], r2 = csr[k2];
+          const int2 e1 = pq[k1], e2 = pq[k2];
+          T* row_p = A + e1.x * np;
+          T* row_q = A + e1.y * np;
+          T a = row_p[e2.x], b = row_p[e2.y], c = row_q[e2.x], d = row_q[e2.y];
+          T ra = r1.x * a - r1.y * c, rb = r1.x * b - r1.y * d;
+          T rc = r1.y * a + r1.x * c, rd = r1.y * b + r1.x * d;
+          row_p[e2.x] = r2.x * ra - r2.y * rb;
+          row_p[e2.y] = r2.y * ra + r2.x * rb;
+          row_q[e2.x] = r2.x * rc - r2.y * rd;
+          row_q[e2.y] = r2.y * rc + r2.x * rd;
+        }
+        for (int e = threadIdx.x; e < na * np; e += blockDim.x) {
+          const int a1 = e / np, j = e - a1 * np;
+          const int kk = act[a1];
+          const T2 rr = csr[kk];
+          const int2 ee = pq[kk];
+          T vp = Vt[ee.x * np + j], vq = Vt[ee.y * np + j];
+          Vt[ee.x * np + j] = rr.x * vp - rr.y * vq;
+          Vt[ee.y * np + j] = rr.y * vp + rr.x * vq;
+        }
+        __syncthreads();
+      }
+    } else
+#endif
+    {
     for (int r = 0; r < m; ++r) {
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
         int p, q;
@@ -581,6 +695,7 @@ __device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double relto
         }
       }
       __syncthreads();
+    }
     }
     double om = cta_max((double)offmax, sh.red);
     if (om <= (double)tol || last) return sweep + 1;
