@@ -453,7 +453,9 @@ __device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double relto
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     T offmax = 0;
 #if QCX_JAC_COMPACT
-    if (half <= (int)blockDim.x) {
+    // (FP64 sweeps only: most rotations of an FP32 warm sweep are active, and
+    // there the list building costs more than the skipped items save)
+    if (sizeof(T) == 8 && half <= (int)blockDim.x) {
       // Rounds with compacted rotation lists: the parameter phase also sorts the
       // rotations into active (s != 0) and skipped ones (warp ballots and a
       // prefix over the warps), and the update touches only the 2x2 blocks and
