@@ -234,6 +234,7 @@ def run_gpu(args):
     mols = workload(rank, args.ntraj, args.workload)
     b = qg.Batch(mols, etemp=ETEMP)
     b.set_precision(args.precision)
+    b.set_guess(args.guess)
     b.egrad()
     b.sync()
     stream = torch.cuda.ExternalStream(b.stream())
@@ -333,7 +334,7 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD_NAMES[args.workload], "ntraj_per_gpu": b.nmol,
                        "atoms": [NMIN, NMAX] if args.workload == "batch" else [10, 81],
-                       "etemp_K": ETEMP, "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)",
+                       "etemp_K": ETEMP, "precision": args.precision, "scc_guess": args.guess, "l2": "flushed between timed steps (256 MiB write)",
                        "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters)),
                        "mean_scc_iters_fp64": float(np.mean(it64)),
                        "active_trajectories": int(np.sum(act))},
@@ -369,6 +370,9 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="batch", choices=["batch", "cid"])
     ap.add_argument("--no-plain", action="store_true", help="skip the single-trajectory FP64 reference leg")
+    ap.add_argument("--guess", default="zero", choices=["zero", "previous"],
+                    help="SCC start: zero moments every step (the reference's behaviour, default) or the "
+                         "trajectory's converged moments of the previous step (opt-in)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -76,6 +76,17 @@ int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, do
 #define QCX_PRECISION_MIXED 1
 int qcx_batch_set_precision(qcx_batch* b, int precision);
 
+/* Starting point of each SCC: QCX_GUESS_ZERO (default) starts from zero
+ * moments, as the reference does by creating a fresh wavefunction on every
+ * call (src/tblite.f90:133); QCX_GUESS_PREVIOUS starts a molecule's SCC from
+ * its converged moments of the previous evaluation (when that SCC converged;
+ * coordinates set in between do not matter), which needs fewer iterations
+ * along a trajectory and reaches the same solution to the SCC tolerances.
+ * This option has no counterpart in the reference. */
+#define QCX_GUESS_ZERO 0
+#define QCX_GUESS_PREVIOUS 1
+int qcx_batch_set_guess(qcx_batch* b, int guess);
+
 /* Copy host state in. Any pointer may be NULL to keep the current value.
  * xyz, vel: [natom][3]; mass: [natom] (atomic units). */
 int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass);

@@ -76,6 +76,7 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_kernel_launches.argtypes = [ctypes.c_void_p]
     lib.qcx_batch_sync.argtypes = [ctypes.c_void_p]
     lib.qcx_batch_set_precision.argtypes = [ctypes.c_void_p, c_int]
+    lib.qcx_batch_set_guess.argtypes = [ctypes.c_void_p, c_int]
     lib.qcx_batch_get_progress.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int64)]
     lib.qcx_batch_stream.restype = ctypes.c_void_p
     lib.qcx_batch_stream.argtypes = [ctypes.c_void_p]
@@ -151,8 +152,15 @@ class Batch:
         self._check(self._lib.qcx_batch_set_scc(self._h, int(max_iter), float(econv), float(pconv), float(mixing)),
                     "set_scc")
 
+    def set_guess(self, guess):
+        """0 / "zero": every SCC starts from zero moments (the reference's fresh
+        wavefunction); 1 / "previous": a trajectory's SCC starts from the converged
+        moments of its previous geometry."""
+        g = {"zero": 0, "previous": 1}.get(guess, guess)
+        self._check(self._lib.qcx_batch_set_guess(self._h, int(g)), "set_guess")
+
     def set_precision(self, precision):
-        """0 / "fp64": FP64 SCC; 1 / "mixed": FP32 SCC iterations finished in FP64."""
+        """0 / "fp64": FP64 SCC; 1 / "mixed": FP32 iterations, then double-float finishing iterations."""
         p = {"fp64": 0, "mixed": 1}.get(precision, precision)
         self._check(self._lib.qcx_batch_set_precision(self._h, int(p)), "set_precision")
 

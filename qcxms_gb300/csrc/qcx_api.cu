@@ -103,7 +103,7 @@ struct qcx_batch {
   double *d_cn = nullptr, *d_cnd = nullptr, *d_dedcn = nullptr, *d_dedcnd = nullptr, *d_mrad = nullptr,
          *d_dmrad = nullptr, *d_w4 = nullptr, *d_dw4 = nullptr, *d_qat = nullptr;
   double *d_mats = nullptr, *d_vecs = nullptr, *d_energy = nullptr, *d_ekin = nullptr;
-  int *d_status = nullptr, *d_iters = nullptr, *d_active = nullptr, *d_order = nullptr;
+  int *d_status = nullptr, *d_iters = nullptr, *d_active = nullptr, *d_order = nullptr, *d_have_prev = nullptr;
   long long* d_steps = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -179,7 +179,7 @@ void free_batch(qcx_batch* b) {
   void* ptrs[] = {b->d_prm, b->d_mol, b->d_Z, b->d_atom_mol, b->d_sh_atom, b->d_sh_k, b->d_sh_ao, b->d_pairs,
                   b->d_xyz, b->d_grad, b->d_vel, b->d_mass, b->d_cn, b->d_cnd, b->d_dedcn, b->d_dedcnd,
                   b->d_mrad, b->d_dmrad, b->d_w4, b->d_dw4, b->d_qat, b->d_mats, b->d_vecs, b->d_energy,
-                  b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps, b->d_order};
+                  b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps, b->d_order, b->d_have_prev};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->d_gpairs) cudaFree(b->d_gpairs);
@@ -271,7 +271,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
       dalloc(&b->d_mats, (size_t)mat_off) || dalloc(&b->d_vecs, (size_t)vec_off) ||
       dalloc(&b->d_energy, (size_t)nmol * kNumEnergy) || dalloc(&b->d_ekin, nmol) || dalloc(&b->d_status, nmol) ||
       dalloc(&b->d_iters, nmol) || dalloc(&b->d_active, nmol) || dalloc(&b->d_steps, nmol) ||
-      dalloc(&b->d_order, nmol))
+      dalloc(&b->d_order, nmol) || dalloc(&b->d_have_prev, nmol))
     return -1;
   {
     // launch order of the per-molecule kernels: decreasing nao^3 (work of the SCC)
@@ -332,6 +332,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   CK(cudaMemset(b->d_energy, 0, sizeof(double) * nmol * kNumEnergy));
   CK(cudaMemset(b->d_ekin, 0, sizeof(double) * nmol));
   CK(cudaMemset(b->d_steps, 0, sizeof(long long) * nmol));
+  CK(cudaMemset(b->d_have_prev, 0, sizeof(int) * nmol));
   {
     std::vector<int> on(nmol, 1);
     CK(cudaMemcpy(b->d_active, on.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
@@ -375,6 +376,8 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   d.ekin = b->d_ekin;
   d.active = b->d_active;
   d.steps_done = b->d_steps;
+  d.have_prev = b->d_have_prev;
+  d.guess = 0;
   d.order = b->d_order;
   d.max_nao = b->max_nao;
   d.smem_bytes = (int)scc_smem_bytes(b->max_nao, 0);
@@ -436,6 +439,20 @@ int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, do
   return 0;
 }
 
+int qcx_batch_set_guess(qcx_batch* b, int guess) {
+  if (!b || (guess != QCX_GUESS_ZERO && guess != QCX_GUESS_PREVIOUS)) {
+    set_error("qcx_batch_set_guess: guess must be 0 (zero moments) or 1 (previous converged moments)");
+    return -1;
+  }
+  if (guess != b->dev.guess && b->graph_exec) {
+    cudaGraphExecDestroy(b->graph_exec);
+    cudaGraphDestroy(b->graph);
+    b->graph_exec = nullptr;
+    b->graph = nullptr;
+  }
+  b->dev.guess = guess;
+  return 0;
+}
 int qcx_batch_set_precision(qcx_batch* b, int precision) {
   if (!b || (precision != 0 && precision != 1)) {
     set_error("qcx_batch_set_precision: precision must be 0 (FP64) or 1 (mixed)");

@@ -133,6 +133,8 @@ struct DevBatch {
   double* ekin;    // [nmol]
   int* active;     // [nmol] 1 while the trajectory runs; 0 after a failed evaluation
   long long* steps_done;  // [nmol] successful energy+gradient evaluations
+  int* have_prev;    // [nmol] 1 when the moment vector of a converged SCC at an earlier geometry is kept
+  int guess;         // SCC start: 0 = zero moments (a fresh wavefunction every call), 1 = the kept moments
   const int* order;  // [nmol] molecules by decreasing size: CTA b of a per-molecule kernel takes order[b]
   int max_nao;
   int smem_bytes;  // dynamic shared memory granted to the SCC kernel

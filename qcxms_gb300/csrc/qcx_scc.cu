@@ -1306,11 +1306,11 @@ __device__ __forceinline__ void dd_add(float& h, float& l, float d) {
 }
 
 // C = op(A) op(B) in double-float, with the index conventions of cta_gemm
-// (ta: A stored K x M; tb: B stored N x K). Each operand is a pair of planes
-// (hi, lo) with the same leading dimension. The result goes to the planes
-// (Ch, Cl), or, when Cd is given, to Cd as FP64.
-__device__ void cta_gemm_dd(int M, int N, int K, const float* Ah, const float* Al, int lda, bool ta, const float* Bh,
-                            const float* Bl, int ldb, bool tb, float* Ch, float* Cl, double* Cd, int ldc) {
+// (ta: A stored K x M; tb: B stored N x K). Each element is a float2 (hi, lo),
+// so one 8-byte load brings both parts. The result goes to C, or, when Cd is
+// given, to Cd as FP64.
+__device__ void cta_gemm_dd(int M, int N, int K, const float2* A, int lda, bool ta, const float2* B, int ldb,
+                            bool tb, float2* C, double* Cd, int ldc) {
   int tilesM = (M + 1) / 2, tilesN = (N + 1) / 2;
   for (int t = threadIdx.x; t < tilesM * tilesN; t += blockDim.x) {
     int i0 = (t / tilesN) * 2, j0 = (t % tilesN) * 2;
@@ -1318,16 +1318,14 @@ __device__ void cta_gemm_dd(int M, int N, int K, const float* Ah, const float* A
     int i1 = i1ok ? i0 + 1 : i0, j1 = j1ok ? j0 + 1 : j0;
     float h00 = 0.f, l00 = 0.f, h01 = 0.f, l01 = 0.f, h10 = 0.f, l10 = 0.f, h11 = 0.f, l11 = 0.f;
     for (int k = 0; k < K; ++k) {
-      long long a0 = ta ? (long long)k * lda + i0 : (long long)i0 * lda + k;
-      long long a1 = ta ? (long long)k * lda + i1 : (long long)i1 * lda + k;
-      long long b0 = tb ? (long long)j0 * ldb + k : (long long)k * ldb + j0;
-      long long b1 = tb ? (long long)j1 * ldb + k : (long long)k * ldb + j1;
-      float a0h = Ah[a0], a0l = Al[a0], a1h = Ah[a1], a1l = Al[a1];
-      float b0h = Bh[b0], b0l = Bl[b0], b1h = Bh[b1], b1l = Bl[b1];
-      dd_fma(h00, l00, a0h, a0l, b0h, b0l);
-      dd_fma(h01, l01, a0h, a0l, b1h, b1l);
-      dd_fma(h10, l10, a1h, a1l, b0h, b0l);
-      dd_fma(h11, l11, a1h, a1l, b1h, b1l);
+      const float2 a0 = A[ta ? (long long)k * lda + i0 : (long long)i0 * lda + k];
+      const float2 a1 = A[ta ? (long long)k * lda + i1 : (long long)i1 * lda + k];
+      const float2 b0 = B[tb ? (long long)j0 * ldb + k : (long long)k * ldb + j0];
+      const float2 b1 = B[tb ? (long long)j1 * ldb + k : (long long)k * ldb + j1];
+      dd_fma(h00, l00, a0.x, a0.y, b0.x, b0.y);
+      dd_fma(h01, l01, a0.x, a0.y, b1.x, b1.y);
+      dd_fma(h10, l10, a1.x, a1.y, b0.x, b0.y);
+      dd_fma(h11, l11, a1.x, a1.y, b1.x, b1.y);
     }
     dd_norm(h00, l00);
     dd_norm(h01, l01);
@@ -1335,12 +1333,8 @@ __device__ void cta_gemm_dd(int M, int N, int K, const float* Ah, const float* A
     dd_norm(h11, l11);
     auto put = [&](int i, int j, float h, float l) {
       long long c = (long long)i * ldc + j;
-      if (Cd) {
-        Cd[c] = (double)h + (double)l;
-      } else {
-        Ch[c] = h;
-        Cl[c] = l;
-      }
+      if (Cd) Cd[c] = (double)h + (double)l;
+      else C[c] = make_float2(h, l);
     };
     put(i0, j0, h00, l00);
     if (j1ok) put(i0, j1, h01, l01);
@@ -1351,22 +1345,47 @@ __device__ void cta_gemm_dd(int M, int N, int K, const float* Ah, const float* A
   }
 }
 
+// C = A B_hi in FP32 (A: M x K, ld lda; B: K x N float2, ld ldb, hi parts only)
+__device__ void cta_gemm_hi(int M, int N, int K, const float* A, int lda, const float2* B, int ldb, float* C,
+                            int ldc) {
+  int tilesM = (M + 1) / 2, tilesN = (N + 1) / 2;
+  for (int t = threadIdx.x; t < tilesM * tilesN; t += blockDim.x) {
+    int i0 = (t / tilesN) * 2, j0 = (t % tilesN) * 2;
+    bool i1ok = i0 + 1 < M, j1ok = j0 + 1 < N;
+    int i1 = i1ok ? i0 + 1 : i0, j1 = j1ok ? j0 + 1 : j0;
+    float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+    for (int k = 0; k < K; ++k) {
+      const float a0 = A[(long long)i0 * lda + k], a1 = A[(long long)i1 * lda + k];
+      const float b0 = B[(long long)k * ldb + j0].x, b1 = B[(long long)k * ldb + j1].x;
+      c00 = fmaf(a0, b0, c00);
+      c01 = fmaf(a0, b1, c01);
+      c10 = fmaf(a1, b0, c10);
+      c11 = fmaf(a1, b1, c11);
+    }
+    C[(long long)i0 * ldc + j0] = c00;
+    if (j1ok) C[(long long)i0 * ldc + j1] = c01;
+    if (i1ok) {
+      C[(long long)i1 * ldc + j0] = c10;
+      if (j1ok) C[(long long)i1 * ldc + j1] = c11;
+    }
+  }
+}
+
 // Double-float coefficient rows and the matrices of one molecule's finishing
-// iterations (mixed mode). Planes: V (rows = MOs, ld np) and its transpose Vt
-// (ld n, kept in step with V so that the products with V^T read their operand
-// along rows), B = V F V^T (ld np), F and S (ld n), T and M scratch (ld n); Kf
-// and dV are FP32 scratch (ld n).
+// iterations (mixed mode), each element a float2 (hi, lo): V (rows = MOs, ld
+// np) and its transpose Vt (ld n, kept in step with V so that the products with
+// V^T read their operand along rows), B = V F V^T (ld np), F and S (ld n), T and
+// M scratch (ld n); Kf and dV are FP32 scratch (ld n).
 struct DDMats {
-  float *Vh, *Vl, *Vth, *Vtl, *Bh, *Bl, *Fh, *Fl, *Sh, *Sl, *Th, *Tl, *Mh, *Ml, *Kf, *dV;
+  float2 *V, *Vt, *B, *F, *S, *T, *M;
+  float *Kf, *dV;
 };
 
 // Vt = V^T
 __device__ void dd_transpose(const DDMats& d, int n, int np) {
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int k = e / n, j = e - k * n;
-    long long x = (long long)j * np + k;
-    d.Vth[e] = d.Vh[x];
-    d.Vtl[e] = d.Vl[x];
+    d.Vt[e] = d.V[(long long)j * np + k];
   }
   __syncthreads();
 }
@@ -1376,21 +1395,19 @@ __device__ void dd_add_rows(const DDMats& d, int n, int np) {
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int i = e / n, j = e - i * n;
     long long x = (long long)i * np + j;
-    float h = d.Vh[x], l = d.Vl[x];
-    dd_add(h, l, d.dV[e]);
-    d.Vh[x] = h;
-    d.Vl[x] = l;
-    d.Vth[(long long)j * n + i] = h;
-    d.Vtl[(long long)j * n + i] = l;
+    float2 v = d.V[x];
+    dd_add(v.x, v.y, d.dV[e]);
+    d.V[x] = v;
+    d.Vt[(long long)j * n + i] = v;
   }
   __syncthreads();
 }
 
 // B = V F V^T
 __device__ void dd_rotate_fock(const DDMats& d, int n, int np) {
-  cta_gemm_dd(n, n, n, d.Fh, d.Fl, n, false, d.Vth, d.Vtl, n, false, d.Th, d.Tl, nullptr, n);
+  cta_gemm_dd(n, n, n, d.F, n, false, d.Vt, n, false, d.T, nullptr, n);
   __syncthreads();
-  cta_gemm_dd(n, n, n, d.Vh, d.Vl, np, false, d.Th, d.Tl, n, false, d.Bh, d.Bl, nullptr, np);
+  cta_gemm_dd(n, n, n, d.V, np, false, d.T, n, false, d.B, nullptr, np);
   __syncthreads();
 }
 
@@ -1400,19 +1417,20 @@ __device__ void dd_rotate_fock(const DDMats& d, int n, int np) {
 __device__ double dd_orthonormalize(const DDMats& d, int n, int np, int steps, SccShared& sh) {
   double emax = 0.0;
   for (int st = 0; st < steps; ++st) {
-    cta_gemm_dd(n, n, n, d.Sh, d.Sl, n, false, d.Vth, d.Vtl, n, false, d.Th, d.Tl, nullptr, n);
+    cta_gemm_dd(n, n, n, d.S, n, false, d.Vt, n, false, d.T, nullptr, n);
     __syncthreads();
-    cta_gemm_dd(n, n, n, d.Vh, d.Vl, np, false, d.Th, d.Tl, n, false, d.Mh, d.Ml, nullptr, n);
+    cta_gemm_dd(n, n, n, d.V, np, false, d.T, n, false, d.M, nullptr, n);
     __syncthreads();
     float em = 0.f;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
       int i = e / n, j = e - i * n;
-      float dev = __fadd_rn(__fsub_rn(d.Mh[e], i == j ? 1.f : 0.f), d.Ml[e]);
+      const float2 m = d.M[e];
+      float dev = __fadd_rn(__fsub_rn(m.x, i == j ? 1.f : 0.f), m.y);
       em = fmaxf(em, fabsf(dev));
       d.Kf[e] = -0.5f * dev;
     }
     emax = cta_max((double)em, sh.red);
-    cta_gemm<float, float, float, float>(n, n, n, d.Kf, n, false, d.Vh, np, false, d.dV, n);
+    cta_gemm_hi(n, n, n, d.Kf, n, d.V, np, d.dV, n);
     __syncthreads();
     dd_add_rows(d, n, np);
     // the defect left is about 3/4 n emax^2
@@ -1435,8 +1453,8 @@ __device__ bool refine_dd(const DDMats& d, int n, double* lam, double kfail, dou
     if (pass > 0) dd_rotate_fock(d, n, np);
     // diagonal in FP64
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      long long x = (long long)i * np + i;
-      lam[i] = (double)d.Bh[x] + (double)d.Bl[x];
+      const float2 b = d.B[(long long)i * np + i];
+      lam[i] = (double)b.x + (double)b.y;
     }
     __syncthreads();
     float km = 0.f;
@@ -1444,7 +1462,7 @@ __device__ bool refine_dd(const DDMats& d, int n, double* lam, double kfail, dou
       int j = e / n, i = e - j * n;
       float k = 0.f;
       if (i != j) {
-        float b = 0.5f * (d.Bh[(long long)i * np + j] + d.Bh[(long long)j * np + i]);
+        float b = 0.5f * (d.B[(long long)i * np + j].x + d.B[(long long)j * np + i].x);
         float dd = __double2float_rn(lam[j] - lam[i]);
         if (b != 0.f) k = (dd > 1e-30f || dd < -1e-30f) ? b / dd : 1e30f;
       }
@@ -1457,14 +1475,16 @@ __device__ bool refine_dd(const DDMats& d, int n, double* lam, double kfail, dou
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
       float c = 0.f;
       for (int i = 0; i < n; ++i)
-        if (i != j) c += 0.5f * (d.Bh[(long long)i * np + j] + d.Bh[(long long)j * np + i]) * d.Kf[(long long)j * n + i];
+        if (i != j)
+          c += 0.5f * (d.B[(long long)i * np + j].x + d.B[(long long)j * np + i].x) * d.Kf[(long long)j * n + i];
       d.dV[j] = c;
     }
     __syncthreads();
     for (int j = threadIdx.x; j < n; j += blockDim.x) lam[j] += (double)d.dV[j];
     __syncthreads();
     if (kmax == 0.0) return true;
-    cta_gemm<float, float, float, float>(n, n, n, d.Kf, n, false, d.Vh, np, false, d.dV, n);
+    // K^T V with the hi parts of V
+    cta_gemm_hi(n, n, n, d.Kf, n, d.V, np, d.dV, n);
     __syncthreads();
     dd_add_rows(d, n, np);
     if (kmax >= ns_min) dd_orthonormalize(d, n, np, 1, sh);
@@ -1475,8 +1495,8 @@ __device__ bool refine_dd(const DDMats& d, int n, double* lam, double kfail, dou
 }
 
 // Cd = sum_{k < nocc} w_k v_k^T v_k (FP64 result, ld n) for the double-float
-// rows v_k = V[perm[k]]: G_k = w_k v_k goes to the T planes, the rows in order
-// to the M planes, and one double-float product G^T V_occ forms the matrix.
+// rows v_k = V[perm[k]]: G_k = w_k v_k goes to T, the rows in order to M, and
+// one double-float product G^T V_occ forms the matrix.
 __device__ void dd_density(const DDMats& d, int n, int nocc, const int* perm, const double* w, double* Cd,
                            SccShared& sh) {
   const int np = n + (n & 1);
@@ -1486,20 +1506,17 @@ __device__ void dd_density(const DDMats& d, int n, int nocc, const int* perm, co
   __syncthreads();
   for (int e = threadIdx.x; e < nocc * n; e += blockDim.x) {
     int k = e / n, j = e - k * n;
-    long long x = (long long)perm[k] * np + j;
-    float vh = d.Vh[x], vl = d.Vl[x];
-    float p = __fmul_rn(wh[k], vh);
-    float er = __fmaf_rn(wh[k], vh, -p);
-    er = __fmaf_rn(wh[k], vl, er);
-    er = __fmaf_rn(wl[k], vh, er);
+    const float2 v = d.V[(long long)perm[k] * np + j];
+    float p = __fmul_rn(wh[k], v.x);
+    float er = __fmaf_rn(wh[k], v.x, -p);
+    er = __fmaf_rn(wh[k], v.y, er);
+    er = __fmaf_rn(wl[k], v.x, er);
     dd_norm(p, er);
-    d.Th[e] = p;
-    d.Tl[e] = er;
-    d.Mh[e] = vh;
-    d.Ml[e] = vl;
+    d.T[e] = make_float2(p, er);
+    d.M[e] = v;
   }
   __syncthreads();
-  cta_gemm_dd(n, n, nocc, d.Th, d.Tl, n, true, d.Mh, d.Ml, n, false, nullptr, nullptr, Cd, n);
+  cta_gemm_dd(n, n, nocc, d.T, n, true, d.M, n, false, nullptr, Cd, n);
   __syncthreads();
 }
 
@@ -1663,6 +1680,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     if (threadIdx.x == 0) {
       bt.status[mol] = status;
       bt.iters[mol] = 0;
+      if (bt.have_prev) bt.have_prev[mol] = 0;
     }
     return;
   }
@@ -1688,20 +1706,13 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   // copy plus a lo plane in the W slot (free until W is formed), scratch in
   // the T, C and X slots (X is only needed without an FP32 phase)
   DDMats dm;
-  dm.Vh = (float*)JV;
-  dm.Vl = dm.Vh + (long long)np * np;
-  dm.Vth = Q32;  // the FP32 quadrupoles are not needed after the FP32 iterations
-  dm.Vtl = dm.Vth + nn;
-  dm.Bh = (float*)JA;
-  dm.Bl = dm.Bh + (long long)np * np;
-  dm.Fh = (float*)F;
-  dm.Fl = dm.Fh + nn;
-  dm.Sh = S32;
-  dm.Sl = (float*)Wm;
-  dm.Th = (float*)T;
-  dm.Tl = dm.Th + nn;
-  dm.Mh = (float*)C;
-  dm.Ml = dm.Mh + nn;
+  dm.V = (float2*)JV;
+  dm.Vt = (float2*)Q32;  // the FP32 quadrupoles are not needed after the FP32 iterations
+  dm.B = (float2*)JA;
+  dm.F = (float2*)F;
+  dm.S = (float2*)Wm;
+  dm.T = (float2*)T;
+  dm.M = (float2*)C;
   dm.Kf = (float*)X;
   dm.dV = dm.Kf + nn;
   if (MIXED) {
@@ -1715,7 +1726,11 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       for (int c = 0; c < 6; ++c) Q32[c * nn + e] = (float)Qm[c * nn + e];
     }
   }
-  for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = 0.0;
+  // start from zero moments (the reference's fresh wavefunction), or, when the
+  // caller asked for it, from the converged output moments of the previous
+  // geometry of this trajectory (still in xout)
+  const bool warm_guess = bt.guess == 1 && bt.have_prev != nullptr && bt.have_prev[mol] != 0;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = warm_guess ? xout[i] : 0.0;
   __syncthreads();
 
   double en[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -1809,7 +1824,11 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
           for (int c = 0; c < 3; ++c) f -= 0.5 * (vdp[3 * A + c] * Dm[c * nn + e] + vdp[3 * B + c] * Dm[c * nn + ji]);
 #pragma unroll
           for (int c = 0; c < 6; ++c) f -= 0.5 * (vqp[6 * A + c] * Qm[c * nn + e] + vqp[6 * B + c] * Qm[c * nn + ji]);
-          if (MIXED && have32) dd_split(f, dm.Fh[e], dm.Fl[e]);  // double-float finishing iterations
+          if (MIXED && have32) {  // double-float finishing iterations
+            float2 v;
+            dd_split(f, v.x, v.y);
+            dm.F[e] = v;
+          }
           else F[e] = f;
         }
       }
@@ -1893,11 +1912,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       if (!have64) {
         // FP32 coefficients -> double-float rows, re-orthonormalised in the S
         // metric (the FP32 rows live in the lo plane of B, so this precedes B)
-        for (long long e = threadIdx.x; e < (long long)np * np; e += blockDim.x) {
-          dm.Vh[e] = JV32[e];
-          dm.Vl[e] = 0.f;
-        }
-        for (long long e = threadIdx.x; e < nn; e += blockDim.x) dm.Sl[e] = __double2float_rn(S[e] - (double)S32[e]);
+        for (long long e = threadIdx.x; e < (long long)np * np; e += blockDim.x) dm.V[e] = make_float2(JV32[e], 0.f);
+        for (long long e = threadIdx.x; e < nn; e += blockDim.x)
+          dm.S[e] = make_float2(S32[e], __double2float_rn(S[e] - (double)S32[e]));
         __syncthreads();
         dd_transpose(dm, n, np);
         dd_orthonormalize(dm, n, np, 2, sh);
@@ -1911,19 +1928,17 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       if (!refined) {
         // FP64 Jacobi on B in the current basis: planes -> FP64 through the T
         // and C slots, and the rotated rows back to double-float
-        float* tB = (float*)T;
-        float* tV = (float*)C;
+        float2* tB = (float2*)T;
+        float2* tV = (float2*)C;
         const long long np2 = (long long)np * np;
         for (long long e = threadIdx.x; e < np2; e += blockDim.x) {
-          tB[e] = dm.Bh[e];
-          tB[np2 + e] = dm.Bl[e];
-          tV[e] = dm.Vh[e];
-          tV[np2 + e] = dm.Vl[e];
+          tB[e] = dm.B[e];
+          tV[e] = dm.V[e];
         }
         __syncthreads();
         for (long long e = threadIdx.x; e < np2; e += blockDim.x) {
-          JA[e] = (double)tB[e] + (double)tB[np2 + e];
-          JV[e] = (double)tV[e] + (double)tV[np2 + e];
+          JA[e] = (double)tB[e].x + (double)tB[e].y;
+          JV[e] = (double)tV[e].x + (double)tV[e].y;
         }
         __syncthreads();
         for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -1940,7 +1955,11 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         double* tD = C;
         for (long long e = threadIdx.x; e < np2; e += blockDim.x) tD[e] = JV[e];
         __syncthreads();
-        for (long long e = threadIdx.x; e < np2; e += blockDim.x) dd_split(tD[e], dm.Vh[e], dm.Vl[e]);
+        for (long long e = threadIdx.x; e < np2; e += blockDim.x) {
+          float2 v;
+          dd_split(tD[e], v.x, v.y);
+          dm.V[e] = v;
+        }
         __syncthreads();
         dd_transpose(dm, n, np);
       }
@@ -2239,6 +2258,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     if (eig_fail) st |= kEigenNotConverged;
     if (!isfinite(eel)) st |= kNonFinite;
     bt.status[mol] = st;
+    if (bt.have_prev) bt.have_prev[mol] = st == 0 ? 1 : 0;
     bt.iters[mol] = it;
   }
 }
