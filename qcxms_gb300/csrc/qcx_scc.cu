@@ -18,6 +18,9 @@ namespace qcx {
 #ifndef QCX_JAC32_WARM_SWEEPS
 #define QCX_JAC32_WARM_SWEEPS 1
 #endif
+#ifndef QCX_JAC32_COLD_TOL
+#define QCX_JAC32_COLD_TOL 2e-6
+#endif
 #ifndef QCX_MIXED_SWITCH
 #define QCX_MIXED_SWITCH 1e-4
 #endif
@@ -785,7 +788,8 @@ __device__ double fermi_warp32(int n, const double* eps, double nel, double kT, 
     float N = 0.0f, dN = 0.0f;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      float f = 1.0f / (1.0f + expf((d[k] - mu) * ikT));
+      // fast exp and division: the FP32 iterations need the level to ~1e-6 electrons
+      float f = __fdividef(1.0f, 1.0f + __expf((d[k] - mu) * ikT));
       N += 2.0f * f;
       dN += 2.0f * f * (1.0f - f) * ikT;
     }
@@ -1880,7 +1884,11 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
                                 QCX_REFINE32_PASSES, 1e-3, sh, efermi, 25.0 * md.kT);
       PHASE_MARK(16);
       if (try32 && !ok32) backoff32 = QCX_REFINE32_BACKOFF;
-      if (!ok32) jacobi<float>(JA32, JV32, n, have32, 2e-6, sh, have32 ? QCX_JAC32_WARM_SWEEPS : 30);
+      // the first (cold) solve only seeds the FP32 iterations: it stops at a
+      // looser tolerance, the warm sweeps and refinements of later iterations
+      // take the basis further
+      if (!ok32) jacobi<float>(JA32, JV32, n, have32, have32 ? 2e-6 : QCX_JAC32_COLD_TOL, sh,
+                               have32 ? QCX_JAC32_WARM_SWEEPS : 30);
 #ifdef QCX_SCC_PHASE_TIMING
       if (threadIdx.x == 0) atomicAdd(&g_phase_cycles[ok32 ? 13 : 14], 1ull);
 #endif
@@ -2062,17 +2070,23 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       double ef;
       double ts = fp32_phase ? fermi_warp32(n, eps, nel, md.kT, focc, &ef, efermi, it > 1)
                              : fermi_warp(n, eps, nel, md.kT, focc, &ef, 1e-13, efermi, it > 1);
+      // highest occupied orbital + 1 (occupations are >= 0, so focc > 0 is a
+      // test on the bit pattern, not an FP64 compare); the warp has just written focc
+      __syncwarp();
+      int last = 0;
+      for (int k = threadIdx.x; k < n; k += 32)
+        if (__double_as_longlong(focc[k]) > 0) last = k + 1;
+      for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
       if (threadIdx.x == 0) {
         sh.scal[0] = ts;
         sh.scal[1] = ef;
+        sh.scal[2] = (double)last;
       }
     }
     __syncthreads();
     ets = sh.scal[0];
     efermi = sh.scal[1];
-    // occupations are >= 0, so focc > 0 is a test on the bit pattern (no FP64 compare)
-    for (int k = 0; k < n; ++k)
-      if (__double_as_longlong(focc[k]) > 0) nocc = k + 1;
+    nocc = (int)sh.scal[2];
     PHASE_MARK(7);
     // P = C f C^T over the occupied (sorted) orbitals; the FP32 iterations keep
     // P as FP32 (in the P slot) for the FP32 moments
