@@ -55,6 +55,20 @@ WORKLOAD_NAMES = {
 }
 
 
+def reduce_over_ranks(t, done, world, device):
+    """Whole-job figures of weakly scaled ranks: the slowest rank's time (max) and
+    the units all ranks processed (sum). No other collective touches the data path."""
+    import torch
+    v = torch.tensor([t, done], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        tmax, dsum = v[0:1].clone(), v[1:2].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(dsum, op=dist.ReduceOp.SUM)
+        return float(tmax[0]), float(dsum[0])
+    return float(v[0]), float(v[1])
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -269,13 +283,7 @@ def run_gpu(args):
         barrier()
     _, steps1 = b.progress()
     done = float(np.sum(steps1 - steps0))
-    ms_all = torch.tensor([total_ms, done], dtype=torch.float64, device="cuda")
-    if world > 1:
-        t = ms_all.clone()
-        torch.distributed.all_reduce(t[0:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:2], op=torch.distributed.ReduceOp.SUM)
-        ms_all = t
-    total_ms, done_all = float(ms_all[0]), float(ms_all[1])
+    total_ms, done_all = reduce_over_ranks(total_ms, done, world, "cuda")
     value = done_all / (total_ms * 1e-3)
 
     # ---- end to end through the public API with pinned host buffers ----
@@ -295,11 +303,7 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t0
     _, s1 = b.progress()
     e2e_done = float(np.sum(s1 - s0))
-    if world > 1:
-        t = torch.tensor([e2e_s, e2e_done], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t[0:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:2], op=torch.distributed.ReduceOp.SUM)
-        e2e_s, e2e_done = float(t[0]), float(t[1])
+    e2e_s, e2e_done = reduce_over_ranks(e2e_s, e2e_done, world, "cuda")
     e2e = e2e_done / e2e_s
     h2d = 2 * 3 * 8 * b.natom
     d2h = 2 * 3 * 8 * b.natom + 8 * b.nmol
