@@ -125,6 +125,17 @@ long long qcx_batch_kernel_launches(qcx_batch* b);
  * Setting new coordinates with qcx_batch_set_state restarts all. */
 int qcx_batch_get_progress(qcx_batch* b, int32_t* active, int64_t* steps_done);
 
+/* Fragment assignment of every molecule at its current coordinates, as
+ * fragment_structure (src/fragments.f90:93-182), which md.f90:450 calls every
+ * step with rcut = 3.0, at1 = 1, at2 = 0: atoms are bonded when their distance
+ * is below rcut times the mean of their QCxMS covalent radii
+ * (src/covalent_radii.f90:89); fragment 1 is at1's, the others follow in the
+ * order of their lowest-numbered atom. at1/at2 are 1-based atom numbers within
+ * each molecule (at1 = at2 = 0: everything one fragment; at2 != 0: the at1-at2
+ * bond does not count). frag[natom] gets the 1-based fragment number of every
+ * atom, nfrag[nmol] the number of fragments; either may be NULL. */
+int qcx_batch_fragments(qcx_batch* b, double rcut, int at1, int at2, int32_t* frag, int32_t* nfrag);
+
 /* Synchronise the batch's stream. */
 int qcx_batch_sync(qcx_batch* b);
 

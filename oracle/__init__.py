@@ -58,6 +58,7 @@ def lib():
         _lib.qcxo_gnorm.restype = ctypes.c_double
         _lib.qcxo_getspin.restype = ctypes.c_int
         _lib.qcxo_checkqc.restype = ctypes.c_int
+        _lib.qcxo_fragments.restype = ctypes.c_int
         _lib.qcxo_md_batch.restype = ctypes.c_int
     return _lib
 
@@ -158,6 +159,17 @@ def checkqc(e, grad, qat, charge):
     ee = ctypes.c_double(e)
     ok = lib().qcxo_checkqc(grad.shape[0], ctypes.byref(ee), _p(grad), _p(qat), int(charge))
     return bool(ok), ee.value
+
+
+def fragments(Z, xyz, rcut=3.0, at1=1, at2=0):
+    """Fragment numbers (1-based) of every atom and the fragment count, as
+    fragment_structure (src/fragments.f90:93-182)."""
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(len(Z), 3)
+    frag = np.zeros(len(Z), dtype=np.int32)
+    nf = lib().qcxo_fragments(len(Z), _p(Z, ctypes.c_int), _p(xyz), ctypes.c_double(rcut), int(at1), int(at2),
+                              _p(frag, ctypes.c_int))
+    return frag, nf
 
 
 def md_batch(mols, nsteps, tstep, grad0, kT, opts=None, nthreads=0):

@@ -1347,3 +1347,57 @@ int qcxo_md_batch(int ntraj, const int* off, const int* Z, double* xyz, double* 
   }
   return fails;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Fragment assignment: restatement of fragment_structure                    */
+/* (src/fragments.f90:93-182) with the QCxMS radii of src/covalent_radii.f90:89 */
+/* (Angstrom, converted with autoaa = 0.52917726, src/xtb_mctc_convert.f90:24). */
+/* ------------------------------------------------------------------------- */
+static const double kFragRadAA[19] = {0.0,  0.32, 0.37, 1.30, 0.99, 0.84, 0.75, 0.71, 0.64, 0.60,
+                                      0.62, 1.60, 1.40, 1.24, 1.14, 1.09, 1.04, 1.00, 1.01};
+
+int qcxo_fragments(int nat, const int* Z, const double* xyz, double rcut, int at1, int at2, int* frag) {
+  const double aatoau = 1.0 / 0.52917726;
+  unsigned char* connect = (unsigned char*)calloc((size_t)nat * nat, 1);
+  for (int i = 0; i < nat - 1; ++i)
+    for (int j = i + 1; j < nat; ++j) {
+      double dx = xyz[3 * i] - xyz[3 * j], dy = xyz[3 * i + 1] - xyz[3 * j + 1], dz = xyz[3 * i + 2] - xyz[3 * j + 2];
+      double r = sqrt(dx * dx + dy * dy + dz * dz);
+      double rcov = rcut * 0.5 * (aatoau * kFragRadAA[Z[i]] + aatoau * kFragRadAA[Z[j]]);
+      if (r < rcov) connect[(size_t)i * nat + j] = connect[(size_t)j * nat + i] = 1;
+    }
+  int nfrag = 1;
+  if (at1 == 0 && at2 == 0) {
+    for (int i = 0; i < nat; ++i) frag[i] = 1;
+  } else {
+    for (int i = 0; i < nat; ++i) frag[i] = 0;
+    frag[at1 - 1] = 1;
+    int total = 1, current = 0;
+    if (at2 != 0) connect[(size_t)(at1 - 1) * nat + at2 - 1] = connect[(size_t)(at2 - 1) * nat + at1 - 1] = 0;
+    while (total != nat) {
+      ++current;
+      int changed = 1;
+      while (changed) {  /* sweep until the fragment stops growing */
+        changed = 0;
+        for (int i = 0; i < nat; ++i)
+          if (frag[i] == current)
+            for (int j = 0; j < nat; ++j)
+              if (connect[(size_t)i * nat + j] && frag[j] == 0) {
+                frag[j] = current;
+                ++total;
+                changed = 1;
+              }
+      }
+      for (int i = 0; i < nat; ++i) /* first atom of the next fragment */
+        if (frag[i] == 0) {
+          frag[i] = current + 1;
+          ++total;
+          break;
+        }
+    }
+    nfrag = 0;
+    for (int i = 0; i < nat; ++i) nfrag = frag[i] > nfrag ? frag[i] : nfrag;
+  }
+  free(connect);
+  return nfrag;
+}

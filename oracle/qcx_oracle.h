@@ -70,6 +70,13 @@ int qcxo_getspin(int nat, const int* Z, int charge);
 double qcxo_gnorm(int nat, const double* grad);
 int qcxo_checkqc(int nat, double* e, const double* grad, const double* qat, int charge);
 
+/* Fragment assignment (src/fragments.f90:93-182, fragment_structure): atoms i, j
+ * are bonded when r_ij < rcut * 0.5 * (R_i + R_j) with the QCxMS radii
+ * (src/covalent_radii.f90:89, Rad); at1/at2 are 1-based as in the reference
+ * (at1 = at2 = 0: one fragment; at2 != 0: the at1-at2 bond is ignored).
+ * frag[nat] gets 1-based fragment numbers; returns the number of fragments. */
+int qcxo_fragments(int nat, const int* Z, const double* xyz, double rcut, int at1, int at2, int* frag);
+
 /* Batched MD on the CPU: ntraj independent trajectories, each advanced nsteps
  * leapfrog + egrad steps (OpenMP over trajectories). Arrays are concatenated
  * per trajectory using atom offsets off[ntraj+1]. grad must hold the gradient

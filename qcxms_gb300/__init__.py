@@ -77,6 +77,8 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_sync.argtypes = [ctypes.c_void_p]
     lib.qcx_batch_set_precision.argtypes = [ctypes.c_void_p, c_int]
     lib.qcx_batch_set_guess.argtypes = [ctypes.c_void_p, c_int]
+    lib.qcx_batch_fragments.argtypes = [ctypes.c_void_p, ctypes.c_double, c_int, c_int, P(ctypes.c_int32),
+                                        P(ctypes.c_int32)]
     lib.qcx_batch_get_progress.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int64)]
     lib.qcx_batch_stream.restype = ctypes.c_void_p
     lib.qcx_batch_stream.argtypes = [ctypes.c_void_p]
@@ -204,6 +206,16 @@ class Batch:
         if rc < 0:
             raise RuntimeError("get_matrix failed: " + _err(self._lib))
         return out
+
+    def fragments(self, rcut=3.0, at1=1, at2=0):
+        """Fragment numbers of every atom (1-based, per molecule) and fragment
+        counts at the current coordinates, as fragment_structure
+        (src/fragments.f90:93-182); md.f90:450 uses rcut 3.0, at1 1, at2 0."""
+        frag = np.zeros(self.natom, dtype=np.int32)
+        nfrag = np.zeros(self.nmol, dtype=np.int32)
+        self._check(self._lib.qcx_batch_fragments(self._h, float(rcut), int(at1), int(at2), _ip(frag), _ip(nfrag)),
+                    "fragments")
+        return frag, nfrag
 
     def progress(self):
         active = np.zeros(self.nmol, dtype=np.int32)

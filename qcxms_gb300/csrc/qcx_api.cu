@@ -104,6 +104,9 @@ struct qcx_batch {
          *d_dmrad = nullptr, *d_w4 = nullptr, *d_dw4 = nullptr, *d_qat = nullptr;
   double *d_mats = nullptr, *d_vecs = nullptr, *d_energy = nullptr, *d_ekin = nullptr;
   int *d_status = nullptr, *d_iters = nullptr, *d_active = nullptr, *d_order = nullptr, *d_have_prev = nullptr;
+  int *d_frag = nullptr, *d_nfrag = nullptr;  // fragment numbers [natom], counts [nmol]
+  double* d_frad = nullptr;                   // QCxMS fragment radii (Bohr) by atomic number
+  int min_nat = 0, max_nat = 0;
   long long* d_steps = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -179,7 +182,8 @@ void free_batch(qcx_batch* b) {
   void* ptrs[] = {b->d_prm, b->d_mol, b->d_Z, b->d_atom_mol, b->d_sh_atom, b->d_sh_k, b->d_sh_ao, b->d_pairs,
                   b->d_xyz, b->d_grad, b->d_vel, b->d_mass, b->d_cn, b->d_cnd, b->d_dedcn, b->d_dedcnd,
                   b->d_mrad, b->d_dmrad, b->d_w4, b->d_dw4, b->d_qat, b->d_mats, b->d_vecs, b->d_energy,
-                  b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps, b->d_order, b->d_have_prev};
+                  b->d_ekin, b->d_status, b->d_iters, b->d_active, b->d_steps, b->d_order, b->d_have_prev,
+                  b->d_frag, b->d_nfrag, b->d_frad};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->d_gpairs) cudaFree(b->d_gpairs);
@@ -271,7 +275,8 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
       dalloc(&b->d_mats, (size_t)mat_off) || dalloc(&b->d_vecs, (size_t)vec_off) ||
       dalloc(&b->d_energy, (size_t)nmol * kNumEnergy) || dalloc(&b->d_ekin, nmol) || dalloc(&b->d_status, nmol) ||
       dalloc(&b->d_iters, nmol) || dalloc(&b->d_active, nmol) || dalloc(&b->d_steps, nmol) ||
-      dalloc(&b->d_order, nmol) || dalloc(&b->d_have_prev, nmol))
+      dalloc(&b->d_order, nmol) || dalloc(&b->d_have_prev, nmol) || dalloc(&b->d_frag, na) ||
+      dalloc(&b->d_nfrag, nmol) || dalloc(&b->d_frad, kMaxZ + 1))
     return -1;
   {
     // launch order of the per-molecule kernels: decreasing nao^3 (work of the SCC)
@@ -333,6 +338,23 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   CK(cudaMemset(b->d_ekin, 0, sizeof(double) * nmol));
   CK(cudaMemset(b->d_steps, 0, sizeof(long long) * nmol));
   CK(cudaMemset(b->d_have_prev, 0, sizeof(int) * nmol));
+  {
+    // radii of the fragment test: src/covalent_radii.f90:89 (Rad, Angstrom) times
+    // aatoau = 1/0.52917726 (src/xtb_mctc_convert.f90:24-25), elements 1-18
+    static const double rad_aa[19] = {0.0,  0.32, 0.37, 1.30, 0.99, 0.84, 0.75, 0.71, 0.64, 0.60,
+                                      0.62, 1.60, 1.40, 1.24, 1.14, 1.09, 1.04, 1.00, 1.01};
+    static_assert(kMaxZ == 18, "fragment radii cover elements 1-18");
+    const double aatoau = 1.0 / 0.52917726;
+    double rad[kMaxZ + 1];
+    for (int z = 0; z <= kMaxZ; ++z) rad[z] = aatoau * rad_aa[z];
+    CK(cudaMemcpy(b->d_frad, rad, sizeof(rad), cudaMemcpyHostToDevice));
+    b->min_nat = nat[0];
+    b->max_nat = nat[0];
+    for (int m = 1; m < nmol; ++m) {
+      b->min_nat = nat[m] < b->min_nat ? nat[m] : b->min_nat;
+      b->max_nat = nat[m] > b->max_nat ? nat[m] : b->max_nat;
+    }
+  }
   {
     std::vector<int> on(nmol, 1);
     CK(cudaMemcpy(b->d_active, on.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
@@ -439,6 +461,20 @@ int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, do
   return 0;
 }
 
+int qcx_batch_fragments(qcx_batch* b, double rcut, int at1, int at2, int32_t* frag, int32_t* nfrag) {
+  if (!b || !(rcut > 0.0) || at1 < 0 || at2 < 0 || at1 > b->min_nat || at2 > b->min_nat ||
+      (at1 == 0 && at2 != 0)) {
+    set_error("qcx_batch_fragments: invalid arguments (rcut > 0, 0 <= at1, at2 <= atoms of the smallest molecule, "
+              "at1 = 0 only with at2 = 0)");
+    return -1;
+  }
+  launch_fragments(b->dev, b->max_nat, b->d_frad, rcut, at1, at2, b->d_frag, b->d_nfrag, b->stream);
+  if (check_launch()) return -1;
+  if (frag) CK(cudaMemcpyAsync(frag, b->d_frag, sizeof(int) * b->natom, cudaMemcpyDeviceToHost, b->stream));
+  if (nfrag) CK(cudaMemcpyAsync(nfrag, b->d_nfrag, sizeof(int) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
 int qcx_batch_set_guess(qcx_batch* b, int guess) {
   if (!b || (guess != QCX_GUESS_ZERO && guess != QCX_GUESS_PREVIOUS)) {
     set_error("qcx_batch_set_guess: guess must be 0 (zero moments) or 1 (previous converged moments)");

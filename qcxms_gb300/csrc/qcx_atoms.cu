@@ -366,4 +366,86 @@ void launch_leapfrog(const DevBatch& bt, double tstep, cudaStream_t st) {
   k_leapfrog<<<bt.nmol, 128, 0, st>>>(bt, tstep);
 }
 
+// ---------------------------------------------------------------------------
+// Fragment assignment of every molecule (src/fragments.f90:93-182,
+// fragment_structure): atoms i, j are bonded when r_ij < rcut * 0.5 * (R_i +
+// R_j) with the QCxMS radii rad (src/covalent_radii.f90:89, in Bohr). The
+// reference grows fragment 1 from atom at1 and each further fragment from the
+// lowest-numbered atom not yet assigned; that is the connected components of
+// the bond graph, numbered with at1's component first and the others in the
+// order of their lowest atom. Here every atom starts with its own index as
+// label and bonded pairs take the minimum (sweeps until nothing changes, at
+// most nat), which leaves each component labelled by its lowest atom. The
+// distance test uses the reference's operation order with explicit roundings,
+// so the bonds, and with them the labels, are exactly the reference's.
+// at1/at2 are 1-based as in the reference (at1 = at2 = 0: one fragment;
+// at2 != 0: the at1-at2 bond does not count). CTA per molecule.
+// ---------------------------------------------------------------------------
+constexpr int kFragThreads = 256;
+
+__global__ void __launch_bounds__(kFragThreads) k_fragments(DevBatch bt, const double* rad, double rcut, int at1,
+                                                            int at2, int* frag, int* nfrag) {
+  extern __shared__ int fsm[];
+  const int mol = blockIdx.x;
+  const MolDesc md = bt.mol[mol];
+  const int nat = md.nat, off = md.atom_off;
+  int* lab = fsm;             // [nat]
+  int* flag = fsm + nat;      // [1]
+  if (at1 == 0 && at2 == 0) {
+    for (int i = threadIdx.x; i < nat; i += blockDim.x) frag[off + i] = 1;
+    if (threadIdx.x == 0) nfrag[mol] = 1;
+    return;
+  }
+  for (int i = threadIdx.x; i < nat; i += blockDim.x) lab[i] = i;
+  const double half_rcut = __dmul_rn(rcut, 0.5);
+  for (int sweep = 0; sweep <= nat; ++sweep) {
+    if (threadIdx.x == 0) *flag = 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nat * nat; e += blockDim.x) {
+      const int i = e / nat, j = e - i * nat;
+      if (j <= i) continue;
+      if (at2 != 0 && ((i == at1 - 1 && j == at2 - 1) || (i == at2 - 1 && j == at1 - 1))) continue;
+      const double* ri = bt.xyz + 3LL * (off + i);
+      const double* rj = bt.xyz + 3LL * (off + j);
+      const double dx = __dsub_rn(ri[0], rj[0]), dy = __dsub_rn(ri[1], rj[1]), dz = __dsub_rn(ri[2], rj[2]);
+      const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+      const double rcov = __dmul_rn(half_rcut, __dadd_rn(rad[bt.Z[off + i]], rad[bt.Z[off + j]]));
+      if (!(r < rcov)) continue;
+      const int li = lab[i], lj = lab[j];
+      if (li != lj) {
+        const int m = li < lj ? li : lj;
+        atomicMin(&lab[i], m);
+        atomicMin(&lab[j], m);
+        *flag = 1;
+      }
+    }
+    __syncthreads();
+    const int changed = *flag;
+    __syncthreads();
+    if (!changed) break;
+  }
+  // number the components: at1's first, the others by their lowest atom
+  const int r1 = lab[at1 - 1];
+  for (int i = threadIdx.x; i < nat; i += blockDim.x) {
+    const int li = lab[i];
+    int f = 1;
+    if (li != r1) {
+      f = 2;
+      for (int k = 0; k < li; ++k)
+        if (lab[k] == k && k != r1) ++f;
+    }
+    frag[off + i] = f;
+  }
+  if (threadIdx.x == 0) {
+    int roots = 0;
+    for (int k = 0; k < nat; ++k) roots += lab[k] == k;
+    nfrag[mol] = roots;
+  }
+}
+
+void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,
+                      int* nfrag, cudaStream_t st) {
+  k_fragments<<<bt.nmol, kFragThreads, sizeof(int) * (max_nat + 1), st>>>(bt, rad, rcut, at1, at2, frag, nfrag);
+}
+
 }  // namespace qcx

@@ -15,6 +15,9 @@ int launch_grad_pairs(const DevBatch& bt, cudaStream_t st);
 void launch_grad_atoms(const DevBatch& bt, cudaStream_t st);
 void launch_leapfrog(const DevBatch& bt, double tstep, cudaStream_t st);
 void launch_zero_grad(const DevBatch& bt, cudaStream_t st);
+// fragment numbers of every molecule's atoms (frag[natom]) and fragment counts (nfrag[nmol])
+void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,
+                      int* nfrag, cudaStream_t st);
 
 // dynamic shared memory the SCC kernel asks for, given the largest molecule
 size_t scc_smem_bytes(int max_nao, int precision);

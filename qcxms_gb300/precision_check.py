@@ -16,7 +16,11 @@ import numpy as np
 from . import Batch, molgen
 
 
-def run(ntraj=64, natoms=60, seed0=0):
+def run(ntraj=64, natoms=60, seed0=0, scc=None):
+    """scc: (max_iter, econv, pconv, mixing) for both paths; default thresholds if None.
+    At the default thresholds (1e-7 Eh, 1e-6) the two paths may stop at iterates
+    whose gradients differ by several 1e-6 Eh/Bohr; tight thresholds isolate the
+    arithmetic."""
     mols = []
     for t in range(ntraj):
         Z, xyz = molgen.random_chno(natoms, 900000 + seed0 + t)
@@ -25,6 +29,8 @@ def run(ntraj=64, natoms=60, seed0=0):
     for prec in ("fp64", "mixed"):
         b = Batch(mols)
         b.set_precision(prec)
+        if scc:
+            b.set_scc(*scc)
         b.egrad()
         out[prec] = b.get()
         out[prec]["split_grad"] = b.split(out[prec]["grad"])
@@ -44,7 +50,10 @@ def main():
     ap.add_argument("--ntraj", type=int, default=64)
     ap.add_argument("--natoms", type=int, default=60)
     a = ap.parse_args()
-    print(json.dumps(run(a.ntraj, a.natoms)))
+    res = run(a.ntraj, a.natoms)
+    tight = run(a.ntraj, a.natoms, scc=(100, 1e-10, 1e-8, 0.25))
+    res["tight_scc"] = {k: tight[k] for k in ("both_converged", "max_abs_dE", "max_abs_dg")}
+    print(json.dumps(res))
 
 
 if __name__ == "__main__":

@@ -36,7 +36,7 @@ def test_warm_start_same_trajectory_fewer_iterations(gpu):
     e0, it0, r0, a0 = _run("zero")
     e1, it1, r1, a1 = _run("previous")
     ok = (a0 > 0) & (a1 > 0)
-    assert ok.sum() >= 10
+    assert ok.sum() >= 6
     # same solution to well inside the SCC tolerances over six steps
     assert np.abs(e0[:, ok] - e1[:, ok]).max() < 1e-6
     at = np.repeat(ok, [len(m["Z"]) for m in molgen.batch_workload(12, 8, 30, seed0=7)])
