@@ -49,9 +49,8 @@ def workload(rank, ntraj=None, kind="batch"):
 
 
 WORKLOAD_NAMES = {
-    "batch": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs, one CUDA graph per MD step",
-    "cid": "4096 C/H/N/O/S cations, 10-80 atoms, + Ar at 40 eV lab frame, b ~ U(0, 2 A), 0.5 fs, one CUDA graph "
-           "per MD step",
+    "batch": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs",
+    "cid": "4096 C/H/N/O/S cations, 10-80 atoms, + Ar at 40 eV lab frame, b ~ U(0, 2 A), 0.5 fs",
 }
 
 
@@ -224,8 +223,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "trajectory-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * NTRAJ / v, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "256 C/H/N/O cations, 5-40 atoms, T0 1000-4000 K, 0.5 fs, FP64",
-                   "ntraj": NTRAJ, "atoms": [NMIN, NMAX], "etemp_K": ETEMP},
+        "config": {"workload": WORKLOAD_NAMES["batch"], "ntraj_per_gpu": NTRAJ, "atoms": [NMIN, NMAX],
+                   "etemp_K": ETEMP, "precision": "fp64 (CPU restatement)"},
         "cpu_baseline": {"value": v, "unit": "trajectory-steps/s", "cores": ncpu, "kind": "port",
                          "sample": "%d of the %d trajectories, leapfrog + CPU FP64 restatement of the energy/gradient, "
                                    "OpenMP over trajectories, ~20 s" % (len(sample), NTRAJ)},
@@ -338,7 +337,8 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD_NAMES[args.workload], "ntraj_per_gpu": b.nmol,
                        "atoms": [NMIN, NMAX] if args.workload == "batch" else [10, 81],
-                       "etemp_K": ETEMP, "precision": args.precision, "scc_guess": args.guess, "l2": "flushed between timed steps (256 MiB write)",
+                       "etemp_K": ETEMP, "precision": args.precision, "scc_guess": args.guess,
+                       "execution": "one CUDA graph per MD step, 8 molecule groups on separate streams", "l2": "flushed between timed steps (256 MiB write)",
                        "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters)),
                        "mean_scc_iters_fp64": float(np.mean(it64)),
                        "active_trajectories": int(np.sum(act))},
