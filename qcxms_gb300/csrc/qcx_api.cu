@@ -116,9 +116,10 @@ struct qcx_batch {
   int precision = 0;
   int step_launches = 0;
   // Molecule groups: contiguous chunks of the size order (largest first).
-  // After the batch-wide coordination numbers and integrals, each group runs
-  // its SCC and gradient kernels on its own stream, so that the gradients of
-  // groups that converge early overlap the SCC of the slowest molecules.
+  // After the batch-wide coordination numbers, each group runs its integral,
+  // SCC and gradient kernels on its own stream, so that the group of the
+  // largest molecules starts its SCC after its own integrals and the gradients
+  // of groups that converge early overlap the SCC of the slowest molecules.
   int ngroup = 1;
   std::vector<int> g_start, g_count;      // range of each group in the size order
   std::vector<int> g_pair_start;          // first pair of each group in d_gpairs
@@ -148,10 +149,10 @@ int enqueue_egrad(qcx_batch* b) {
   const DevBatch& d = b->dev;
   int n = 0;
   launch_cn(d, b->stream);
-  n += 1 + launch_integrals(d, b->stream);
   launch_zero_grad(d, b->stream);
-  ++n;
+  n += 2;
   if (b->ngroup == 1) {
+    n += launch_integrals(d, b->stream);
     launch_scc(d, b->precision, b->stream);
     n += 1 + launch_grad_pairs(d, b->stream);
     launch_grad_atoms(d, b->stream);
@@ -162,6 +163,7 @@ int enqueue_egrad(qcx_batch* b) {
     cudaStream_t st = b->g_stream[g];
     if (g > 0 && cudaStreamWaitEvent(st, b->g_fork, 0) != cudaSuccess) return -1;
     DevBatch gd = group_dev(b, g);
+    n += launch_integrals(gd, st);  // the group's shell pairs only
     launch_scc(gd, b->precision, st);
     n += 1 + launch_grad_pairs(gd, st);
     launch_grad_atoms(gd, st);
