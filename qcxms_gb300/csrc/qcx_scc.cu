@@ -1733,7 +1733,12 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   // start from zero moments (the reference's fresh wavefunction), or, when the
   // caller asked for it, from the converged output moments of the previous
   // geometry of this trajectory (still in xout)
-  const bool warm_guess = bt.guess == 1 && bt.have_prev != nullptr && bt.have_prev[mol] != 0;
+  const bool warm_guess = bt.guess == 1 && bt.have_prev != nullptr && (bt.have_prev[mol] & 1) != 0;
+  // bit 1 of have_prev: the first-iteration FP32 eigenvectors of the previous SCC
+  // of this molecule are kept (after the three FP32 dipole matrices in the kD32 slots)
+  float* B32 = D32 + 3 * nn;
+  const bool basis_kept = MIXED && bt.have_prev != nullptr && (bt.have_prev[mol] & 2) != 0;
+  bool basis_saved = false;
   for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = warm_guess ? xout[i] : 0.0;
   __syncthreads();
 
@@ -1846,7 +1851,40 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     // Jacobi rotations update C^T in place.
     if (fp32_phase) {
       // ---- FP32 iteration ----
-      if (!have32) {
+      // First FP32 iteration: start the eigensolve from the kept eigenvectors of
+      // the previous geometry, re-orthonormalised in the new overlap (two
+      // Newton-Schulz steps), when they are close to orthonormal there; the
+      // sweeps then converge to the same tolerance as from scratch, in fewer sweeps.
+      bool seeded = false;
+      if (!have32 && basis_kept) {
+        for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+          int r = e / np, c = e - r * np;
+          JV32[e] = (r < n && c < n) ? B32[r * n + c] : (r == c ? 1.f : 0.f);
+        }
+        __syncthreads();
+        float* C32 = (float*)C;
+        for (int st = 0; st < 2; ++st) {
+          cta_gemm<float, float, float, float>(n, n, n, S32, n, false, JV32, np, true, T32, n);
+          __syncthreads();
+          cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, T32, n, false, C32, n);
+          __syncthreads();
+          float em = 0.f;
+          for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            int i = e / n, j = e - i * n;
+            float d = C32[e] - (i == j ? 1.f : 0.f);
+            em = fmaxf(em, fabsf(d));
+            C32[e] = (i == j ? 1.f : 0.f) - 0.5f * d;
+          }
+          const double emax = cta_max((double)em, sh.red);
+          if (st == 0 && !(emax < 0.25)) break;  // too far from the new metric: start from scratch
+          cta_gemm<float, float, float, float>(n, n, n, C32, n, false, JV32, np, false, T32, n);
+          __syncthreads();
+          for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV32[(e / n) * np + (e % n)] = T32[e];
+          __syncthreads();
+          if (st == 1) seeded = true;
+        }
+      }
+      if (!have32 && !seeded) {
         cta_gemm<float, float, float, float>(n, n, n, (const float*)F, n, false, X32, n, false, T32, n);
         __syncthreads();
         cta_gemm<float, float, float, float>(n, n, n, X32, n, true, T32, n, false, JA32, np);
@@ -1887,17 +1925,25 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       // the first (cold) solve only seeds the FP32 iterations: it stops at a
       // looser tolerance, the warm sweeps and refinements of later iterations
       // take the basis further
-      if (!ok32) jacobi<float>(JA32, JV32, n, have32, have32 ? 2e-6 : QCX_JAC32_COLD_TOL, sh,
+      if (!ok32) jacobi<float>(JA32, JV32, n, have32 || seeded, have32 ? 2e-6 : QCX_JAC32_COLD_TOL, sh,
                                have32 ? QCX_JAC32_WARM_SWEEPS : 30);
 #ifdef QCX_SCC_PHASE_TIMING
       if (threadIdx.x == 0) atomicAdd(&g_phase_cycles[ok32 ? 13 : 14], 1ull);
 #endif
       PHASE_MARK(3);
       if (!have32) {
-        // eigenvectors of X^T F X -> C^T = V X^T
-        cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, X32, n, true, T32, n);
-        __syncthreads();
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV32[(e / n) * np + (e % n)] = T32[e];
+        if (!seeded) {
+          // eigenvectors of X^T F X -> C^T = V X^T
+          cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, X32, n, true, T32, n);
+          __syncthreads();
+          for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV32[(e / n) * np + (e % n)] = T32[e];
+          __syncthreads();
+        }
+        // keep this first-iteration basis for the next geometry
+        if (bt.have_prev) {
+          for (int e = threadIdx.x; e < n * n; e += blockDim.x) B32[e] = JV32[(e / n) * np + (e % n)];
+          basis_saved = true;
+        }
         have32 = true;
       }
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -2272,7 +2318,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     if (eig_fail) st |= kEigenNotConverged;
     if (!isfinite(eel)) st |= kNonFinite;
     bt.status[mol] = st;
-    if (bt.have_prev) bt.have_prev[mol] = st == 0 ? 1 : 0;
+    if (bt.have_prev) bt.have_prev[mol] = (st == 0 ? 1 : 0) | (basis_saved ? 2 : 0);
     bt.iters[mol] = it;
   }
 }
