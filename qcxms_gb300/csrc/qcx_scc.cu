@@ -856,7 +856,7 @@ __device__ __forceinline__ float chol_solve_lane(const float (&row)[NM], float b
 }
 
 template <int NM>
-__device__ void spd_solve_warp(const double* M, double* rhs, int k) {
+__device__ __noinline__ void spd_solve_warp(const double* M, double* rhs, int k) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   float row[NM];
@@ -918,10 +918,16 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
   int k = it < nmem ? it : nmem;
   double* dfm = df + (long long)m * len;
   double* um = u + (long long)m * len;
+  // the residual f and the new difference vector are read by every dot product
+  // below: keep them in shared memory (the moment scratch holds 10 n >= len
+  // doubles; the second vector only when both fit)
+  double* fs = sh.mom;
+  double* ds = 2 * len <= 10 * mv.md.nao ? sh.mom + len : nullptr;
   double nrm[1] = {0.0};
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
     double f = xout[i] - x[i];
     double d = f - fl[i];
+    fs[i] = f;
     dfm[i] = d;
     nrm[0] += d * d;
   }
@@ -929,18 +935,22 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
   double nr = sqrt(nrm[0]);
   if (nr < 1e-300) nr = 1e-300;
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
-    dfm[i] /= nr;
-    um[i] = alpha * dfm[i] + (x[i] - xl[i]) / nr;
+    const double d = dfm[i] / nr;
+    dfm[i] = d;
+    if (ds) ds[i] = d;
+    um[i] = alpha * d + (x[i] - xl[i]) / nr;
   }
   __syncthreads();
+  const double* dv = ds ? ds : dfm;
   // a[j][m] = df_j . df_m ; c_j = df_j . f   (one warp per j)
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = w; j < k; j += kWarps) {
     const double* dfj = df + (long long)j * len;
     double s1 = 0.0, s2 = 0.0;
     for (int i = lane; i < len; i += 32) {
-      s1 += dfj[i] * dfm[i];
-      s2 += dfj[i] * (xout[i] - x[i]);
+      const double dj = dfj[i];
+      s1 += dj * dv[i];
+      s2 += dj * fs[i];
     }
     s1 = warp_sum(s1);
     s2 = warp_sum(s2);
@@ -1016,7 +1026,7 @@ __device__ void broyden(const MolView& mv, double* x, const double* xout, int it
   }
   __syncthreads();
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
-    double f = xout[i] - x[i];
+    double f = fs[i];
     double s = 0.0;
     for (int j = 0; j < k; ++j) s += rhs[j] * u[(long long)j * len + i];
     xl[i] = x[i];
