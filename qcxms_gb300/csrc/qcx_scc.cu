@@ -18,6 +18,11 @@ namespace qcx {
 #ifndef QCX_JAC32_WARM_SWEEPS
 #define QCX_JAC32_WARM_SWEEPS 1
 #endif
+// FP32 warm sweeps skip rotations between orbitals on the same side of the
+// Fermi level (beyond 25 kT) while the moment residual is above 1e-3
+#ifndef QCX_JAC32_OCC_FILTER
+#define QCX_JAC32_OCC_FILTER 0
+#endif
 #ifndef QCX_JAC32_COLD_TOL
 #define QCX_JAC32_COLD_TOL 2e-6
 #endif
@@ -421,7 +426,8 @@ __device__ __forceinline__ bool nonzero(double s) { return __double_as_longlong(
 // Returns the number of sweeps, or -1 if max_sweeps were not enough.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& sh, int max_sweeps) {
+__device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& sh, int max_sweeps,
+                                     double mu = 0.0, double occ_gap = -1.0) {
   const int np = n + (n & 1);
   const int half = np / 2;
   const int m = np - 1;
@@ -588,7 +594,14 @@ __device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double relto
         T aa = apq < T(0) ? -apq : apq;
         offmax = aa > offmax ? aa : offmax;
         T c = 1, s = 0;
-        if (aa > tiny) {
+        bool rot = aa > tiny;
+        if (rot && occ_gap > 0.0) {
+          // both orbitals fully occupied or both empty: the rotation cannot change
+          // the density, skip it (the caller only asks for this far from convergence)
+          const T ep = A[p * np + p] - (T)mu, eq = A[q * np + q] - (T)mu, g = (T)occ_gap;
+          rot = !((ep > g && eq > g) || (ep < -g && eq < -g));
+        }
+        if (rot) {
           T app = A[p * np + p], aqq = A[q * np + q];
           T theta = (aqq - app) / (T(2) * apq);
           T at = theta < T(0) ? -theta : theta;
@@ -1605,10 +1618,14 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   // FP64 Jacobi storage: shared memory when it fits, else the A / V slots.
   double* JA = (mode <= 1) ? sh.jac : Ag;
   double* JV = (mode == 0) ? sh.jac + (long long)np * np : Vg;
-  // FP32 storage (mixed): both matrices inside the FP64 A region; X32 and the
-  // FP32 coefficients live in the W and C slots until the FP64 phase.
-  float* JA32 = (float*)JA;
-  float* JV32 = (float*)JA + (long long)np * np;
+  // FP32 storage (mixed): both matrices inside the FP64 A region (shared
+  // memory up to mode 1). When the FP64 A does not fit (mode 2) but the FP32 A
+  // does, the FP32 A goes to shared memory and the FP32 coefficient rows to the
+  // A slot (which the finishing iterations overwrite only after copying them).
+  const bool a32_shared =
+      mode == 2 && scc_fixed_bytes(n) + sizeof(float) * (size_t)np * np <= (size_t)bt.smem_bytes;
+  float* JA32 = a32_shared ? (float*)sh.jac : (float*)JA;
+  float* JV32 = a32_shared ? (float*)Ag : (float*)JA + (long long)np * np;
   float* T32 = (float*)T;
   float* X32 = (float*)Wm;
 
@@ -1763,6 +1780,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   int stall32 = 0;
   int backoff32 = 0;    // FP32 iterations left before the next refinement attempt
   int n64 = 0;          // FP64 iterations done
+  double last_res = 1.0;  // moment residual of the previous iteration
   PHASE_BEGIN();
 #ifdef QCX_SCC_PHASE_TIMING
   long long _t_start = clock64();
@@ -1935,8 +1953,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       // the first (cold) solve only seeds the FP32 iterations: it stops at a
       // looser tolerance, the warm sweeps and refinements of later iterations
       // take the basis further
+      const bool occ_filter = QCX_JAC32_OCC_FILTER && have32 && last_res > 1e-3;
       if (!ok32) jacobi<float>(JA32, JV32, n, have32 || seeded, have32 ? 2e-6 : QCX_JAC32_COLD_TOL, sh,
-                               have32 ? QCX_JAC32_WARM_SWEEPS : 30);
+                               have32 ? QCX_JAC32_WARM_SWEEPS : 30, efermi, occ_filter ? 25.0 * md.kT : -1.0);
 #ifdef QCX_SCC_PHASE_TIMING
       if (threadIdx.x == 0) atomicAdd(&g_phase_cycles[ok32 ? 13 : 14], 1ull);
 #endif
@@ -2253,6 +2272,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       cta_sum<2>(acc, sh.red);
       eband = acc[0];
       double res = sqrt(acc[1] / len);
+      last_res = res;
       eel = eband + en[0] + en[1] + en[2] + en[3] + en[4] + ets;
       double de = fabs(eel - eprev);
       eprev = eel;

@@ -90,3 +90,27 @@ def test_cid_md_mixed_vs_fp64(gpu):
     assert ok.sum() >= 2
     assert np.all(np.isfinite(out["mixed"]["energy"]))
     assert np.abs(out["fp64"]["energy"] - out["mixed"]["energy"])[ok].max() < 1e-5
+
+
+def test_large_molecules_mixed_vs_fp64(gpu):
+    """Molecules of 75-85 atoms (about 170-210 atomic orbitals): their FP64 Jacobi
+    matrices no longer fit in shared memory, the FP32 ones partly do."""
+    mols = []
+    for s, n in enumerate([75, 85]):
+        Z, xyz = molgen.random_chno(n, 7100 + s)
+        mols.append({"Z": Z, "xyz": xyz, "charge": 1})
+    out = {}
+    for prec in ("fp64", "mixed"):
+        b = qg.Batch(mols)
+        b.set_precision(prec)
+        b.egrad()
+        out[prec] = b.get()
+        out[prec]["nao"] = b.sizes()[0]
+    assert (out["mixed"]["nao"] > 162).all()
+    ok = (out["fp64"]["status"] == 0) & (out["mixed"]["status"] == 0)
+    assert ok.any()
+    assert np.abs(out["fp64"]["energy"] - out["mixed"]["energy"])[ok].max() < 1e-6
+    ga = b.split(out["fp64"]["grad"])
+    gb = b.split(out["mixed"]["grad"])
+    for i in np.nonzero(ok)[0]:
+        assert np.abs(ga[i] - gb[i]).max() < 1e-5
