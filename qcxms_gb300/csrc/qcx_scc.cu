@@ -18,11 +18,6 @@ namespace qcx {
 #ifndef QCX_JAC32_WARM_SWEEPS
 #define QCX_JAC32_WARM_SWEEPS 1
 #endif
-// FP32 warm sweeps skip rotations between orbitals on the same side of the
-// Fermi level (beyond 25 kT) while the moment residual is above 1e-3
-#ifndef QCX_JAC32_OCC_FILTER
-#define QCX_JAC32_OCC_FILTER 0
-#endif
 #ifndef QCX_JAC32_COLD_TOL
 #define QCX_JAC32_COLD_TOL 2e-6
 #endif
@@ -426,8 +421,7 @@ __device__ __forceinline__ bool nonzero(double s) { return __double_as_longlong(
 // Returns the number of sweeps, or -1 if max_sweeps were not enough.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& sh, int max_sweeps,
-                                     double mu = 0.0, double occ_gap = -1.0) {
+__device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double reltol, SccShared& sh, int max_sweeps) {
   const int np = n + (n & 1);
   const int half = np / 2;
   const int m = np - 1;
@@ -594,14 +588,7 @@ __device__ QCX_JAC_INLINE int jacobi(T* A, T* Vt, int n, bool warm, double relto
         T aa = apq < T(0) ? -apq : apq;
         offmax = aa > offmax ? aa : offmax;
         T c = 1, s = 0;
-        bool rot = aa > tiny;
-        if (rot && occ_gap > 0.0) {
-          // both orbitals fully occupied or both empty: the rotation cannot change
-          // the density, skip it (the caller only asks for this far from convergence)
-          const T ep = A[p * np + p] - (T)mu, eq = A[q * np + q] - (T)mu, g = (T)occ_gap;
-          rot = !((ep > g && eq > g) || (ep < -g && eq < -g));
-        }
-        if (rot) {
+        if (aa > tiny) {
           T app = A[p * np + p], aqq = A[q * np + q];
           T theta = (aqq - app) / (T(2) * apq);
           T at = theta < T(0) ? -theta : theta;
@@ -1780,7 +1767,6 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   int stall32 = 0;
   int backoff32 = 0;    // FP32 iterations left before the next refinement attempt
   int n64 = 0;          // FP64 iterations done
-  double last_res = 1.0;  // moment residual of the previous iteration
   PHASE_BEGIN();
 #ifdef QCX_SCC_PHASE_TIMING
   long long _t_start = clock64();
@@ -1953,9 +1939,8 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       // the first (cold) solve only seeds the FP32 iterations: it stops at a
       // looser tolerance, the warm sweeps and refinements of later iterations
       // take the basis further
-      const bool occ_filter = QCX_JAC32_OCC_FILTER && have32 && last_res > 1e-3;
       if (!ok32) jacobi<float>(JA32, JV32, n, have32 || seeded, have32 ? 2e-6 : QCX_JAC32_COLD_TOL, sh,
-                               have32 ? QCX_JAC32_WARM_SWEEPS : 30, efermi, occ_filter ? 25.0 * md.kT : -1.0);
+                               have32 ? QCX_JAC32_WARM_SWEEPS : 30);
 #ifdef QCX_SCC_PHASE_TIMING
       if (threadIdx.x == 0) atomicAdd(&g_phase_cycles[ok32 ? 13 : 14], 1ull);
 #endif
@@ -2272,7 +2257,6 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       cta_sum<2>(acc, sh.red);
       eband = acc[0];
       double res = sqrt(acc[1] / len);
-      last_res = res;
       eel = eband + en[0] + en[1] + en[2] + en[3] + en[4] + ets;
       double de = fabs(eel - eprev);
       eprev = eel;
