@@ -6,7 +6,10 @@
 //
 // Generalized eigenproblem F C = S C e: S = L L^T (Cholesky, once per
 // geometry), X = L^-T, A = X^T F X, cyclic parallel Jacobi on A (round-robin
-// pair ordering, n/2 disjoint rotations per round), C = X V.
+// pair ordering, n/2 disjoint rotations per round), C = X V. Later iterations
+// refine the previous coefficients: B = C^T F C is nearly diagonal, and a
+// first-order (GEMM) refinement, exact rotations of hard pairs, or a warm
+// Jacobi sweep on B updates them.
 #include <cfloat>
 #include <type_traits>
 
@@ -1538,11 +1541,14 @@ __device__ void dd_density(const DDMats& d, int n, int nocc, const int* perm, co
 // the SCC kernel
 //
 // MIXED = 0: every iteration in FP64.
-// MIXED = 1: iterations run the transforms, the Jacobi eigensolve and the
-//   density in FP32 until the moment residual drops below kMixedSwitch; the
-//   remaining iterations (and always the final one) are FP64, warm-started
-//   from the FP32 eigenvectors after one Newton-Schulz re-orthonormalisation.
-//   Potentials, Fermi level, moments, Broyden and energies are FP64 always.
+// MIXED = 1: iterations run the Fock build, potentials, transforms, the
+//   Jacobi eigensolve, Fermi level, density and moments in FP32 until the
+//   moment residual drops below kMixedSwitch; the remaining iterations (at
+//   least two, and always the final one) keep the coefficient rows and their
+//   O(n^3) products in double-float (hi + lo FP32), warm-started from the FP32
+//   eigenvectors after two Newton-Schulz re-orthonormalisations. The Fock
+//   build, potentials, moments, Fermi level, energies of those iterations and
+//   the Broyden mixing are FP64.
 // ---------------------------------------------------------------------------
 constexpr double kMixedSwitch = QCX_MIXED_SWITCH;
 
