@@ -363,6 +363,63 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_fragip(args):
+    """Fragment IPs at trajectory ends (src/analyse.f90:13-467, GFN2): 256
+    structures that fell into 2-5 fragments (molgen.fragmented), the neutral
+    and cation of every fragment in one batch per call of qcx_fragment_ips.
+    Every call goes through the C ABI with host buffers (batch set-up, copies,
+    kernels, results), so the value is end to end. One GPU (replicas only)."""
+    import qcxms_gb300 as qg
+    from qcxms_gb300 import molgen
+    n = args.ntraj or NTRAJ
+    structs = [molgen.fragmented(s, 2 + s % 4) for s in range(n)]
+    prec = 1 if args.precision == "mixed" else 0
+    nfrag = sum(int(np.max(s["frag"])) for s in structs)
+    # single points on the GPU: neutral and cation of every fragment, less the
+    # bare protons (no electrons: self energy on the host); their coordinates
+    # go in and their energies and status words come out every call
+    nsp = h2d = 0
+    for s in structs:
+        for f in range(1, int(np.max(s["frag"])) + 1):
+            na = int(np.sum(s["frag"] == f))
+            lone_h = na == 1 and int(s["Z"][s["frag"] == f][0]) == 1
+            nsp += 1 if lone_h else 2
+            h2d += (1 if lone_h else 2) * (24 * na + 4 * na)
+    d2h = 12 * nsp
+    for _ in range(args.warmup):
+        qg.fragment_ips(structs, 1, precision=prec)
+    ts = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            ip, ef, ok = qg.fragment_ips(structs, 1, precision=prec)
+            ts.append(time.perf_counter() - t0)
+    el = sum(ts)
+    value = n * args.steps / el
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        done, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < 10.0 and done < n:
+            s = structs[done]
+            oracle.fragment_ips(s["Z"], s["xyz"], s["frag"], 1)
+            done += 1
+        cel = time.perf_counter() - t0
+        cpu = {"value": done / cel, "unit": "structures/s", "cores": 1, "kind": "port",
+               "sample": "first %d of the %d structures (%.1f s), CPU FP64 restatement, one thread" % (done, n, cel)}
+    line = {"metric": "fragment-IP structures/s", "value": value, "unit": "structures/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == 0 else "f64/f32", "data": "synthetic",
+            "config": {"workload": "%d fragmented C/H/N/O structures, 2-5 fragments, neutral + cation per "
+                                   "fragment, 300 K" % n, "fragments": nfrag, "gpu_single_points": nsp,
+                       "precision": args.precision, "ipok_fraction": float(np.mean(ok)),
+                       "l2": "inputs copied from host every call (batch built per call)"},
+            "e2e": {"value": value, "unit": "structures/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "clocks": clk.summary(), "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -372,7 +429,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ntraj", type=int, default=None, help="smaller batch for profiling runs (default 256)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "cid"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "cid", "fragip"])
     ap.add_argument("--no-plain", action="store_true", help="skip the single-trajectory FP64 reference leg")
     ap.add_argument("--guess", default="zero", choices=["zero", "previous"],
                     help="SCC start: zero moments every step (the reference's behaviour, default) or the "
@@ -380,6 +437,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "fragip":
+        run_fragip(args)
     else:
         run_gpu(args)
 

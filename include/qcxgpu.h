@@ -153,6 +153,44 @@ int qcx_batch_profile_egrad(qcx_batch* b, float* ms);
 int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat);
 
 /*
+ * Fragment ionisation potentials (electron affinities for mchrg < 0) of ntraj
+ * fragmented structures, all single points in one batch: the GFN2 path of
+ * analyse (src/analyse.f90:13-467) that write_fragments
+ * (src/write_fragments.f90:100-106) calls when a trajectory ends. nat[ntraj],
+ * num and xyz ([natom][3], Bohr) of all trajectories concatenated, frag[natom]
+ * the 1-based fragment number of every atom (qcx_batch_fragments, or
+ * fragment_structure, src/fragments.f90:93-182), 1..nfrag without gaps,
+ * nfrag <= QCX_MAX_FRAGMENTS. Each fragment keeps its atoms in their original
+ * order (avg_frag_struc, src/analyse.f90:471-503); its neutral and its ions of
+ * charge sign(mchrg)*1..|mchrg| are evaluated at etemp (analyse uses 300 K for
+ * GFN2, src/analyse.f90:244-248), spin-restricted as eqm/get_xtb_egrad do. A
+ * fragment left without electrons gets the self energy of eself
+ * (src/iniqm.f90:430-450). Outputs, per trajectory t:
+ *   fragip[t][i][c-1] = (E(charge c) - E(neutral)) * 27.21138505 eV for
+ *     fragment i < nfrag and c = 1..|mchrg| (src/analyse.f90:367-368), 0 where
+ *     an energy is 0 or for trajectories with one fragment;
+ *   efrag[t][i][c] (may be NULL): the energies (Eh), c = 0 the neutral;
+ *   ipok[t]: 0 if any of its calculations failed (SCC not converged, |E| <
+ *     1e-10, src/iniqm.f90:415-421; more charge than valence electrons) or an
+ *     IP lies outside the bounds of src/analyse.f90:386-403, else 1.
+ * precision: QCX_PRECISION_FP64 or QCX_PRECISION_MIXED. Returns 0, 5 (method
+ * not GFN2) or -1 (invalid input, CUDA error).
+ */
+#define QCX_MAX_FRAGMENTS 10
+#define QCX_FRAGIP_MAX_CHARGE 4
+int qcx_fragment_ips(int method, int ntraj, const int32_t* nat, const int32_t* num, const double* xyz,
+                     const int32_t* frag, int mchrg, double etemp, int precision, double* fragip, double* efrag,
+                     int32_t* ipok);
+
+/*
+ * Boltzmann weights of fragment IPs, boltz (src/utility.f90:469-498):
+ * fragchrg2(i,j) = exp(-ip(i,j)/f) / sum exp(-ip/f), f = temp * kB * (627.50947428
+ * for units 1, kcal/mol; 27.21138505 for units 2, eV). ip and fragchrg2 are
+ * Fortran arrays (nfrag, mchrg): element (i,j) at [i + j*nfrag], 0-based.
+ */
+int qcx_boltz(int units, int nfrag, int mchrg, double temp, const double* ip, double* fragchrg2);
+
+/*
  * Allocation-free variant of qcx_egrad for callers that cannot call
  * cudaMalloc (for example a host program whose device memory belongs to
  * another runtime's capped pool, or a path that must not trigger the device

@@ -60,6 +60,8 @@ def lib():
         _lib.qcxo_checkqc.restype = ctypes.c_int
         _lib.qcxo_fragments.restype = ctypes.c_int
         _lib.qcxo_md_batch.restype = ctypes.c_int
+        _lib.qcxo_eself.restype = ctypes.c_double
+        _lib.qcxo_nel.restype = ctypes.c_int
     return _lib
 
 
@@ -146,6 +148,85 @@ def leapfrog(grad, mass, tstep, xyz, vel):
 def getspin(Z, charge):
     Z = np.ascontiguousarray(Z, dtype=np.int32)
     return lib().qcxo_getspin(len(Z), _p(Z, ctypes.c_int), int(charge))
+
+
+AUTOEV = 27.21138505  # src/xtb_mctc_convert.f90:27
+AUTOKCAL = 627.50947428  # src/xtb_mctc_convert.f90:30
+KB = 3.166808578545117e-06  # src/xtb_mctc_constants.f90:35
+
+
+def eself(Z):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    return lib().qcxo_eself(len(Z), _p(Z, ctypes.c_int))
+
+
+def nel(Z, charge):
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    return lib().qcxo_nel(len(Z), _p(Z, ctypes.c_int), int(charge))
+
+
+def fragment_ips(Z, xyz, frag, mchrg=1, etemp=300.0, opts=None, iterations=False):
+    """IPs/EAs of the fragments of one structure, restating the GFN2 path of
+    analyse (src/analyse.f90:13-467) with eqm (src/iniqm.f90:241-427).
+
+    Returns (fragip (nfrag, |mchrg|) in eV, energies (nfrag, |mchrg|+1) in Eh,
+    ipok), plus the largest SCC iteration count of its single points when
+    ``iterations`` is set."""
+    Z = np.asarray(Z, dtype=np.int32)
+    xyz = np.asarray(xyz, dtype=np.float64).reshape(len(Z), 3)
+    frag = np.asarray(frag)
+    nfrag = int(frag.max())
+    nch = abs(mchrg)
+    fragip = np.zeros((nfrag, nch))
+    E = np.zeros((nfrag, nch + 1))
+    ipok = True
+    maxit = 0
+    if nfrag < 2:  # src/analyse.f90:137-142
+        return (fragip, E, ipok, maxit) if iterations else (fragip, E, ipok)
+    for i in range(nfrag):
+        # avg_frag_struc (src/analyse.f90:471-503): atoms of fragment i in their order
+        sel = np.nonzero(frag == i + 1)[0]
+        Zf, xf = Z[sel], xyz[sel]
+        for c in range(nch + 1):
+            ch = c if mchrg > 0 else -c
+            ne = nel(Zf, ch)
+            if ne == 0:
+                E[i, c] = eself(Zf)
+            elif ne > 0:
+                rc, e, g, q, info = egrad(Zf, xf, ch, kT=etemp * KB, opts=opts)
+                E[i, c] = e if rc == 0 else 0.0
+                maxit = max(maxit, info["iterations"])
+            if abs(E[i, c]) < 1e-10:  # src/iniqm.f90:415-421
+                ipok = False
+        for c in range(1, nch + 1):
+            if E[i, c] != 0 and E[i, 0] != 0:  # src/analyse.f90:367-403
+                ip = (E[i, c] - E[i, 0]) * AUTOEV
+                fragip[i, c - 1] = ip
+                if mchrg < 0:
+                    bad = ip > 40.0 or ip < -35.0
+                elif mchrg == 1:
+                    bad = ip < 0.0 or ip > 50.0
+                else:
+                    bad = ip < 0.0 or ip > 100.0
+                if bad:
+                    ipok = False
+    return (fragip, E, ipok, maxit) if iterations else (fragip, E, ipok)
+
+
+def boltz(units, temp, ip):
+    """boltz (src/utility.f90:469-498), loop for loop."""
+    const = AUTOKCAL if units == 1 else AUTOEV
+    f = temp * KB * const
+    nfrag, mchrg = ip.shape
+    esum = 0.0
+    for i in range(nfrag):
+        for j in range(mchrg):
+            esum = esum + np.exp(-ip[i, j] / f)
+    out = np.zeros_like(ip)
+    for i in range(nfrag):
+        for j in range(mchrg):
+            out[i, j] = np.exp(-ip[i, j] / f) / esum
+    return out
 
 
 def gnorm(grad):

@@ -1292,6 +1292,25 @@ void qcxo_ekinet(int nat, const double* vel, const double* mass, double* ekin, d
 }
 
 /* src/utility.f90:449-464 */
+/* eself (src/iniqm.f90:430-450): energy of atoms without electrons,
+ * sum of z^2/2 * gam + z^3/3 * gam3 with z = valence electrons; gam, gam3 are
+ * the atomic hardness and third-order parameter (first shell of this set). */
+double qcxo_eself(int nat, const int* Z) {
+  double e = 0.0;
+  for (int a = 0; a < nat; ++a) {
+    double z = qcx_nvalence[Z[a]];
+    e = e + 0.5 * z * z * qcx_sh_hardness[Z[a]][0] + z * z * z * qcx_sh_gamma3[Z[a]][0] / 3.0;
+  }
+  return e;
+}
+
+/* valence electrons minus charge, electrons_amount (src/iniqm.f90:45-63) */
+int qcxo_nel(int nat, const int* Z, int charge) {
+  int n = 0;
+  for (int a = 0; a < nat; ++a) n += (int)qcx_nvalence[Z[a]];
+  return n - charge;
+}
+
 int qcxo_getspin(int nat, const int* Z, int charge) {
   int j = 0;
   for (int a = 0; a < nat; ++a) j += Z[a];

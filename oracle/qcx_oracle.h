@@ -67,6 +67,8 @@ void qcxo_leapfrog(int nat, const double* grad, const double* mass, double tstep
                    double* xyz, double* vel, double* ke);
 void qcxo_ekinet(int nat, const double* vel, const double* mass, double* ekin, double* temp);
 int qcxo_getspin(int nat, const int* Z, int charge);
+double qcxo_eself(int nat, const int* Z);
+int qcxo_nel(int nat, const int* Z, int charge);
 double qcxo_gnorm(int nat, const double* grad);
 int qcxo_checkqc(int nat, double* e, const double* grad, const double* qat, int charge);
 

@@ -11,6 +11,9 @@ ctypes and mirrors the reference's Fortran interface:
 * :class:`Batch` -- many trajectories advanced together (leapfrog of
   ``src/md.f90:749-773`` followed by the energy/gradient call, as in the MD
   loop at ``src/md.f90:390-396``).
+* :func:`fragment_ips` / :func:`boltz` -- the GFN2 fragment IPs of ``analyse``
+  (``src/analyse.f90:13-467``) for many fragmented structures in one batch,
+  and ``boltz`` (``src/utility.f90:469-498``).
 
 There is no CPU fallback: if the CUDA library cannot be loaded, every call
 raises.
@@ -22,7 +25,8 @@ import numpy as np
 
 from . import constants
 
-__all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "load_library", "library_path",
+__all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "fragment_ips", "boltz", "load_library",
+           "library_path",
            "STATUS_SCC_NOT_CONVERGED", "STATUS_NON_FINITE", "STATUS_CHOLESKY_FAILED", "STATUS_EIGEN_NOT_CONVERGED"]
 
 # method selectors, src/tblite.f90:34-40
@@ -84,6 +88,10 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_stream.argtypes = [ctypes.c_void_p]
     lib.qcx_batch_profile_egrad.argtypes = [ctypes.c_void_p, P(ctypes.c_float)]
     lib.qcx_batch_get_sizes.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32)]
+    lib.qcx_fragment_ips.argtypes = [c_int, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double),
+                                     P(ctypes.c_int32), c_int, c_double, c_int, P(c_double), P(c_double),
+                                     P(ctypes.c_int32)]
+    lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
     _lib = lib
     return lib
 
@@ -120,6 +128,49 @@ def get_xtb_egrad(num, xyz, charge, multiplicity, method=gfn2_xtb, etemp=300.0, 
         with open(output_file, "w") as f:
             f.write("qcxgpu GFN2-xTB energy %.12f Eh stat %d %s\n" % (e[0], stat, _err(lib) if stat else ""))
     return q, float(e[0]), g, int(stat)
+
+
+MAX_FRAGMENTS = 10
+
+
+def fragment_ips(structs, mchrg=1, etemp=300.0, precision=0, method=gfn2_xtb):
+    """Fragment IPs (EAs for ``mchrg`` < 0) of fragmented structures in one batch.
+
+    Mirrors the GFN2 path of ``analyse`` (``src/analyse.f90:13-467``):
+    ``structs`` is a list of dicts with ``Z``, ``xyz`` (Bohr) and ``frag``
+    (1-based fragment number per atom). Returns ``(fragip, efrag, ipok)``:
+    ``fragip[t]`` is an ``(nfrag, |mchrg|)`` array in eV, ``efrag[t]`` the
+    ``(nfrag, |mchrg|+1)`` energies in Eh (column 0 the neutral) and ``ipok[t]``
+    a bool. Raises on invalid input or a CUDA error.
+    """
+    lib = load_library()
+    nch = abs(int(mchrg))
+    nat = np.array([len(s["Z"]) for s in structs], dtype=np.int32)
+    Z = np.ascontiguousarray(np.concatenate([np.asarray(s["Z"]) for s in structs]), dtype=np.int32)
+    xyz = np.ascontiguousarray(np.concatenate([np.asarray(s["xyz"], dtype=np.float64).reshape(-1, 3)
+                                               for s in structs]))
+    frag = np.ascontiguousarray(np.concatenate([np.asarray(s["frag"]) for s in structs]), dtype=np.int32)
+    ip = np.zeros((len(structs), MAX_FRAGMENTS, max(nch, 1)))
+    ef = np.zeros((len(structs), MAX_FRAGMENTS, max(nch, 1) + 1))
+    ok = np.zeros(len(structs), dtype=np.int32)
+    rc = lib.qcx_fragment_ips(int(method), len(structs), _ip(nat), _ip(Z), _dp(xyz), _ip(frag), int(mchrg),
+                              float(etemp), int(precision), _dp(ip), _dp(ef), _ip(ok))
+    if rc != 0:
+        raise RuntimeError("qcx_fragment_ips returned %d: %s" % (rc, _err(lib)))
+    nf = [int(np.max(s["frag"])) for s in structs]
+    return [ip[t, :nf[t]] for t in range(len(structs))], [ef[t, :nf[t]] for t in range(len(structs))], ok.astype(bool)
+
+
+def boltz(units, temp, ip):
+    """Boltzmann weights of an ``(nfrag, mchrg)`` IP array, ``boltz`` of
+    ``src/utility.f90:469-498`` (units 1: kcal/mol, 2: eV)."""
+    lib = load_library()
+    ip = np.asfortranarray(ip, dtype=np.float64)
+    out = np.zeros_like(ip, order="F")
+    rc = lib.qcx_boltz(int(units), ip.shape[0], ip.shape[1], float(temp), _dp(ip), _dp(out))
+    if rc != 0:
+        raise RuntimeError("qcx_boltz: %s" % _err(lib))
+    return out
 
 
 class Batch:

@@ -406,6 +406,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   d.max_nao = b->max_nao;
   d.smem_bytes = (int)scc_smem_bytes(b->max_nao, 0);
   d.max_iter = QCX_SCC_MAXITER;
+  d.mixed_min_nao = 0;
   d.econv = QCX_SCC_ECONV;
   d.pconv = QCX_SCC_PCONV;
   d.mix_alpha = QCX_BROYDEN_ALPHA;
@@ -422,6 +423,12 @@ int check_launch() {
 }
 
 }  // namespace
+
+namespace qcx {
+// error text for qcx_last_error, set by the other translation units
+void set_last_error(const std::string& s) { set_error(s); }
+void batch_set_mixed_min_nao(qcx_batch* b, int n) { b->dev.mixed_min_nao = n; }
+}  // namespace qcx
 
 extern "C" {
 

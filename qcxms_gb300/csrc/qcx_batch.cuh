@@ -140,6 +140,7 @@ struct DevBatch {
   int smem_bytes;  // dynamic shared memory granted to the SCC kernel
   // SCC controls
   int max_iter;
+  int mixed_min_nao;  // mixed mode: molecules with fewer AOs run FP64 iterations only
   double econv, pconv, mix_alpha;
 };
 

@@ -2,7 +2,11 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "qcx_batch.cuh"
+
+struct qcx_batch;  // the batch handle of the C ABI (include/qcxgpu.h)
 
 namespace qcx {
 
@@ -18,6 +22,12 @@ void launch_zero_grad(const DevBatch& bt, cudaStream_t st);
 // fragment numbers of every molecule's atoms (frag[natom]) and fragment counts (nfrag[nmol])
 void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,
                       int* nfrag, cudaStream_t st);
+
+// sets the text qcx_last_error() returns
+void set_last_error(const std::string& s);
+// mixed mode: molecules with fewer atomic orbitals run FP64 SCC iterations only
+// (0 by default; set before the batch's first evaluation)
+void batch_set_mixed_min_nao(::qcx_batch* b, int n);
 
 // dynamic shared memory the SCC kernel asks for, given the largest molecule
 size_t scc_smem_bytes(int max_nao, int precision);

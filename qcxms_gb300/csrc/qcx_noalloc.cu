@@ -312,6 +312,7 @@ extern "C" int qcx_egrad_noalloc(int method, int nat, const int32_t* num, const 
   d.max_nao = nao;
   d.smem_bytes = (int)scc_smem_bytes(nao, 0);
   d.max_iter = QCX_SCC_MAXITER;
+  d.mixed_min_nao = 0;
   d.econv = QCX_SCC_ECONV;
   d.pconv = QCX_SCC_PCONV;
   d.mix_alpha = QCX_BROYDEN_ALPHA;

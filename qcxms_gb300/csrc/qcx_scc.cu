@@ -1765,7 +1765,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   double en[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   double eprev = 0.0, eel = 0.0, ets = 0.0, eband = 0.0, efermi = 0.0;
   int it, converged = 0, eig_fail = 0;
-  bool fp32_phase = MIXED != 0 && bt.max_iter > 8;
+  bool fp32_phase = MIXED != 0 && bt.max_iter > 8 && n >= bt.mixed_min_nao;
   bool have64 = false;  // JV holds an orthonormal FP64 basis from a previous iteration
   bool have32 = false;  // JV32 holds FP32 eigenvectors from a previous iteration
   int bro_it = 0;       // Broyden updates since the last (re)start of the mixer

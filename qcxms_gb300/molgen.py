@@ -143,3 +143,33 @@ def cid_workload(ntraj, nmin=10, nmax=80, seed0=0, e_lab_ev=40.0, bmax_aa=2.0, t
                      "mass": np.concatenate([m, [MASS_AU[AR_Z]]]), "charge": 1, "temp": temp,
                      "impact_parameter": b})
     return mols
+
+
+def fragmented(seed, nparts, spacing=25.0):
+    """A trajectory end that has fallen apart: nparts random C/H/N/O molecules
+    (3-12 atoms; a quarter of the parts lone H atoms) ``spacing`` Bohr apart,
+    atom order shuffled so that the fragments interleave. ``frag`` holds the
+    fragment numbers that fragment_structure (src/fragments.f90:93-182) gives
+    at rcut 3.0, at1 = 1: the first atom's part is fragment 1, the others
+    follow in the order of their lowest-numbered atom."""
+    rng = np.random.default_rng(seed)
+    Zs, xs, part = [], [], []
+    for k in range(nparts):
+        if rng.random() < 0.25:
+            Z, x = np.array([1]), np.zeros((1, 3))
+        else:
+            Z, x = random_chno(int(rng.integers(3, 13)), 1000 * seed + k)
+            x = np.asarray(x, dtype=np.float64).reshape(-1, 3)
+            x = x - x.mean(0)
+        Zs.append(np.asarray(Z))
+        xs.append(x + np.array([spacing * k, rng.normal() * 3.0, rng.normal() * 3.0]))
+        part += [k] * len(Z)
+    Z, xyz, part = np.concatenate(Zs), np.concatenate(xs), np.array(part)
+    perm = rng.permutation(len(Z))
+    Z, xyz, part = Z[perm], xyz[perm], part[perm]
+    number = {}
+    for p in part:
+        if p not in number:
+            number[p] = len(number) + 1
+    frag = np.array([number[p] for p in part], dtype=np.int32)
+    return {"Z": Z, "xyz": xyz, "frag": frag}
