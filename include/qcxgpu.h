@@ -136,6 +136,34 @@ int qcx_batch_get_progress(qcx_batch* b, int32_t* active, int64_t* steps_done);
  * atom, nfrag[nmol] the number of fragments; either may be NULL. */
 int qcx_batch_fragments(qcx_batch* b, double rcut, int at1, int at2, int32_t* frag, int32_t* nfrag);
 
+/*
+ * MD bookkeeping and exit rules of an electron-impact fragmentation run on the
+ * device (src/md.f90:285-682 with it > 0, isec = 1), evaluated after every step
+ * of qcx_batch_step inside the captured step graph: per trajectory the step
+ * count, the running mean temperature and total-energy error (exit when an
+ * energy evaluation failed or |Eerror| > 0.1 Eh, src/md.f90:316-342), fragment
+ * numbers at rcut 3.0 (src/md.f90:450) and the fragments' temperatures
+ * (intenergy, src/md.f90:715-741), and the exits: more than 6 fragments, more
+ * than nfragexit fragments, 2 or more fragments for over 1000 steps, nfragexit
+ * fragments for more than `more` further steps (the reference uses 250), and
+ * max_steps (src/md.f90:456-462, 620-679). A trajectory that exits stops (its
+ * active flag drops to 0). Call after qcx_batch_egrad of the start geometry:
+ * the first loop top uses that energy and the kinetic energy of the current
+ * velocities (ekinet, src/mdinit.f90:57-76). New coordinates through
+ * qcx_batch_set_state switch the rules off. Not covered: the electron-impact
+ * heating of the first steps (impactscale, setetemp; the electronic
+ * temperature stays fixed), the CID branch, the output-file averages.
+ */
+int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps);
+
+/* State of the MD rules per trajectory (any pointer may be NULL): nstep,
+ * nfrag (fragments at the last step), fragstate (1: exit on fragment count or
+ * step limit, 2: fragments constant for 1000 steps, 0 otherwise), mdok (1: the
+ * run counts), done (1: the run has ended), tav (sum of the step
+ * temperatures, K), eerror (Eh), fragT [nmol][10] (K). */
+int qcx_batch_get_md_state(qcx_batch* b, int32_t* nstep, int32_t* nfrag, int32_t* fragstate, int32_t* mdok,
+                           int32_t* done, double* tav, double* eerror, double* fragT);
+
 /* Synchronise the batch's stream. */
 int qcx_batch_sync(qcx_batch* b);
 

@@ -229,6 +229,94 @@ def boltz(units, temp, ip):
     return out
 
 
+FSTOAU = 41.3413733365614  # src/xtb_mctc_convert.f90:54
+
+
+def _temp(e, n):
+    """e / (0.5*3*n*kB) with 0.5*3*n in default (single) real (src/md.f90:289, 736)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return float(np.float64(e) / (float(np.float32(1.5) * np.float32(n)) * KB))
+
+
+def md_rules_top(s, epot, ekin, nuc):
+    """Top of the MD loop (src/md.f90:286-342), nadd = 0, it > 0, isec = 1."""
+    s["nstep"] += 1
+    t = _temp(ekin, nuc)
+    s["tav"] = s["tav"] + t
+    s["epav"] = s["epav"] + epot
+    s["ekav"] = s["ekav"] + ekin
+    s["edum"] = (s["edum"] + epot) + ekin
+    eav = s["edum"] / float(np.float32(s["nstep"]))
+    s["eerror"] = (eav - epot) - ekin
+    if s["nfrag"] == 1:
+        s["fragT"][0] = s["tav"] / s["nstep"]
+    if epot == 0 or abs(s["eerror"]) > float(np.float32(0.1)):
+        s["mdok"] = 1 if 1 < s["nfrag"] <= 4 else 0
+        s["done"] = 1
+        return True
+    return False
+
+
+def md_rules_begin(vel, mass, epot):
+    """State before the loop: ekinet (src/mdinit.f90:57-76) and the first top."""
+    s = {"nstep": 0, "nfrag": 1, "fconst": 0, "morestep": 0, "fragstate": 0, "mdok": 0, "done": 0, "tav": 0.0,
+         "epav": 0.0, "ekav": 0.0, "edum": 0.0, "eerror": 0.0, "ttime": 0.0, "dtime": 0.0, "fragT": [0.0] * 10}
+    ek = 0.0
+    for i in range(len(mass)):
+        v = vel[i]
+        ek = ek + mass[i] * ((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])
+    ek = ek * 0.5
+    if epot == 0:
+        s["done"] = 1  # src/md.f90:185
+    else:
+        md_rules_top(s, epot, ek, len(mass))
+    return s
+
+
+def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more, max_steps):
+    """Rest of one loop iteration after leapfrog + egrad (src/md.f90:426-679,
+    electron-impact branch), then the next top. epot = 0 for a failed call."""
+    if s["done"]:
+        return s
+    s["ttime"] = s["ttime"] + tstep / FSTOAU
+    if s["nfrag"] == 1:
+        s["morestep"] = 0
+    if s["nfrag"] > 1 and s["dtime"] < 1.0e-6:
+        s["dtime"] = s["ttime"] / 1000.0
+    s["nfrag"] = nfrag
+    if nfrag > 1:  # intenergy, src/md.f90:715-741
+        eint, cnt = [0.0] * 10, [0] * 10
+        for i in range(len(mass)):
+            j = frag[i] - 1
+            if j >= 10:
+                continue
+            v = vel[i]
+            eint[j] = eint[j] + (0.5 * mass[i]) * ((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])
+            cnt[j] += 1
+        for j in range(min(nfrag, 10)):
+            s["fragT"][j] = _temp(eint[j], cnt[j])
+    stop = False
+    if nfrag > 6:
+        stop = True
+    elif nfrag > nfragexit:
+        s["fragstate"], s["mdok"], stop = 1, 1, True
+    else:
+        s["fconst"] = s["fconst"] + 1 if nfrag >= 2 else 0
+        if s["fconst"] > 1000:
+            s["fragstate"], s["mdok"], stop = 2, 1, True
+        elif nfrag >= nfragexit:
+            s["morestep"] += 1
+            if s["morestep"] > more:
+                s["fragstate"], s["mdok"], stop = 1, 1, True
+    if not stop and s["nstep"] >= max_steps:
+        s["fragstate"], s["mdok"], stop = 1, 1, True
+    if stop:
+        s["done"] = 1
+    else:
+        md_rules_top(s, epot, ekin, len(mass))
+    return s
+
+
 def gnorm(grad):
     grad = np.ascontiguousarray(grad, dtype=np.float64)
     return lib().qcxo_gnorm(grad.shape[0], _p(grad))

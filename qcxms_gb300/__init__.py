@@ -91,6 +91,8 @@ def load_library(build_if_missing=True):
     lib.qcx_fragment_ips.argtypes = [c_int, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double),
                                      P(ctypes.c_int32), c_int, c_double, c_int, P(c_double), P(c_double),
                                      P(ctypes.c_int32)]
+    lib.qcx_batch_set_md_rules.argtypes = [ctypes.c_void_p, c_int, c_int, c_int]
+    lib.qcx_batch_get_md_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 5 + [P(c_double)] * 3
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
     _lib = lib
     return lib
@@ -267,6 +269,23 @@ class Batch:
         self._check(self._lib.qcx_batch_fragments(self._h, float(rcut), int(at1), int(at2), _ip(frag), _ip(nfrag)),
                     "fragments")
         return frag, nfrag
+
+    def set_md_rules(self, nfragexit=2, more=250, max_steps=10000):
+        """Run the MD bookkeeping and exit rules of an electron-impact
+        fragmentation run (src/md.f90:285-682) on the device after every step;
+        call after egrad() of the start geometry."""
+        self._check(self._lib.qcx_batch_set_md_rules(self._h, int(nfragexit), int(more), int(max_steps)),
+                    "set_md_rules")
+
+    def md_state(self):
+        n = self.nmol
+        i32 = lambda: np.zeros(n, dtype=np.int32)
+        nstep, nfrag, fragstate, mdok, done = i32(), i32(), i32(), i32(), i32()
+        tav, eerror, fragT = np.zeros(n), np.zeros(n), np.zeros((n, 10))
+        self._check(self._lib.qcx_batch_get_md_state(self._h, _ip(nstep), _ip(nfrag), _ip(fragstate), _ip(mdok),
+                                                     _ip(done), _dp(tav), _dp(eerror), _dp(fragT)), "md_state")
+        return {"nstep": nstep, "nfrag": nfrag, "fragstate": fragstate, "mdok": mdok, "done": done, "tav": tav,
+                "eerror": eerror, "fragT": fragT}
 
     def progress(self):
         active = np.zeros(self.nmol, dtype=np.int32)

@@ -108,6 +108,10 @@ struct qcx_batch {
   double* d_frad = nullptr;                   // QCxMS fragment radii (Bohr) by atomic number
   int min_nat = 0, max_nat = 0;
   long long* d_steps = nullptr;
+  // MD bookkeeping and exit rules on the device (qcx_batch_set_md_rules)
+  MdState* d_md = nullptr;
+  bool md_on = false;
+  MdRules md_rules{};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   double graph_tstep = 0.0;
@@ -189,6 +193,7 @@ void free_batch(qcx_batch* b) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->d_gpairs) cudaFree(b->d_gpairs);
+  if (b->d_md) cudaFree(b->d_md);
   for (size_t g = 1; g < b->g_stream.size(); ++g)
     if (b->g_stream[g]) cudaStreamDestroy(b->g_stream[g]);
   for (cudaEvent_t e : b->g_join)
@@ -196,6 +201,14 @@ void free_batch(qcx_batch* b) {
   if (b->g_fork) cudaEventDestroy(b->g_fork);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
+}
+
+// the step graph is captured again at the next qcx_batch_step
+static void drop_graph(qcx_batch* b) {
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->graph_exec = nullptr;
+  b->graph = nullptr;
 }
 
 int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, const double* charge,
@@ -484,6 +497,46 @@ int qcx_batch_fragments(qcx_batch* b, double rcut, int at1, int at2, int32_t* fr
   CK(cudaStreamSynchronize(b->stream));
   return 0;
 }
+int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps) {
+  if (!b || nfragexit < 1 || more < 0 || max_steps < 1) {
+    set_error("qcx_batch_set_md_rules: nfragexit >= 1, more >= 0, max_steps >= 1");
+    return -1;
+  }
+  if (!b->d_md && dalloc(&b->d_md, b->nmol)) return -1;
+  b->md_rules.nfragexit = nfragexit;
+  b->md_rules.more = more;
+  b->md_rules.max_steps = max_steps;
+  launch_md_begin(b->dev, b->d_md, b->stream);
+  if (check_launch()) return -1;
+  CK(cudaStreamSynchronize(b->stream));
+  if (!b->md_on) drop_graph(b);
+  b->md_on = true;
+  return 0;
+}
+
+int qcx_batch_get_md_state(qcx_batch* b, int32_t* nstep, int32_t* nfrag, int32_t* fragstate, int32_t* mdok,
+                           int32_t* done, double* tav, double* eerror, double* fragT) {
+  if (!b || !b->d_md) {
+    set_error("qcx_batch_get_md_state: no MD rules set up (qcx_batch_set_md_rules)");
+    return -1;
+  }
+  std::vector<MdState> st(b->nmol);
+  CK(cudaMemcpyAsync(st.data(), b->d_md, sizeof(MdState) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  for (int m = 0; m < b->nmol; ++m) {
+    if (nstep) nstep[m] = st[m].nstep;
+    if (nfrag) nfrag[m] = st[m].nfrag;
+    if (fragstate) fragstate[m] = st[m].fragstate;
+    if (mdok) mdok[m] = st[m].mdok;
+    if (done) done[m] = st[m].done;
+    if (tav) tav[m] = st[m].tav;
+    if (eerror) eerror[m] = st[m].eerror;
+    if (fragT)
+      for (int j = 0; j < 10; ++j) fragT[10 * m + j] = st[m].fragT[j];
+  }
+  return 0;
+}
+
 int qcx_batch_set_guess(qcx_batch* b, int guess) {
   if (!b || (guess != QCX_GUESS_ZERO && guess != QCX_GUESS_PREVIOUS)) {
     set_error("qcx_batch_set_guess: guess must be 0 (zero moments) or 1 (previous converged moments)");
@@ -517,6 +570,11 @@ int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, cons
   if (!b) return -1;
   size_t n3 = sizeof(double) * 3 * b->natom;
   if (xyz) {
+    if (b->md_on) {
+      // new coordinates start new runs: the MD rules must be set up again
+      b->md_on = false;
+      drop_graph(b);
+    }
     CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));
     // new coordinates start every trajectory afresh
     std::vector<int> on(b->nmol, 1);
@@ -551,6 +609,14 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     launch_leapfrog(b->dev, tstep, b->stream);
     int n = enqueue_egrad(b);
+    if (n >= 0 && b->md_on) {
+      // fragment_structure(nuc, iat, xyz, 3.0, 1, 0, list) of src/md.f90:450, then the rules
+      launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream);
+      MdRules r = b->md_rules;
+      r.tstep = tstep;
+      launch_md_rules(b->dev, b->d_md, b->d_frag, b->d_nfrag, r, b->stream);
+      n += 2;
+    }
     cudaError_t ce = cudaStreamEndCapture(b->stream, &b->graph);
     if (n < 0 || ce != cudaSuccess) {
       if (ce == cudaSuccess && b->graph) cudaGraphDestroy(b->graph);

@@ -23,6 +23,20 @@ void launch_zero_grad(const DevBatch& bt, cudaStream_t st);
 void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,
                       int* nfrag, cudaStream_t st);
 
+// Per-trajectory state of the MD bookkeeping and exit rules (src/md.f90:285-682)
+struct MdState {
+  int nstep, nfrag, fconst, morestep, fragstate, mdok, done, pad;
+  double tav, epav, ekav, edum, eerror, ttime, dtime;
+  double fragT[10];
+};
+struct MdRules {
+  int nfragexit, more, max_steps;
+  double tstep;
+};
+void launch_md_begin(const DevBatch& bt, MdState* st, cudaStream_t stream);
+void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const MdRules& r,
+                     cudaStream_t stream);
+
 // sets the text qcx_last_error() returns
 void set_last_error(const std::string& s);
 // mixed mode: molecules with fewer atomic orbitals run FP64 SCC iterations only

@@ -1,0 +1,173 @@
+// MD bookkeeping and exit rules of a fragmentation run on the device.
+//
+// The MD loop of QCxMS (src/md.f90:285-682) does, per trajectory and step:
+//   top     nstep += 1; T, running sums of T, Epot, Ekin and Etot; the energy
+//           error Eerror = <Etot> - Etot; an exit when Epot == 0 (failed
+//           energy call) or |Eerror| > 0.1 Eh (src/md.f90:288-342)
+//   step    leapfrog + egrad (src/md.f90:388-396)
+//   after   morestep reset and first-fragmentation time (src/md.f90:426-428);
+//           fragment_structure at rcut 3.0 and the fragments' temperatures
+//           (intenergy, src/md.f90:450-454, 715-741); the exit rules of an
+//           electron-impact run (src/md.f90:456-462, 620-666) and the step
+//           limit (src/md.f90:671-679).
+// Here that bookkeeping runs as one thread per trajectory after the step's
+// fragment kernel, inside the captured step graph, so no host round trip is
+// needed per step. The arithmetic keeps the reference's operation order and
+// its single-precision literals (0.5*3*n, 0.1, float(nstep)) with explicit
+// roundings. Not covered: the electron-impact heating of the first nadd steps
+// (impactscale, setetemp: this path runs at a fixed electronic temperature),
+// the CID branch, averages for the output files.
+#include <cuda_runtime.h>
+
+#include "qcx_consts.h"
+#include "qcx_kernels.h"
+
+namespace qcx {
+
+namespace {
+
+// e / (0.5*3*n*kB) with 0.5*3*n evaluated in default (single) real, as the
+// reference writes it (src/md.f90:289, 736)
+__device__ double temp_of(double e, int n) {
+  const float f = 1.5f * (float)n;
+  return __ddiv_rn(e, __dmul_rn((double)f, QCX_KTOAU));
+}
+
+// energy of molecule mol for the bookkeeping: 0 after a failed evaluation,
+// which is how the reference's loop sees a failed energy call
+__device__ double epot_of(const DevBatch& bt, int mol) {
+  if (bt.status[mol] & (kSccNotConverged | kNonFinite | kCholeskyFailed)) return 0.0;
+  return bt.energy[(long long)mol * kNumEnergy + kETotal];
+}
+
+// top of the loop (src/md.f90:286-342); returns true when the run ends here
+__device__ bool md_top(MdState& s, double epot, double ekin, int nuc) {
+  s.nstep += 1;
+  const double t = temp_of(ekin, nuc);
+  s.tav = __dadd_rn(s.tav, t);
+  s.epav = __dadd_rn(s.epav, epot);
+  s.ekav = __dadd_rn(s.ekav, ekin);
+  // nadd = 0: every step enters the running mean of Etot
+  s.edum = __dadd_rn(__dadd_rn(s.edum, epot), ekin);
+  const double eav = __ddiv_rn(s.edum, (double)(float)s.nstep);
+  s.eerror = __dsub_rn(__dsub_rn(eav, epot), ekin);
+  if (s.nfrag == 1) s.fragT[0] = __ddiv_rn(s.tav, (double)s.nstep);
+  const bool err = epot == 0.0 || fabs(s.eerror) > (double)0.1f;
+  if (err) {
+    // with fragments already formed the trajectory is taken anyway (isec = 1)
+    s.mdok = (s.nfrag > 1 && s.nfrag <= 4) ? 1 : 0;
+    s.done = 1;
+  }
+  return err;
+}
+
+}  // namespace
+
+// Start of the loop: Ekin of the current velocities (ekinet,
+// src/mdinit.f90:57-76), Epot of the last evaluation, then the first top.
+__global__ void k_md_begin(DevBatch bt, MdState* st) {
+  const int mol = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mol >= bt.nmol) return;
+  MdState s = {};
+  s.nfrag = 1;
+  const MolDesc md = bt.mol[mol];
+  if (!bt.active[mol]) {
+    s.done = 1;
+    st[mol] = s;
+    return;
+  }
+  double ek = 0.0;
+  for (int i = 0; i < md.nat; ++i) {
+    const double* v = bt.vel + 3LL * (md.atom_off + i);
+    const double v2 = __dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2]));
+    ek = __dadd_rn(ek, __dmul_rn(bt.mass[md.atom_off + i], v2));
+  }
+  ek = __dmul_rn(ek, 0.5);
+  const double epot = epot_of(bt, mol);
+  if (epot == 0.0) {
+    s.done = 1;  // src/md.f90:185: no run without a starting energy
+  } else {
+    md_top(s, epot, ek, md.nat);
+  }
+  if (s.done) bt.active[mol] = 0;
+  st[mol] = s;
+}
+
+// After a step (leapfrog, egrad, fragment numbers of the new coordinates):
+// the end of the loop body, then the top of the next iteration.
+__global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int* nfrag, MdRules r) {
+  const int mol = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mol >= bt.nmol) return;
+  MdState s = st[mol];
+  if (s.done) return;
+  const MolDesc md = bt.mol[mol];
+  s.ttime = __dadd_rn(s.ttime, __ddiv_rn(r.tstep, QCX_FSTOAU));
+  // src/md.f90:426-428, with the fragment count of the previous step
+  if (s.nfrag == 1) s.morestep = 0;
+  if (s.nfrag > 1 && s.dtime < 1.0e-6) s.dtime = __ddiv_rn(s.ttime, 1000.0);
+  const int nf = nfrag[mol];
+  s.nfrag = nf;
+  if (nf > 1) {
+    // intenergy (src/md.f90:715-741) for the first 10 fragments (its arrays hold 10)
+    double eint[10];
+    int cnt[10];
+    for (int j = 0; j < 10; ++j) {
+      eint[j] = 0.0;
+      cnt[j] = 0;
+    }
+    for (int i = 0; i < md.nat; ++i) {
+      const int j = frag[md.atom_off + i] - 1;
+      if (j < 0 || j >= 10) continue;
+      const double* v = bt.vel + 3LL * (md.atom_off + i);
+      const double v2 = __dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2]));
+      eint[j] = __dadd_rn(eint[j], __dmul_rn(__dmul_rn(0.5, bt.mass[md.atom_off + i]), v2));
+      cnt[j] += 1;
+    }
+    for (int j = 0; j < nf && j < 10; ++j) s.fragT[j] = temp_of(eint[j], cnt[j]);
+  }
+  bool exit_now = false;
+  if (nf > 6) {
+    exit_now = true;  // "More than 6 fragments. Error?" (mdok stays 0)
+  } else if (nf > r.nfragexit) {
+    s.fragstate = 1;
+    s.mdok = 1;
+    exit_now = true;
+  } else {
+    s.fconst = nf >= 2 ? s.fconst + 1 : 0;
+    if (s.fconst > 1000) {
+      s.fragstate = 2;
+      s.mdok = 1;
+      exit_now = true;
+    } else if (nf >= r.nfragexit) {
+      s.morestep += 1;
+      if (s.morestep > r.more) {
+        s.fragstate = 1;
+        s.mdok = 1;
+        exit_now = true;
+      }
+    }
+  }
+  if (!exit_now && s.nstep >= r.max_steps) {
+    s.fragstate = 1;
+    s.mdok = 1;
+    exit_now = true;
+  }
+  if (exit_now) {
+    s.done = 1;
+  } else {
+    md_top(s, epot_of(bt, mol), bt.ekin[mol], md.nat);
+  }
+  if (s.done) bt.active[mol] = 0;
+  st[mol] = s;
+}
+
+void launch_md_begin(const DevBatch& bt, MdState* st, cudaStream_t stream) {
+  k_md_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st);
+}
+
+void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const MdRules& r,
+                     cudaStream_t stream) {
+  k_md_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, frag, nfrag, r);
+}
+
+}  // namespace qcx

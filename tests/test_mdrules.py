@@ -1,0 +1,134 @@
+"""MD bookkeeping and exit rules of an electron-impact fragmentation run
+(src/md.f90:285-682, it > 0, isec = 1, no heating phase).
+
+CPU: the oracle restatement on hand-built sequences with a known outcome for
+every exit rule. GPU: the device rules inside the captured step graph against
+the oracle fed with the same per-step energies, kinetic energies, velocities
+and fragment numbers; integer state and every double bit for bit."""
+import numpy as np
+import pytest
+
+import qcxms_gb300 as qg
+from qcxms_gb300 import constants, molgen
+
+DT = 0.5 * constants.FSTOAU
+
+
+def _run(o, seq, nfragexit=2, more=3, max_steps=100000, epot0=-10.0):
+    """Feed (epot, nfrag) pairs; eight atoms at rest, unit masses, the first
+    nfrag - 1 atoms each a fragment of their own."""
+    mass = [1.0] * 8
+    vel = [[0.0, 0.0, 0.0]] * 8
+    s = o.md_rules_begin(vel, mass, epot0)
+    for k, (e, nf) in enumerate(seq):
+        frag = list(range(1, nf)) + [nf] * (8 - nf + 1)
+        o.md_rules_step(s, e, 0.0, vel, mass, frag, nf, DT, nfragexit, more, max_steps)
+        if s["done"]:
+            return s, k + 1
+    return s, len(seq)
+
+
+def test_oracle_exit_rules_known_answers(oracle_lib):
+    o = oracle_lib
+    # energy error above 0.1 Eh: exit, taken only with 2..4 fragments
+    s, k = _run(o, [(-10.0, 1)] * 5 + [(-9.5, 1)])
+    assert s["done"] and s["mdok"] == 0 and k == 6 and s["fragstate"] == 0
+    s, k = _run(o, [(-10.0, 2)] * 2 + [(-9.5, 2)], nfragexit=3)
+    assert s["done"] and s["mdok"] == 1 and k == 3
+    # a failed energy call (Epot = 0) ends the run at the next loop top
+    s, k = _run(o, [(-10.0, 1), (0.0, 1)])
+    assert s["done"] and s["mdok"] == 0 and k == 2
+    # nfragexit fragments: `more` further steps, then exit with fragstate 1
+    s, k = _run(o, [(-10.0, 1)] * 3 + [(-10.0, 2)] * 10, nfragexit=2, more=3)
+    assert s["done"] and s["mdok"] == 1 and s["fragstate"] == 1 and k == 3 + 4
+    # back to one fragment resets the count one step later (src/md.f90:426)
+    s, k = _run(o, [(-10.0, 2)] * 3 + [(-10.0, 1)] + [(-10.0, 2)] * 10, nfragexit=2, more=3)
+    assert k == 4 + 4 and s["fragstate"] == 1
+    # more than nfragexit fragments: immediate exit
+    s, k = _run(o, [(-10.0, 1)] * 2 + [(-10.0, 3)], nfragexit=2)
+    assert s["done"] and s["mdok"] == 1 and s["fragstate"] == 1 and k == 3
+    # more than 6 fragments: an error, not taken
+    s, k = _run(o, [(-10.0, 7)], nfragexit=10)
+    assert s["done"] and s["mdok"] == 0 and k == 1
+    # two fragments for more than 1000 steps: fragstate 2
+    s, k = _run(o, [(-10.0, 2)] * 1100, nfragexit=3)
+    assert s["done"] and s["fragstate"] == 2 and k == 1001
+    # step limit
+    s, k = _run(o, [(-10.0, 1)] * 50, max_steps=20)
+    assert s["done"] and s["mdok"] == 1 and s["fragstate"] == 1 and s["nstep"] == 20 and k == 20
+    # no start energy: no run at all
+    s = o.md_rules_begin([[0.0] * 3], [1.0], 0.0)
+    assert s["done"] and s["nstep"] == 0
+
+
+def test_oracle_temperatures(oracle_lib):
+    o = oracle_lib
+    mass = [2.0, 3.0, 4.0]
+    vel = [[0.1, 0.0, 0.0], [0.0, 0.2, 0.0], [0.0, 0.0, 0.3]]
+    s = o.md_rules_begin(vel, mass, -5.0)
+    ek = 0.5 * (2.0 * 0.01 + 3.0 * 0.04 + 4.0 * 0.09)
+    assert s["nstep"] == 1 and abs(s["tav"] - ek / (1.5 * 3 * o.KB)) < 1e-9
+    o.md_rules_step(s, -5.0, ek, vel, mass, [1, 2, 2], 2, DT, 3, 250, 100)
+    # fragment 2 holds atoms 2 and 3: T = E_int / (1.5 * 2 * kB)
+    e2 = 0.5 * 3.0 * 0.04 + 0.5 * 4.0 * 0.09
+    assert abs(s["fragT"][1] - e2 / (1.5 * 2 * o.KB)) < 1e-9
+
+
+def _kicked_batch():
+    """Cations with their H atoms kicked outward (0.02 au, about 10 eV for H):
+    some lose one H (2 fragments), some two (3), some none."""
+    mols = []
+    for k in range(12):
+        Z, xyz = molgen.random_chno(6 + k % 5, 300 + k)
+        Z = np.asarray(Z)
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+        vel = molgen.maxwell_boltzmann(Z, 300.0, 300 + k)
+        hs = np.nonzero(Z == 1)[0]
+        nkick = k % 3
+        c = xyz.mean(0)
+        for h in hs[:nkick]:
+            d = xyz[h] - c
+            vel[h] += 0.02 * d / np.linalg.norm(d)
+        mols.append({"Z": Z, "xyz": xyz, "vel": vel, "mass": molgen.masses(Z), "charge": 1})
+    return mols
+
+
+@pytest.mark.gpu
+def test_gpu_md_rules_match_oracle(gpu, oracle_lib):
+    o = oracle_lib
+    mols = _kicked_batch()
+    b = qg.Batch(mols)
+    b.egrad()
+    r0 = b.get()
+    nfragexit, more, max_steps = 2, 5, 40
+    b.set_md_rules(nfragexit, more, max_steps)
+    off = np.concatenate([[0], np.cumsum([len(m["Z"]) for m in mols])])
+    fail = qg.STATUS_SCC_NOT_CONVERGED | qg.STATUS_NON_FINITE | qg.STATUS_CHOLESKY_FAILED
+    ref = []
+    for i, m in enumerate(mols):
+        e = 0.0 if r0["status"][i] & fail else r0["energy"][i]
+        ref.append(o.md_rules_begin(r0["vel"][off[i]:off[i + 1]], list(m["mass"]), e))
+    for step in range(max_steps + 2):
+        st = b.md_state()
+        for i in range(len(mols)):
+            s = ref[i]
+            assert st["nstep"][i] == s["nstep"] and st["done"][i] == s["done"], (step, i)
+            assert st["nfrag"][i] == s["nfrag"] and st["fragstate"][i] == s["fragstate"], (step, i)
+            assert st["mdok"][i] == s["mdok"], (step, i)
+            assert st["tav"][i] == s["tav"] and st["eerror"][i] == s["eerror"], (step, i)
+            assert np.array_equal(st["fragT"][i], np.array(s["fragT"])), (step, i)
+        if st["done"].all():
+            break
+        b.step(1, DT)
+        r = b.get()
+        frag, nf = b.fragments(3.0, 1, 0)
+        for i, m in enumerate(mols):
+            e = 0.0 if r["status"][i] & fail else r["energy"][i]
+            o.md_rules_step(ref[i], e, r["ekin"][i], r["vel"][off[i]:off[i + 1]], list(m["mass"]),
+                            list(frag[off[i]:off[i + 1]]), int(nf[i]), DT, nfragexit, more, max_steps)
+    st = b.md_state()
+    assert st["done"].all()
+    # the set exercises the fragment exits and the step limit
+    assert (st["nfrag"] >= 2).sum() >= 3 and (st["nstep"] == max_steps).sum() >= 1
+    active, _ = b.progress()
+    assert not active.any()
