@@ -150,11 +150,28 @@ int qcx_batch_fragments(qcx_batch* b, double rcut, int at1, int at2, int32_t* fr
  * active flag drops to 0). Call after qcx_batch_egrad of the start geometry:
  * the first loop top uses that energy and the kinetic energy of the current
  * velocities (ekinet, src/mdinit.f90:57-76). New coordinates through
- * qcx_batch_set_state switch the rules off. Not covered: the electron-impact
- * heating of the first steps (impactscale, setetemp; the electronic
- * temperature stays fixed), the CID branch, the output-file averages.
+ * qcx_batch_set_state switch the rules off. The heating of the first steps is
+ * set up by qcx_batch_set_md_heating. Not covered: a per-step electronic
+ * temperature (ieetemp != 0), the CID branch, the output-file averages.
  */
 int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps);
+
+/* Heating of the first steps of an electron-impact run (impactscale,
+ * src/impact.f90:12-55, called by src/md.f90:439-441 while nstep <= nadd and
+ * the molecule is one fragment): each step the velocities are scaled by
+ * 1 + velof * scal, scal grown in steps of 0.0002 until the kinetic energy
+ * reaches eimp * fadd * nstep + Ekin(start); nadd = (tadd + tstep)/tstep - 1
+ * and fadd = tstep/(tadd + tstep) as src/md.f90:265-266. eimp[nmol] (Eh),
+ * tadd[nmol] (atomic time units) and velof[natom] (NULL: all 1) come from each
+ * trajectory's start file (rdstart); tstep is the step of qcx_batch_step. Call
+ * before qcx_batch_set_md_rules, which reads these values. The running mean of
+ * the total energy starts after the nadd steps (src/md.f90:304-309). A run whose
+ * scaling needs 20000 increments ends (the reference stops the program). The
+ * electronic temperature stays the batch's: with the default ieetemp = 0,
+ * setetemp (src/utility.f90:69-86) gives the constant 5000 + 20000 ax, which is
+ * the etemp to create the batch with. */
+int qcx_batch_set_md_heating(qcx_batch* b, const double* eimp, const double* tadd, const double* velof,
+                             double tstep);
 
 /* State of the MD rules per trajectory (any pointer may be NULL): nstep,
  * nfrag (fragments at the last step), fragstate (1: exit on fragment count or

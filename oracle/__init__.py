@@ -245,8 +245,11 @@ def md_rules_top(s, epot, ekin, nuc):
     s["tav"] = s["tav"] + t
     s["epav"] = s["epav"] + epot
     s["ekav"] = s["ekav"] + ekin
-    s["edum"] = (s["edum"] + epot) + ekin
-    eav = s["edum"] / float(np.float32(s["nstep"]))
+    if s["nstep"] > s["nadd"]:
+        s["edum"] = (s["edum"] + epot) + ekin
+        eav = s["edum"] / float(np.float32(s["nstep"] - s["nadd"]))
+    else:
+        eav = epot + ekin
     s["eerror"] = (eav - epot) - ekin
     if s["nfrag"] == 1:
         s["fragT"][0] = s["tav"] / s["nstep"]
@@ -257,15 +260,49 @@ def md_rules_top(s, epot, ekin, nuc):
     return False
 
 
-def md_rules_begin(vel, mass, epot):
-    """State before the loop: ekinet (src/mdinit.f90:57-76) and the first top."""
-    s = {"nstep": 0, "nfrag": 1, "fconst": 0, "morestep": 0, "fragstate": 0, "mdok": 0, "done": 0, "tav": 0.0,
-         "epav": 0.0, "ekav": 0.0, "edum": 0.0, "eerror": 0.0, "ttime": 0.0, "dtime": 0.0, "fragT": [0.0] * 10}
+def _ekinet(vel, mass, velof=None, scal=0.0):
+    """ekinet (src/mdinit.f90:57-76) of vel * (1 + velof * scal)."""
     ek = 0.0
     for i in range(len(mass)):
-        v = vel[i]
-        ek = ek + mass[i] * ((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])
-    ek = ek * 0.5
+        f = 1.0 + (1.0 if velof is None else velof[i]) * scal
+        x, y, z = vel[i][0] * f, vel[i][1] * f, vel[i][2] * f
+        ek = ek + mass[i] * ((x * x + y * y) + z * z)
+    return ek * 0.5
+
+
+def impactscale(vel, mass, velof, eimp, ff, e0):
+    """impactscale (src/impact.f90:12-55); scales vel in place, False after
+    20000 increments."""
+    esoll = eimp * ff + e0
+    scal, k = 0.0, 0
+    while True:
+        k += 1
+        e = _ekinet(vel, mass, velof, scal)
+        scal = scal + float(np.float32(0.0002))
+        if not (esoll - e > float(np.float32(0.001)) and k < 20000):
+            break
+    for i in range(len(mass)):
+        f = 1.0 + (1.0 if velof is None else velof[i]) * scal
+        for d in range(3):
+            vel[i][d] = vel[i][d] * f
+    return k < 20000
+
+
+def md_heating(eimp, tadd, tstep):
+    """(eimp, fadd, nadd) of src/md.f90:265-266."""
+    return eimp, tstep / (tadd + tstep), int((tadd + tstep) / tstep - 1.0)
+
+
+def md_rules_begin(vel, mass, epot, heat=None):
+    """State before the loop: ekinet (src/mdinit.f90:57-76) and the first top.
+    heat = (eimp, fadd, nadd) of md_heating, or None."""
+    s = {"nstep": 0, "nfrag": 1, "fconst": 0, "morestep": 0, "fragstate": 0, "mdok": 0, "done": 0, "tav": 0.0,
+         "epav": 0.0, "ekav": 0.0, "edum": 0.0, "eerror": 0.0, "ttime": 0.0, "dtime": 0.0, "fragT": [0.0] * 10,
+         "eimp": 0.0, "fadd": 0.0, "nadd": 0, "heat_failed": 0}
+    if heat is not None:
+        s["eimp"], s["fadd"], s["nadd"] = heat
+    ek = _ekinet(vel, mass)
+    s["ekinstart"] = ek
     if epot == 0:
         s["done"] = 1  # src/md.f90:185
     else:
@@ -273,9 +310,10 @@ def md_rules_begin(vel, mass, epot):
     return s
 
 
-def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more, max_steps):
+def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more, max_steps, velof=None):
     """Rest of one loop iteration after leapfrog + egrad (src/md.f90:426-679,
-    electron-impact branch), then the next top. epot = 0 for a failed call."""
+    electron-impact branch), then the next top. epot = 0 for a failed call.
+    vel (the velocities after leapfrog) is scaled in place while heating."""
     if s["done"]:
         return s
     s["ttime"] = s["ttime"] + tstep / FSTOAU
@@ -283,6 +321,10 @@ def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more,
         s["morestep"] = 0
     if s["nfrag"] > 1 and s["dtime"] < 1.0e-6:
         s["dtime"] = s["ttime"] / 1000.0
+    if s["nstep"] <= s["nadd"] and s["nfrag"] == 1:  # src/md.f90:439-441
+        if not impactscale(vel, mass, velof, s["eimp"], s["fadd"] * s["nstep"], s["ekinstart"]):
+            s["heat_failed"], s["done"] = 1, 1
+            return s
     s["nfrag"] = nfrag
     if nfrag > 1:  # intenergy, src/md.f90:715-741
         eint, cnt = [0.0] * 10, [0] * 10

@@ -91,6 +91,7 @@ def load_library(build_if_missing=True):
     lib.qcx_fragment_ips.argtypes = [c_int, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double),
                                      P(ctypes.c_int32), c_int, c_double, c_int, P(c_double), P(c_double),
                                      P(ctypes.c_int32)]
+    lib.qcx_batch_set_md_heating.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double), c_double]
     lib.qcx_batch_set_md_rules.argtypes = [ctypes.c_void_p, c_int, c_int, c_int]
     lib.qcx_batch_get_md_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 5 + [P(c_double)] * 3
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
@@ -276,6 +277,16 @@ class Batch:
         call after egrad() of the start geometry."""
         self._check(self._lib.qcx_batch_set_md_rules(self._h, int(nfragexit), int(more), int(max_steps)),
                     "set_md_rules")
+
+    def set_md_heating(self, eimp, tadd, tstep, velof=None):
+        """Heating of the first steps (impactscale, src/impact.f90:12-55):
+        eimp[nmol] (Eh), tadd[nmol] (atomic time units), velof[natom] or None;
+        call before set_md_rules."""
+        eimp = np.ascontiguousarray(eimp, dtype=np.float64)
+        tadd = np.ascontiguousarray(tadd, dtype=np.float64)
+        vf = None if velof is None else np.ascontiguousarray(velof, dtype=np.float64)
+        self._check(self._lib.qcx_batch_set_md_heating(self._h, _dp(eimp), _dp(tadd), _dp(vf), float(tstep)),
+                    "set_md_heating")
 
     def md_state(self):
         n = self.nmol

@@ -110,6 +110,9 @@ struct qcx_batch {
   long long* d_steps = nullptr;
   // MD bookkeeping and exit rules on the device (qcx_batch_set_md_rules)
   MdState* d_md = nullptr;
+  double* d_md_heat = nullptr;  // [nmol][3] eimp, fadd, nadd (qcx_batch_set_md_heating)
+  double* d_velof = nullptr;    // [natom] velocity scaling weights of the heating
+  bool md_heat = false;
   bool md_on = false;
   MdRules md_rules{};
   cudaGraph_t graph = nullptr;
@@ -194,6 +197,8 @@ void free_batch(qcx_batch* b) {
     if (p) cudaFree(p);
   if (b->d_gpairs) cudaFree(b->d_gpairs);
   if (b->d_md) cudaFree(b->d_md);
+  if (b->d_md_heat) cudaFree(b->d_md_heat);
+  if (b->d_velof) cudaFree(b->d_velof);
   for (size_t g = 1; g < b->g_stream.size(); ++g)
     if (b->g_stream[g]) cudaStreamDestroy(b->g_stream[g]);
   for (cudaEvent_t e : b->g_join)
@@ -506,11 +511,39 @@ int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps)
   b->md_rules.nfragexit = nfragexit;
   b->md_rules.more = more;
   b->md_rules.max_steps = max_steps;
-  launch_md_begin(b->dev, b->d_md, b->stream);
+  launch_md_begin(b->dev, b->d_md, b->md_heat ? b->d_md_heat : nullptr, b->stream);
   if (check_launch()) return -1;
   CK(cudaStreamSynchronize(b->stream));
   if (!b->md_on) drop_graph(b);
   b->md_on = true;
+  return 0;
+}
+
+int qcx_batch_set_md_heating(qcx_batch* b, const double* eimp, const double* tadd, const double* velof,
+                             double tstep) {
+  if (!b || !eimp || !tadd || !(tstep > 0.0)) {
+    set_error("qcx_batch_set_md_heating: eimp[nmol], tadd[nmol] and tstep > 0 are required");
+    return -1;
+  }
+  std::vector<double> h(3 * (size_t)b->nmol);
+  for (int m = 0; m < b->nmol; ++m) {
+    if (!(eimp[m] >= 0.0) || !(tadd[m] >= 0.0)) {
+      set_error("qcx_batch_set_md_heating: eimp and tadd must be >= 0");
+      return -1;
+    }
+    // src/md.f90:265-266: nadd = (tadd + tstep) / tstep - 1 (truncated), fadd = tstep / (tadd + tstep)
+    h[3 * m] = eimp[m];
+    h[3 * m + 1] = tstep / (tadd[m] + tstep);
+    h[3 * m + 2] = (double)(int)((tadd[m] + tstep) / tstep - 1.0);
+  }
+  std::vector<double> vf(b->natom, 1.0);
+  if (velof)
+    for (int a = 0; a < b->natom; ++a) vf[a] = velof[a];
+  if (!b->d_md_heat && dalloc(&b->d_md_heat, 3 * (size_t)b->nmol)) return -1;
+  if (!b->d_velof && dalloc(&b->d_velof, (size_t)b->natom)) return -1;
+  CK(cudaMemcpy(b->d_md_heat, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_velof, vf.data(), sizeof(double) * vf.size(), cudaMemcpyHostToDevice));
+  b->md_heat = true;
   return 0;
 }
 
@@ -614,7 +647,7 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
       launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream);
       MdRules r = b->md_rules;
       r.tstep = tstep;
-      launch_md_rules(b->dev, b->d_md, b->d_frag, b->d_nfrag, r, b->stream);
+      launch_md_rules(b->dev, b->d_md, b->d_frag, b->d_nfrag, b->md_heat ? b->d_velof : nullptr, r, b->stream);
       n += 2;
     }
     cudaError_t ce = cudaStreamEndCapture(b->stream, &b->graph);

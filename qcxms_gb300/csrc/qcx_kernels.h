@@ -25,17 +25,20 @@ void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double
 
 // Per-trajectory state of the MD bookkeeping and exit rules (src/md.f90:285-682)
 struct MdState {
-  int nstep, nfrag, fconst, morestep, fragstate, mdok, done, pad;
+  int nstep, nfrag, fconst, morestep, fragstate, mdok, done, heat_failed;
+  int nadd, pad;
   double tav, epav, ekav, edum, eerror, ttime, dtime;
+  double eimp, fadd, ekinstart;  // heating of the first nadd steps (impactscale)
   double fragT[10];
 };
 struct MdRules {
   int nfragexit, more, max_steps;
   double tstep;
 };
-void launch_md_begin(const DevBatch& bt, MdState* st, cudaStream_t stream);
-void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const MdRules& r,
-                     cudaStream_t stream);
+// heat [nmol][3] = (eimp, fadd, nadd) or nullptr (no heating); velof [natom] or nullptr
+void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, cudaStream_t stream);
+void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
+                     const MdRules& r, cudaStream_t stream);
 
 // sets the text qcx_last_error() returns
 void set_last_error(const std::string& s);

@@ -14,9 +14,10 @@
 // fragment kernel, inside the captured step graph, so no host round trip is
 // needed per step. The arithmetic keeps the reference's operation order and
 // its single-precision literals (0.5*3*n, 0.1, float(nstep)) with explicit
-// roundings. Not covered: the electron-impact heating of the first nadd steps
-// (impactscale, setetemp: this path runs at a fixed electronic temperature),
-// the CID branch, averages for the output files.
+// roundings. The heating of the first nadd steps (impactscale, src/md.f90:439-441)
+// runs here too; the electronic temperature stays the batch's (setetemp with
+// ieetemp = 0, the default, gives the constant 5000 + 20000 ax). Not covered:
+// ieetemp != 0, the CID branch, averages for the output files.
 #include <cuda_runtime.h>
 
 #include "qcx_consts.h"
@@ -47,9 +48,14 @@ __device__ bool md_top(MdState& s, double epot, double ekin, int nuc) {
   s.tav = __dadd_rn(s.tav, t);
   s.epav = __dadd_rn(s.epav, epot);
   s.ekav = __dadd_rn(s.ekav, ekin);
-  // nadd = 0: every step enters the running mean of Etot
-  s.edum = __dadd_rn(__dadd_rn(s.edum, epot), ekin);
-  const double eav = __ddiv_rn(s.edum, (double)(float)s.nstep);
+  // the running mean of Etot starts after the nadd heating steps
+  double eav;
+  if (s.nstep > s.nadd) {
+    s.edum = __dadd_rn(__dadd_rn(s.edum, epot), ekin);
+    eav = __ddiv_rn(s.edum, (double)(float)(s.nstep - s.nadd));
+  } else {
+    eav = __dadd_rn(epot, ekin);
+  }
   s.eerror = __dsub_rn(__dsub_rn(eav, epot), ekin);
   if (s.nfrag == 1) s.fragT[0] = __ddiv_rn(s.tav, (double)s.nstep);
   const bool err = epot == 0.0 || fabs(s.eerror) > (double)0.1f;
@@ -61,15 +67,58 @@ __device__ bool md_top(MdState& s, double epot, double ekin, int nuc) {
   return err;
 }
 
+// kinetic energy of the velocities v * (1 + velof * scal) (ekinet, src/mdinit.f90:57-76)
+__device__ double ekin_scaled(const DevBatch& bt, const MolDesc& md, const double* velof, double scal) {
+  double ek = 0.0;
+  for (int i = 0; i < md.nat; ++i) {
+    const long long a = md.atom_off + i;
+    const double f = __dadd_rn(1.0, __dmul_rn(velof ? velof[a] : 1.0, scal));
+    const double* v = bt.vel + 3 * a;
+    const double x = __dmul_rn(v[0], f), y = __dmul_rn(v[1], f), z = __dmul_rn(v[2], f);
+    const double v2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+    ek = __dadd_rn(ek, __dmul_rn(bt.mass[a], v2));
+  }
+  return __dmul_rn(ek, 0.5);
+}
+
+// impactscale (src/impact.f90:12-55): grow the scaling factor in steps of
+// 0.0002 until the kinetic energy reaches eimp * ff + e0 (within 0.001 Eh) or
+// 20000 steps pass, then scale the velocities. Returns false after 20000 steps
+// (the reference stops the program there).
+__device__ bool impact_scale(const DevBatch& bt, const MolDesc& md, const double* velof, double eimp, double ff,
+                             double e0) {
+  const double esoll = __dadd_rn(__dmul_rn(eimp, ff), e0);
+  double scal = 0.0;
+  int k = 0;
+  for (;;) {
+    ++k;
+    const double e = ekin_scaled(bt, md, velof, scal);
+    scal = __dadd_rn(scal, (double)0.0002f);
+    if (!(__dsub_rn(esoll, e) > (double)0.001f && k < 20000)) break;
+  }
+  for (int i = 0; i < md.nat; ++i) {
+    const long long a = md.atom_off + i;
+    const double f = __dadd_rn(1.0, __dmul_rn(velof ? velof[a] : 1.0, scal));
+    double* v = bt.vel + 3 * a;
+    for (int d = 0; d < 3; ++d) v[d] = __dmul_rn(v[d], f);
+  }
+  return k < 20000;
+}
+
 }  // namespace
 
 // Start of the loop: Ekin of the current velocities (ekinet,
 // src/mdinit.f90:57-76), Epot of the last evaluation, then the first top.
-__global__ void k_md_begin(DevBatch bt, MdState* st) {
+__global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat) {
   const int mol = blockIdx.x * blockDim.x + threadIdx.x;
   if (mol >= bt.nmol) return;
   MdState s = {};
   s.nfrag = 1;
+  if (heat) {
+    s.eimp = heat[3 * mol];
+    s.fadd = heat[3 * mol + 1];
+    s.nadd = (int)heat[3 * mol + 2];
+  }
   const MolDesc md = bt.mol[mol];
   if (!bt.active[mol]) {
     s.done = 1;
@@ -83,6 +132,7 @@ __global__ void k_md_begin(DevBatch bt, MdState* st) {
     ek = __dadd_rn(ek, __dmul_rn(bt.mass[md.atom_off + i], v2));
   }
   ek = __dmul_rn(ek, 0.5);
+  s.ekinstart = ek;
   const double epot = epot_of(bt, mol);
   if (epot == 0.0) {
     s.done = 1;  // src/md.f90:185: no run without a starting energy
@@ -95,7 +145,8 @@ __global__ void k_md_begin(DevBatch bt, MdState* st) {
 
 // After a step (leapfrog, egrad, fragment numbers of the new coordinates):
 // the end of the loop body, then the top of the next iteration.
-__global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int* nfrag, MdRules r) {
+__global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
+                           MdRules r) {
   const int mol = blockIdx.x * blockDim.x + threadIdx.x;
   if (mol >= bt.nmol) return;
   MdState s = st[mol];
@@ -105,6 +156,16 @@ __global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int*
   // src/md.f90:426-428, with the fragment count of the previous step
   if (s.nfrag == 1) s.morestep = 0;
   if (s.nfrag > 1 && s.dtime < 1.0e-6) s.dtime = __ddiv_rn(s.ttime, 1000.0);
+  // heating while not fragmented (src/md.f90:439-441), before the fragment check
+  if (s.nstep <= s.nadd && s.nfrag == 1) {
+    if (!impact_scale(bt, md, velof, s.eimp, __dmul_rn(s.fadd, (double)s.nstep), s.ekinstart)) {
+      s.heat_failed = 1;
+      s.done = 1;
+      bt.active[mol] = 0;
+      st[mol] = s;
+      return;
+    }
+  }
   const int nf = nfrag[mol];
   s.nfrag = nf;
   if (nf > 1) {
@@ -161,13 +222,13 @@ __global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int*
   st[mol] = s;
 }
 
-void launch_md_begin(const DevBatch& bt, MdState* st, cudaStream_t stream) {
-  k_md_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st);
+void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, cudaStream_t stream) {
+  k_md_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, heat);
 }
 
-void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const MdRules& r,
-                     cudaStream_t stream) {
-  k_md_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, frag, nfrag, r);
+void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
+                     const MdRules& r, cudaStream_t stream) {
+  k_md_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, frag, nfrag, velof, r);
 }
 
 }  // namespace qcx

@@ -132,3 +132,78 @@ def test_gpu_md_rules_match_oracle(gpu, oracle_lib):
     assert (st["nfrag"] >= 2).sum() >= 3 and (st["nstep"] == max_steps).sum() >= 1
     active, _ = b.progress()
     assert not active.any()
+
+
+def test_oracle_impactscale(oracle_lib):
+    o = oracle_lib
+    mass = [1837.0, 21874.0, 29166.0]
+    vel = [[1e-3, 0.0, 0.0], [0.0, -2e-4, 1e-4], [1e-4, 1e-4, 0.0]]
+    e0 = o._ekinet(vel, mass)
+    v = [list(x) for x in vel]
+    assert o.impactscale(v, mass, None, 0.1, 0.05, e0)
+    e1 = o._ekinet(v, mass)
+    # the target eimp * ff + e0 is reached to 0.001 Eh (plus at most one increment of 0.0002)
+    assert e1 > e0 + 0.005 - 0.001 and e1 < e0 + 0.005 + 4.1e-4 * e1
+    # heating weights: atoms with velof 0 keep their velocities
+    v = [list(x) for x in vel]
+    o.impactscale(v, mass, [1.0, 0.0, 1.0], 0.1, 0.05, e0)
+    assert v[1] == vel[1] and v[0] != vel[0]
+    assert o.md_heating(0.2, 10 * DT, DT)[2] == 10
+
+
+@pytest.mark.gpu
+def test_gpu_md_heating_match_oracle(gpu, oracle_lib):
+    """Heating phase: velocities after every step (leapfrog restated by the
+    oracle, then impactscale) and the rule state bit for bit."""
+    o = oracle_lib
+    mols = []
+    for k in range(8):
+        Z, xyz = molgen.random_chno(8 + k, 700 + k)
+        Z = np.asarray(Z)
+        mols.append({"Z": Z, "xyz": np.asarray(xyz, dtype=np.float64).reshape(-1, 3),
+                     "vel": molgen.maxwell_boltzmann(Z, 500.0, 700 + k), "mass": molgen.masses(Z), "charge": 1})
+    b = qg.Batch(mols)
+    b.egrad()
+    rng = np.random.default_rng(5)
+    eimp = rng.uniform(0.05, 0.3, len(mols))
+    tadd = np.array([(8 + k) * DT for k in range(len(mols))])
+    velof = rng.uniform(0.5, 2.0, b.natom)
+    b.set_md_heating(eimp, tadd, DT, velof)
+    nfragexit, more, max_steps = 3, 20, 25
+    b.set_md_rules(nfragexit, more, max_steps)
+    off = np.concatenate([[0], np.cumsum([len(m["Z"]) for m in mols])])
+    fail = qg.STATUS_SCC_NOT_CONVERGED | qg.STATUS_NON_FINITE | qg.STATUS_CHOLESKY_FAILED
+    r = b.get()
+    ref = []
+    for i, m in enumerate(mols):
+        e = 0.0 if r["status"][i] & fail else r["energy"][i]
+        ref.append(o.md_rules_begin(r["vel"][off[i]:off[i + 1]], list(m["mass"]), e,
+                                    o.md_heating(eimp[i], tadd[i], DT)))
+    assert [s["nadd"] for s in ref] == list(range(8, 16))
+    heated = 0
+    for step in range(max_steps + 1):
+        st = b.md_state()
+        for i in range(len(mols)):
+            s = ref[i]
+            assert st["nstep"][i] == s["nstep"] and st["done"][i] == s["done"], (step, i)
+            assert st["tav"][i] == s["tav"] and st["eerror"][i] == s["eerror"], (step, i)
+            assert np.array_equal(st["fragT"][i], np.array(s["fragT"])), (step, i)
+        if st["done"].all():
+            break
+        prev = r
+        b.step(1, DT)
+        r = b.get()
+        frag, nf = b.fragments(3.0, 1, 0)
+        for i, m in enumerate(mols):
+            if ref[i]["done"]:
+                continue
+            sl = slice(off[i], off[i + 1])
+            _, vpre, _ = o.leapfrog(prev["grad"][sl], m["mass"], DT, prev["xyz"][sl], prev["vel"][sl])
+            vpre = [list(x) for x in vpre]
+            scaled = ref[i]["nstep"] <= ref[i]["nadd"] and ref[i]["nfrag"] == 1
+            e = 0.0 if r["status"][i] & fail else r["energy"][i]
+            o.md_rules_step(ref[i], e, r["ekin"][i], vpre, list(m["mass"]), list(frag[sl]), int(nf[i]), DT,
+                            nfragexit, more, max_steps, velof=list(velof[sl]))
+            assert np.array_equal(np.array(vpre), r["vel"][sl]), (step, i)
+            heated += scaled
+    assert heated >= 8 * 8
