@@ -249,6 +249,12 @@ def run_gpu(args):
     b.set_precision(args.precision)
     b.set_guess(args.guess)
     b.egrad()
+    if args.md_rules:
+        # the electron-impact MD loop's heating, bookkeeping and exit rules on the
+        # device (impactscale over the first 100 steps, nfragexit 2, more 250)
+        rng = np.random.default_rng(11 + rank)
+        b.set_md_heating(rng.uniform(0.1, 0.3, b.nmol), np.full(b.nmol, 100 * dt), dt)
+        b.set_md_rules(2, 250, 100000)
     b.sync()
     stream = torch.cuda.ExternalStream(b.stream())
     nao, nat = b.sizes()
@@ -338,6 +344,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD_NAMES[args.workload], "ntraj_per_gpu": b.nmol,
                        "atoms": [NMIN, NMAX] if args.workload == "batch" else [10, 81],
                        "etemp_K": ETEMP, "precision": args.precision, "scc_guess": args.guess,
+                       "md_rules_on_device": bool(args.md_rules),
                        "execution": "one CUDA graph per MD step, 8 molecule groups on separate streams", "l2": "flushed between timed steps (256 MiB write)",
                        "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters)),
                        "mean_scc_iters_fp64": float(np.mean(it64)),
@@ -431,6 +438,9 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="batch", choices=["batch", "cid", "fragip"])
     ap.add_argument("--no-plain", action="store_true", help="skip the single-trajectory FP64 reference leg")
+    ap.add_argument("--md-rules", action="store_true",
+                    help="run the MD heating, bookkeeping and exit rules on the device in the timed steps "
+                         "(the end-to-end leg sets new coordinates, which switches them off)")
     ap.add_argument("--guess", default="zero", choices=["zero", "previous"],
                     help="SCC start: zero moments every step (the reference's behaviour, default) or the "
                          "trajectory's converged moments of the previous step (opt-in)")
