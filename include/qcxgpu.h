@@ -236,6 +236,22 @@ int qcx_fragment_ips(int method, int ntraj, const int32_t* nat, const int32_t* n
 int qcx_boltz(int units, int nfrag, int mchrg, double temp, const double* ip, double* fragchrg2);
 
 /*
+ * Trajectory start files of a QCxMS ensemble (host only, no GPU work), so
+ * that a batched driver can load TMPQCXMS/TMP.n/ of every trajectory instead
+ * of starting one process per trajectory (bin/pqcxms:88-99).
+ * qcx_read_xyz reads start.xyz (xyz format, Angstrom; elements 1..18) into
+ * num[nat] and xyz[nat][3] in Bohr (1/0.52917726 Bohr per Angstrom,
+ * src/xtb_mctc_convert.f90:24-25); with num = xyz = NULL it only returns the
+ * atom count in *nat. qcx_read_start reads qcxms.start as rdstart
+ * (src/utility.f90:379-422) does, in the layout wrstart writes
+ * (src/utility.f90:321-373): the trajectory number, eimp, tadd, then per atom
+ * vx vy vz velof (D22.14 fields). Any output pointer may be NULL.
+ */
+int qcx_read_xyz(const char* path, int max_nat, int32_t* nat, int32_t* num, double* xyz);
+int qcx_read_start(const char* path, int nat, int32_t* itrj, double* eimp, double* tadd, double* vel,
+                   double* velof);
+
+/*
  * Allocation-free variant of qcx_egrad for callers that cannot call
  * cudaMalloc (for example a host program whose device memory belongs to
  * another runtime's capped pool, or a path that must not trigger the device

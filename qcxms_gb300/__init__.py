@@ -25,7 +25,7 @@ import numpy as np
 
 from . import constants
 
-__all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "fragment_ips", "boltz", "load_library",
+__all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "fragment_ips", "boltz", "read_ensemble", "load_library",
            "library_path",
            "STATUS_SCC_NOT_CONVERGED", "STATUS_NON_FINITE", "STATUS_CHOLESKY_FAILED", "STATUS_EIGEN_NOT_CONVERGED"]
 
@@ -94,6 +94,9 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_set_md_heating.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double), c_double]
     lib.qcx_batch_set_md_rules.argtypes = [ctypes.c_void_p, c_int, c_int, c_int]
     lib.qcx_batch_get_md_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 5 + [P(c_double)] * 3
+    lib.qcx_read_xyz.argtypes = [ctypes.c_char_p, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double)]
+    lib.qcx_read_start.argtypes = [ctypes.c_char_p, c_int, P(ctypes.c_int32), P(c_double), P(c_double),
+                                   P(c_double), P(c_double)]
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
     _lib = lib
     return lib
@@ -134,6 +137,40 @@ def get_xtb_egrad(num, xyz, charge, multiplicity, method=gfn2_xtb, etemp=300.0, 
 
 
 MAX_FRAGMENTS = 10
+
+
+def read_ensemble(root="TMPQCXMS", charge=1):
+    """Every trajectory of a QCxMS ensemble directory: ``root/TMP.n/start.xyz``
+    and ``root/TMP.n/qcxms.start`` (wrstart, ``src/utility.f90:321-373``), in
+    the order of n. Returns a list of dicts with Z, xyz (Bohr), vel, velof,
+    eimp, tadd, itrj, mass and charge, ready for :class:`Batch` and
+    :meth:`Batch.set_md_heating`."""
+    lib = load_library()
+    dirs = []
+    for name in os.listdir(root):
+        if name.startswith("TMP.") and name[4:].isdigit():
+            dirs.append((int(name[4:]), os.path.join(root, name)))
+    mols = []
+    for n, d in sorted(dirs):
+        nat = np.zeros(1, dtype=np.int32)
+        p = os.path.join(d, "start.xyz").encode()
+        if lib.qcx_read_xyz(p, 0, _ip(nat), None, None) != 0:
+            raise RuntimeError(_err(lib))
+        na = int(nat[0])
+        Z = np.zeros(na, dtype=np.int32)
+        xyz = np.zeros((na, 3))
+        if lib.qcx_read_xyz(p, na, _ip(nat), _ip(Z), _dp(xyz)) != 0:
+            raise RuntimeError(_err(lib))
+        itrj = np.zeros(1, dtype=np.int32)
+        eimp, tadd = np.zeros(1), np.zeros(1)
+        vel, velof = np.zeros((na, 3)), np.zeros(na)
+        if lib.qcx_read_start(os.path.join(d, "qcxms.start").encode(), na, _ip(itrj), _dp(eimp), _dp(tadd),
+                              _dp(vel), _dp(velof)) != 0:
+            raise RuntimeError(_err(lib))
+        mols.append({"Z": Z, "xyz": xyz, "vel": vel, "velof": velof, "eimp": float(eimp[0]), "tadd": float(tadd[0]),
+                     "itrj": int(itrj[0]), "mass": np.array([constants.MASS_AU[int(z)] for z in Z]),
+                     "charge": charge})
+    return mols
 
 
 def fragment_ips(structs, mchrg=1, etemp=300.0, precision=0, method=gfn2_xtb):

@@ -1,0 +1,168 @@
+// Trajectory start files of a QCxMS ensemble, read on the host so that a
+// batched driver can replace the one-process-per-trajectory fan-out.
+//
+// The production run writes, per trajectory n, TMPQCXMS/TMP.n/start.xyz (the
+// structure, xyz format in Angstrom, written with mctc-io's write_structure)
+// and TMPQCXMS/TMP.n/qcxms.start (wrstart, src/utility.f90:321-373):
+//   line 1        the trajectory number, format (i4)
+//   line 2        eimp (Eh), format (D22.14)
+//   line 3        tadd (atomic time units), format (D22.14)
+//   lines 4..     per atom vx vy vz velof, format (7D22.14) (4 fields used)
+// rdstart (src/utility.f90:379-422) reads the same layout back.
+#include <cctype>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qcxgpu.h"
+#include "qcx_kernels.h"
+
+namespace {
+
+// Angstrom -> Bohr, src/xtb_mctc_convert.f90:24-25
+constexpr double kAAtoAU = 1.0 / 0.52917726;
+
+const char* const kSymbols[] = {"",  "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",
+                                "Ne", "Na", "Mg", "Al", "Si", "P",  "S",  "Cl", "Ar"};
+
+bool read_lines(const char* path, std::vector<std::string>& lines) {
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  std::string cur;
+  int c;
+  while ((c = std::fgetc(f)) != EOF) {
+    if (c == '\n') {
+      lines.push_back(cur);
+      cur.clear();
+    } else if (c != '\r') {
+      cur.push_back((char)c);
+    }
+  }
+  if (!cur.empty()) lines.push_back(cur);
+  std::fclose(f);
+  return true;
+}
+
+// one Fortran real in E or D exponent notation
+bool parse_real(const std::string& tok, double* out) {
+  std::string t = tok;
+  for (char& ch : t)
+    if (ch == 'D' || ch == 'd') ch = 'E';
+  char* end = nullptr;
+  *out = std::strtod(t.c_str(), &end);
+  return end && *end == '\0' && !t.empty();
+}
+
+// Fields of a fixed-width Fortran record: width characters each.
+bool fixed_fields(const std::string& line, int width, int n, double* out) {
+  for (int k = 0; k < n; ++k) {
+    if ((int)line.size() < (k + 1) * width) return false;
+    std::string f = line.substr((size_t)k * width, (size_t)width);
+    size_t a = f.find_first_not_of(' '), b = f.find_last_not_of(' ');
+    if (a == std::string::npos) return false;
+    if (!parse_real(f.substr(a, b - a + 1), out + k)) return false;
+  }
+  return true;
+}
+
+std::vector<std::string> split(const std::string& s) {
+  std::vector<std::string> out;
+  size_t i = 0;
+  while (i < s.size()) {
+    while (i < s.size() && std::isspace((unsigned char)s[i])) ++i;
+    size_t j = i;
+    while (j < s.size() && !std::isspace((unsigned char)s[j])) ++j;
+    if (j > i) out.push_back(s.substr(i, j - i));
+    i = j;
+  }
+  return out;
+}
+
+int symbol_to_z(const std::string& tok) {
+  if (std::isdigit((unsigned char)tok[0])) {
+    int z = std::atoi(tok.c_str());
+    return (z >= 1 && z <= 18) ? z : -1;
+  }
+  std::string s;
+  for (char ch : tok)
+    if (std::isalpha((unsigned char)ch)) s.push_back(s.empty() ? (char)std::toupper(ch) : (char)std::tolower(ch));
+  for (int z = 1; z <= 18; ++z)
+    if (s == kSymbols[z]) return z;
+  return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qcx_read_xyz(const char* path, int max_nat, int32_t* nat, int32_t* num, double* xyz) {
+  std::vector<std::string> lines;
+  if (!path || !nat || max_nat < 0 || !read_lines(path, lines)) {
+    qcx::set_last_error(std::string("qcx_read_xyz: cannot read ") + (path ? path : "(null)"));
+    return -1;
+  }
+  std::vector<std::string> head = lines.empty() ? std::vector<std::string>() : split(lines[0]);
+  int n = head.size() == 1 ? std::atoi(head[0].c_str()) : -1;
+  if (n < 1 || (int)lines.size() < n + 2) {
+    qcx::set_last_error(std::string("qcx_read_xyz: not an xyz file: ") + path);
+    return -1;
+  }
+  *nat = n;
+  if (!num && !xyz) return 0;  // size query
+  if (n > max_nat) {
+    qcx::set_last_error("qcx_read_xyz: more atoms than max_nat");
+    return -1;
+  }
+  for (int a = 0; a < n; ++a) {
+    std::vector<std::string> t = split(lines[2 + a]);
+    double v[3];
+    int z = t.size() >= 4 ? symbol_to_z(t[0]) : -1;
+    if (z < 1 || !parse_real(t[1], v) || !parse_real(t[2], v + 1) || !parse_real(t[3], v + 2)) {
+      qcx::set_last_error(std::string("qcx_read_xyz: bad atom line (elements 1..18) in ") + path);
+      return -1;
+    }
+    if (num) num[a] = z;
+    if (xyz)
+      for (int d = 0; d < 3; ++d) xyz[3 * a + d] = v[d] * kAAtoAU;
+  }
+  return 0;
+}
+
+int qcx_read_start(const char* path, int nat, int32_t* itrj, double* eimp, double* tadd, double* vel,
+                   double* velof) {
+  std::vector<std::string> lines;
+  if (!path || nat < 1 || !read_lines(path, lines)) {
+    qcx::set_last_error(std::string("qcx_read_start: cannot read ") + (path ? path : "(null)"));
+    return -1;
+  }
+  if ((int)lines.size() < 3 + nat) {
+    qcx::set_last_error(std::string("qcx_read_start: fewer lines than 3 + nat in ") + path);
+    return -1;
+  }
+  std::vector<std::string> t = split(lines[0]);
+  double e, ta;
+  if (t.size() != 1 || !fixed_fields(lines[1], 22, 1, &e) || !fixed_fields(lines[2], 22, 1, &ta)) {
+    qcx::set_last_error(std::string("qcx_read_start: bad header in ") + path);
+    return -1;
+  }
+  if (itrj) *itrj = std::atoi(t[0].c_str());
+  if (eimp) *eimp = e;
+  if (tadd) *tadd = ta;
+  for (int a = 0; a < nat; ++a) {
+    double v[4];
+    if (!fixed_fields(lines[3 + a], 22, 4, v)) {
+      qcx::set_last_error(std::string("qcx_read_start: bad velocity record in ") + path);
+      return -1;
+    }
+    if (vel)
+      for (int d = 0; d < 3; ++d) vel[3 * a + d] = v[d];
+    if (velof) velof[a] = v[3];
+  }
+  return 0;
+}
+
+}  // extern "C"

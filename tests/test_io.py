@@ -1,0 +1,77 @@
+"""Ensemble start files (TMPQCXMS/TMP.n/start.xyz and qcxms.start, written by
+wrstart, src/utility.f90:321-373, read by rdstart, src/utility.f90:379-422).
+
+CPU: the library's readers against an independent parse of the fixture in
+tests/golden/TMPQCXMS (made by tests/golden/make_start_files.py in wrstart's
+layout): every value exact. GPU: the loaded ensemble drives a batch with the
+device heating and exit rules."""
+import os
+
+import numpy as np
+import pytest
+
+import qcxms_gb300 as qg
+from qcxms_gb300 import constants
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "TMPQCXMS")
+
+
+def _fortran_reals(line, width=22):
+    return [float(line[i:i + width].replace("D", "E")) for i in range(0, len(line.rstrip("\n")), width)]
+
+
+def test_read_ensemble_matches_files():
+    mols = qg.read_ensemble(GOLDEN)
+    assert [m["itrj"] for m in mols] == [1, 2, 10]
+    for m in mols:
+        d = os.path.join(GOLDEN, "TMP.%d" % m["itrj"])
+        lines = open(os.path.join(d, "qcxms.start")).read().splitlines()
+        assert int(lines[0]) == m["itrj"]
+        assert m["eimp"] == _fortran_reals(lines[1])[0] and m["tadd"] == _fortran_reals(lines[2])[0]
+        for a in range(len(m["Z"])):
+            v = _fortran_reals(lines[3 + a])
+            assert list(m["vel"][a]) == v[:3] and m["velof"][a] == v[3]
+        xl = open(os.path.join(d, "start.xyz")).read().splitlines()
+        assert int(xl[0]) == len(m["Z"])
+        for a in range(len(m["Z"])):
+            t = xl[2 + a].split()
+            assert constants.SYMBOLS[m["Z"][a]] == t[0]
+            assert list(m["xyz"][a]) == [float(x) * (1.0 / 0.52917726) for x in t[1:4]]
+        assert np.array_equal(m["mass"], [constants.MASS_AU[z] for z in m["Z"]])
+
+
+def test_readers_reject_bad_input(tmp_path):
+    lib = qg.load_library()
+    nat = np.zeros(1, dtype=np.int32)
+    assert lib.qcx_read_xyz(str(tmp_path / "missing.xyz").encode(), 0, qg._ip(nat), None, None) == -1
+    bad = tmp_path / "bad.xyz"
+    bad.write_text("2\n\nC 0 0 0\nXx 1 0 0\n")
+    Z, xyz = np.zeros(2, dtype=np.int32), np.zeros((2, 3))
+    assert lib.qcx_read_xyz(str(bad).encode(), 2, qg._ip(nat), qg._ip(Z), qg._dp(xyz)) == -1
+    assert b"bad atom line" in lib.qcx_last_error()
+    # more atoms than the caller's arrays hold
+    ok = tmp_path / "ok.xyz"
+    ok.write_text("2\ncomment\nC 0 0 0\n6 1.5 0 0\n")
+    assert lib.qcx_read_xyz(str(ok).encode(), 1, qg._ip(nat), qg._ip(Z), qg._dp(xyz)) == -1
+    assert lib.qcx_read_xyz(str(ok).encode(), 2, qg._ip(nat), qg._ip(Z), qg._dp(xyz)) == 0
+    assert list(Z) == [6, 6] and xyz[1, 0] == 1.5 / 0.52917726
+    short = tmp_path / "qcxms.start"
+    short.write_text("   1\n  0.10000000000000D+00\n")
+    assert lib.qcx_read_start(str(short).encode(), 2, None, None, None, None, None) == -1
+
+
+@pytest.mark.gpu
+def test_gpu_ensemble_drives_batch(gpu):
+    mols = qg.read_ensemble(GOLDEN)
+    dt = 0.5 * constants.FSTOAU
+    b = qg.Batch(mols)
+    b.egrad()
+    b.set_md_heating([m["eimp"] for m in mols], [m["tadd"] for m in mols], dt,
+                     np.concatenate([m["velof"] for m in mols]))
+    b.set_md_rules(2, 250, 1000)
+    b.step(5, dt)
+    st = b.md_state()
+    active, _ = b.progress()
+    # every trajectory still running has taken the 5 steps after the first loop top
+    assert ((st["nstep"] == 6) | (st["done"] == 1)).all() and (st["nstep"][active > 0] == 6).all()
+    assert active.sum() >= 2
