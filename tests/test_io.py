@@ -75,3 +75,15 @@ def test_gpu_ensemble_drives_batch(gpu):
     # every trajectory still running has taken the 5 steps after the first loop top
     assert ((st["nstep"] == 6) | (st["done"] == 1)).all() and (st["nstep"][active > 0] == 6).all()
     assert active.sum() >= 2
+
+
+@pytest.mark.gpu
+def test_gpu_driver_runs_ensemble_to_the_end(gpu):
+    from qcxms_gb300 import driver
+    res = driver.run_ensemble(GOLDEN, etemp=300.0, max_steps=30, block=10)
+    assert [t["itrj"] for t in res] == [1, 2, 10]
+    for t in res:
+        assert 1 <= t["nstep"] <= 30 and len(t["frag"]) > 0
+        # trajectories that ended in fragments carry their IPs
+        assert ("fragip_eV" in t) == (2 <= t["nfrag"] <= 10)
+    assert any(t["nstep"] == 30 and t["mdok"] for t in res)
