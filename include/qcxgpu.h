@@ -236,6 +236,30 @@ int qcx_fragment_ips(int method, int ntraj, const int32_t* nat, const int32_t* n
 int qcx_boltz(int units, int nfrag, int mchrg, double temp, const double* ip, double* fragchrg2);
 
 /*
+ * Stop rules of the collision MD (CID, src/cid.f90:739-1052) on the device,
+ * evaluated after every step of qcx_batch_step inside the step graph. Every
+ * molecule is the ion followed by ONE collision gas atom (the last atom). Per
+ * step: a failed energy evaluation ends the run (failed = 1); the ion's
+ * centre-of-mass speed from its displacement, its internal temperature
+ * (tinit at the first step) and the running mean avg_temp, and the collision
+ * energy in the centre-of-mass frame ecom_ev (src/cid.f90:769-793, 1209-1215);
+ * the ion's fragments (fragment_structure over the ion's atoms, rcut 3.0);
+ * every 10 steps the gas atom's distance from the ion's centre of mass: after 5
+ * growing checks in a row the collision is marked and the run ends
+ * 800 * (2 tstep in fs) steps later, or add_steps (by ion size,
+ * src/cid.f90:276-278) after a fragmentation that follows the collision; and
+ * at ntot steps at the latest (src/cid.f90:955-1036). A run that ends stops
+ * (active flag 0). Call after qcx_batch_egrad of the start geometry; replaces
+ * the MD rules of qcx_batch_set_md_rules; new coordinates switch it off. Not
+ * covered: the averaged structures and the output files.
+ */
+int qcx_batch_set_cid_rules(qcx_batch* b, double tinit, int ntot);
+/* State of the collision rules per trajectory (any pointer may be NULL). */
+int qcx_batch_get_cid_state(qcx_batch* b, int32_t* nstep, int32_t* nfrag, int32_t* collided, int32_t* fragmented,
+                            int32_t* total_steps, int32_t* done, int32_t* failed, double* avg_temp,
+                            double* ecom_ev);
+
+/*
  * Trajectory start files of a QCxMS ensemble (host only, no GPU work), so
  * that a batched driver can load TMPQCXMS/TMP.n/ of every trajectory instead
  * of starting one process per trajectory (bin/pqcxms:88-99).

@@ -359,6 +359,97 @@ def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more,
     return s
 
 
+def _com(xyz, mass, nuc):
+    """center_of_mass (src/utility.f90:541-562) of the first nuc atoms."""
+    cm, tm = [0.0, 0.0, 0.0], 0.0
+    for i in range(nuc):
+        for d in range(3):
+            cm[d] = cm[d] + mass[i] * xyz[i][d]
+        tm = tm + mass[i]
+    return [c / tm for c in cm]
+
+
+def _norm3(x, y, z):
+    return float(np.sqrt((x * x + y * y) + z * z))
+
+
+def cid_rules_begin(xyz, mass, ntot):
+    """State before the collision loop (src/cid.f90:715-724); the last atom is the gas atom."""
+    nuc = len(mass) - 1
+    s = {"nstep": 0, "m": 0, "step_counter": 0, "collided": 0, "fragmented": 0, "total_steps": ntot, "nfrag": 1,
+         "done": 0, "failed": 0, "distance_dump": 0, "ttime": 0.0, "tav": 0.0, "avgT": 0.0, "new_temp": 0.0,
+         "ecom": 0.0}
+    sm = 0.0
+    for i in range(nuc):
+        sm = sm + mass[i]
+    s["summass"] = sm
+    cm = _com(xyz, mass, nuc)
+    s["old_cm"] = cm
+    g = xyz[nuc]
+    d0 = _norm3(g[0] - cm[0], g[1] - cm[1], g[2] - cm[2])
+    s["lowest"] = s["highest"] = d0
+    return s
+
+
+def cid_rules_step(s, failed, xyz, vel, mass, nfrag, tstep, tinit):
+    """One step of the collision loop after leapfrog + egrad (src/cid.f90:739-1036)."""
+    if s["done"]:
+        return s
+    autofs = 1.0 / FSTOAU
+    mstoau = 1.0 / 2.18769126364e6
+    nuc = len(mass) - 1
+    s["nstep"] += 1
+    s["ttime"] = s["ttime"] + tstep * autofs
+    s["distance_dump"] += 1
+    if failed:
+        s["done"], s["failed"] = 1, 1
+        return s
+    cm = _com(xyz, mass, nuc)
+    oc = s["old_cm"]
+    cm_out = _norm3(cm[0] - oc[0], cm[1] - oc[1], cm[2] - oc[2])
+    s["old_cm"] = cm
+    new_velo = (cm_out / tstep) / mstoau if s["nstep"] != 1 else 0.0
+    ek = 0.0
+    for i in range(nuc):
+        v = vel[i]
+        ek = ek + mass[i] * ((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])
+    ek = ek * 0.5
+    x = new_velo * mstoau
+    e_velo = (0.5 * s["summass"]) * (x * x)
+    ekd = ek - e_velo
+    s["new_temp"] = (2.0 * ekd) / ((3.0 * KB) * float(nuc))
+    if s["nstep"] == 1:
+        s["new_temp"] = tinit
+    s["tav"] = s["tav"] + s["new_temp"]
+    s["m"] += 1
+    s["avgT"] = s["tav"] / s["m"]
+    mgas = mass[nuc]
+    s["ecom"] = ((mgas / (mgas + s["summass"])) * e_velo) * AUTOEV
+    s["nfrag"] = nfrag
+    if s["distance_dump"] == 10:
+        s["distance_dump"] = 0
+        g = xyz[nuc]
+        dist = _norm3(g[0] - cm[0], g[1] - cm[1], g[2] - cm[2])
+        if dist > s["highest"]:
+            s["highest"] = dist
+        if dist < s["lowest"]:
+            s["lowest"] = dist
+        s["step_counter"] = s["step_counter"] + 1 if s["lowest"] < dist else 0
+        if s["step_counter"] == 5:
+            s["collided"] = 1
+            t = 800.0 * ((2.0 * tstep) * autofs)
+            q = float(np.floor(t))  # nint: half away from zero (t > 0)
+            s["total_steps"] = s["nstep"] + int(q) + (1 if t - q >= 0.5 else 0)
+            s["tav"], s["m"] = 0.0, 0
+    if nfrag > 1 and s["collided"] and not s["fragmented"]:
+        add = (nuc // 10) * 1000 if nuc >= 40 else ((nuc // 10) * 500 if nuc > 10 else 0)
+        s["total_steps"] = s["nstep"] + add
+        s["fragmented"] = 1
+    if s["nstep"] >= s["total_steps"]:
+        s["done"] = 1
+    return s
+
+
 def gnorm(grad):
     grad = np.ascontiguousarray(grad, dtype=np.float64)
     return lib().qcxo_gnorm(grad.shape[0], _p(grad))

@@ -91,6 +91,8 @@ def load_library(build_if_missing=True):
     lib.qcx_fragment_ips.argtypes = [c_int, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double),
                                      P(ctypes.c_int32), c_int, c_double, c_int, P(c_double), P(c_double),
                                      P(ctypes.c_int32)]
+    lib.qcx_batch_set_cid_rules.argtypes = [ctypes.c_void_p, c_double, c_int]
+    lib.qcx_batch_get_cid_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 7 + [P(c_double)] * 2
     lib.qcx_batch_set_md_heating.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double), c_double]
     lib.qcx_batch_set_md_rules.argtypes = [ctypes.c_void_p, c_int, c_int, c_int]
     lib.qcx_batch_get_md_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 5 + [P(c_double)] * 3
@@ -324,6 +326,22 @@ class Batch:
         vf = None if velof is None else np.ascontiguousarray(velof, dtype=np.float64)
         self._check(self._lib.qcx_batch_set_md_heating(self._h, _dp(eimp), _dp(tadd), _dp(vf), float(tstep)),
                     "set_md_heating")
+
+    def set_cid_rules(self, tinit, ntot):
+        """Stop rules of the collision MD (src/cid.f90:739-1052) on the device;
+        every molecule is the ion followed by one gas atom. Call after egrad()."""
+        self._check(self._lib.qcx_batch_set_cid_rules(self._h, float(tinit), int(ntot)), "set_cid_rules")
+
+    def cid_state(self):
+        n = self.nmol
+        i32 = lambda: np.zeros(n, dtype=np.int32)
+        v = {k: i32() for k in ("nstep", "nfrag", "collided", "fragmented", "total_steps", "done", "failed")}
+        avg_t, ecom = np.zeros(n), np.zeros(n)
+        self._check(self._lib.qcx_batch_get_cid_state(self._h, _ip(v["nstep"]), _ip(v["nfrag"]), _ip(v["collided"]),
+                                                      _ip(v["fragmented"]), _ip(v["total_steps"]), _ip(v["done"]),
+                                                      _ip(v["failed"]), _dp(avg_t), _dp(ecom)), "cid_state")
+        v["avg_temp"], v["ecom_ev"] = avg_t, ecom
+        return v
 
     def md_state(self):
         n = self.nmol

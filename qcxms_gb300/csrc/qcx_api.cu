@@ -114,6 +114,10 @@ struct qcx_batch {
   double* d_velof = nullptr;    // [natom] velocity scaling weights of the heating
   bool md_heat = false;
   bool md_on = false;
+  // collision MD stop rules on the device (qcx_batch_set_cid_rules)
+  CidState* d_cid = nullptr;
+  bool cid_on = false;
+  CidRules cid_rules{};
   MdRules md_rules{};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -198,6 +202,7 @@ void free_batch(qcx_batch* b) {
   if (b->d_gpairs) cudaFree(b->d_gpairs);
   if (b->d_md) cudaFree(b->d_md);
   if (b->d_md_heat) cudaFree(b->d_md_heat);
+  if (b->d_cid) cudaFree(b->d_cid);
   if (b->d_velof) cudaFree(b->d_velof);
   for (size_t g = 1; g < b->g_stream.size(); ++g)
     if (b->g_stream[g]) cudaStreamDestroy(b->g_stream[g]);
@@ -514,8 +519,50 @@ int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps)
   launch_md_begin(b->dev, b->d_md, b->md_heat ? b->d_md_heat : nullptr, b->stream);
   if (check_launch()) return -1;
   CK(cudaStreamSynchronize(b->stream));
-  if (!b->md_on) drop_graph(b);
+  if (!b->md_on || b->cid_on) drop_graph(b);
   b->md_on = true;
+  b->cid_on = false;
+  return 0;
+}
+
+int qcx_batch_set_cid_rules(qcx_batch* b, double tinit, int ntot) {
+  if (!b || ntot < 1 || b->min_nat < 2) {
+    set_error("qcx_batch_set_cid_rules: ntot >= 1 and molecules of the ion plus one gas atom");
+    return -1;
+  }
+  if (!b->d_cid && dalloc(&b->d_cid, b->nmol)) return -1;
+  b->cid_rules.tinit = tinit;
+  b->cid_rules.ntot = ntot;
+  launch_cid_begin(b->dev, b->d_cid, b->cid_rules, b->stream);
+  if (check_launch()) return -1;
+  CK(cudaStreamSynchronize(b->stream));
+  drop_graph(b);
+  b->cid_on = true;
+  b->md_on = false;
+  return 0;
+}
+
+int qcx_batch_get_cid_state(qcx_batch* b, int32_t* nstep, int32_t* nfrag, int32_t* collided, int32_t* fragmented,
+                            int32_t* total_steps, int32_t* done, int32_t* failed, double* avg_temp,
+                            double* ecom_ev) {
+  if (!b || !b->d_cid) {
+    set_error("qcx_batch_get_cid_state: no collision rules set up (qcx_batch_set_cid_rules)");
+    return -1;
+  }
+  std::vector<CidState> st(b->nmol);
+  CK(cudaMemcpyAsync(st.data(), b->d_cid, sizeof(CidState) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  for (int m = 0; m < b->nmol; ++m) {
+    if (nstep) nstep[m] = st[m].nstep;
+    if (nfrag) nfrag[m] = st[m].nfrag;
+    if (collided) collided[m] = st[m].collided;
+    if (fragmented) fragmented[m] = st[m].fragmented;
+    if (total_steps) total_steps[m] = st[m].total_steps;
+    if (done) done[m] = st[m].done;
+    if (failed) failed[m] = st[m].failed;
+    if (avg_temp) avg_temp[m] = st[m].avgT;
+    if (ecom_ev) ecom_ev[m] = st[m].ecom;
+  }
   return 0;
 }
 
@@ -603,9 +650,10 @@ int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, cons
   if (!b) return -1;
   size_t n3 = sizeof(double) * 3 * b->natom;
   if (xyz) {
-    if (b->md_on) {
-      // new coordinates start new runs: the MD rules must be set up again
+    if (b->md_on || b->cid_on) {
+      // new coordinates start new runs: the MD or collision rules must be set up again
       b->md_on = false;
+      b->cid_on = false;
       drop_graph(b);
     }
     CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));
@@ -648,6 +696,14 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
       MdRules r = b->md_rules;
       r.tstep = tstep;
       launch_md_rules(b->dev, b->d_md, b->d_frag, b->d_nfrag, b->md_heat ? b->d_velof : nullptr, r, b->stream);
+      n += 2;
+    }
+    if (n >= 0 && b->cid_on) {
+      // fragment_structure over the ion's atoms (src/cid.f90:800), then the stop rules
+      launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream, 1);
+      CidRules r = b->cid_rules;
+      r.tstep = tstep;
+      launch_cid_rules(b->dev, b->d_cid, b->d_nfrag, r, b->stream);
       n += 2;
     }
     cudaError_t ce = cudaStreamEndCapture(b->stream, &b->graph);

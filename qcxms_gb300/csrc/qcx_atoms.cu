@@ -384,11 +384,13 @@ void launch_leapfrog(const DevBatch& bt, double tstep, cudaStream_t st) {
 constexpr int kFragThreads = 256;
 
 __global__ void __launch_bounds__(kFragThreads) k_fragments(DevBatch bt, const double* rad, double rcut, int at1,
-                                                            int at2, int* frag, int* nfrag) {
+                                                            int at2, int* frag, int* nfrag, int skip_last) {
   extern __shared__ int fsm[];
   const int mol = blockIdx.x;
   const MolDesc md = bt.mol[mol];
-  const int nat = md.nat, off = md.atom_off;
+  // skip_last: the last atom (a collision gas atom) is not part of the ion; it gets fragment 0
+  const int nat = md.nat - (skip_last && md.nat > 1 ? 1 : 0), off = md.atom_off;
+  if (nat < md.nat && threadIdx.x == 0) frag[off + nat] = 0;
   int* lab = fsm;             // [nat]
   int* flag = fsm + nat;      // [1]
   if (at1 == 0 && at2 == 0) {
@@ -444,8 +446,9 @@ __global__ void __launch_bounds__(kFragThreads) k_fragments(DevBatch bt, const d
 }
 
 void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,
-                      int* nfrag, cudaStream_t st) {
-  k_fragments<<<bt.nmol, kFragThreads, sizeof(int) * (max_nat + 1), st>>>(bt, rad, rcut, at1, at2, frag, nfrag);
+                      int* nfrag, cudaStream_t st, int skip_last) {
+  k_fragments<<<bt.nmol, kFragThreads, sizeof(int) * (max_nat + 1), st>>>(bt, rad, rcut, at1, at2, frag, nfrag,
+                                                                          skip_last);
 }
 
 }  // namespace qcx

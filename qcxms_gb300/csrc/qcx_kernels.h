@@ -20,8 +20,9 @@ void launch_grad_atoms(const DevBatch& bt, cudaStream_t st);
 void launch_leapfrog(const DevBatch& bt, double tstep, cudaStream_t st);
 void launch_zero_grad(const DevBatch& bt, cudaStream_t st);
 // fragment numbers of every molecule's atoms (frag[natom]) and fragment counts (nfrag[nmol])
+// skip_last = 1: the last atom of every molecule is left out (fragment 0)
 void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,
-                      int* nfrag, cudaStream_t st);
+                      int* nfrag, cudaStream_t st, int skip_last = 0);
 
 // Per-trajectory state of the MD bookkeeping and exit rules (src/md.f90:285-682)
 struct MdState {
@@ -39,6 +40,20 @@ struct MdRules {
 void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, cudaStream_t stream);
 void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
                      const MdRules& r, cudaStream_t stream);
+
+// Per-trajectory state of the collision MD stop rules (src/cid.f90:739-1052);
+// the last atom of every molecule is the collision gas atom
+struct CidState {
+  int nstep, m, step_counter, collided, fragmented, total_steps, nfrag, done, failed, distance_dump;
+  double ttime, tav, avgT, lowest, highest, new_temp, ecom, summass;
+  double old_cm[3];
+};
+struct CidRules {
+  double tinit, tstep;
+  int ntot;
+};
+void launch_cid_begin(const DevBatch& bt, CidState* st, const CidRules& r, cudaStream_t stream);
+void launch_cid_rules(const DevBatch& bt, CidState* st, const int* nfrag, const CidRules& r, cudaStream_t stream);
 
 // sets the text qcx_last_error() returns
 void set_last_error(const std::string& s);
