@@ -156,6 +156,12 @@ int qcx_batch_fragments(qcx_batch* b, double rcut, int at1, int at2, int32_t* fr
  */
 int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps);
 
+/* Averaged structure of every trajectory, axyz = the mean of the coordinates
+ * at the loop tops of the current window of avdump = 50 steps
+ * (src/md.f90:352-362, 695); QCxMS hands it to analyse for the fragment IPs.
+ * axyz [natom][3]; requires qcx_batch_set_md_rules. */
+int qcx_batch_get_md_avg_xyz(qcx_batch* b, double* axyz);
+
 /* Heating of the first steps of an electron-impact run (impactscale,
  * src/impact.f90:12-55, called by src/md.f90:439-441 while nstep <= nadd and
  * the molecule is one fragment): each step the velocities are scaled by

@@ -238,8 +238,9 @@ def _temp(e, n):
         return float(np.float64(e) / (float(np.float32(1.5) * np.float32(n)) * KB))
 
 
-def md_rules_top(s, epot, ekin, nuc):
-    """Top of the MD loop (src/md.f90:286-342), nadd = 0, it > 0, isec = 1."""
+def md_rules_top(s, epot, ekin, nuc, xyz=None):
+    """Top of the MD loop (src/md.f90:286-362), it > 0, isec = 1; with xyz the
+    running coordinate sum of the averaged structure (window of 50 steps)."""
     s["nstep"] += 1
     t = _temp(ekin, nuc)
     s["tav"] = s["tav"] + t
@@ -257,7 +258,21 @@ def md_rules_top(s, epot, ekin, nuc):
         s["mdok"] = 1 if 1 < s["nfrag"] <= 4 else 0
         s["done"] = 1
         return True
+    if s["kdump"] > 50 - 1:
+        s["kdump"] = 0
+        s["avxyz"] = None
+    if xyz is not None:
+        if s["avxyz"] is None:
+            s["avxyz"] = [[0.0, 0.0, 0.0] for _ in range(nuc)]
+        for i in range(nuc):
+            for d in range(3):
+                s["avxyz"][i][d] = s["avxyz"][i][d] + xyz[i][d]
     return False
+
+
+def md_avg_xyz(s):
+    """axyz = avxyz / kdump (src/md.f90:695)."""
+    return [[c / s["kdump"] for c in row] for row in s["avxyz"]]
 
 
 def _ekinet(vel, mass, velof=None, scal=0.0):
@@ -293,12 +308,12 @@ def md_heating(eimp, tadd, tstep):
     return eimp, tstep / (tadd + tstep), int((tadd + tstep) / tstep - 1.0)
 
 
-def md_rules_begin(vel, mass, epot, heat=None):
+def md_rules_begin(vel, mass, epot, heat=None, xyz=None):
     """State before the loop: ekinet (src/mdinit.f90:57-76) and the first top.
     heat = (eimp, fadd, nadd) of md_heating, or None."""
     s = {"nstep": 0, "nfrag": 1, "fconst": 0, "morestep": 0, "fragstate": 0, "mdok": 0, "done": 0, "tav": 0.0,
          "epav": 0.0, "ekav": 0.0, "edum": 0.0, "eerror": 0.0, "ttime": 0.0, "dtime": 0.0, "fragT": [0.0] * 10,
-         "eimp": 0.0, "fadd": 0.0, "nadd": 0, "heat_failed": 0}
+         "eimp": 0.0, "fadd": 0.0, "nadd": 0, "heat_failed": 0, "kdump": 50, "avxyz": None}
     if heat is not None:
         s["eimp"], s["fadd"], s["nadd"] = heat
     ek = _ekinet(vel, mass)
@@ -306,17 +321,18 @@ def md_rules_begin(vel, mass, epot, heat=None):
     if epot == 0:
         s["done"] = 1  # src/md.f90:185
     else:
-        md_rules_top(s, epot, ek, len(mass))
+        md_rules_top(s, epot, ek, len(mass), xyz)
     return s
 
 
-def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more, max_steps, velof=None):
+def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more, max_steps, velof=None, xyz=None):
     """Rest of one loop iteration after leapfrog + egrad (src/md.f90:426-679,
     electron-impact branch), then the next top. epot = 0 for a failed call.
     vel (the velocities after leapfrog) is scaled in place while heating."""
     if s["done"]:
         return s
     s["ttime"] = s["ttime"] + tstep / FSTOAU
+    s["kdump"] += 1  # src/md.f90:400
     if s["nfrag"] == 1:
         s["morestep"] = 0
     if s["nfrag"] > 1 and s["dtime"] < 1.0e-6:
@@ -355,7 +371,7 @@ def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more,
     if stop:
         s["done"] = 1
     else:
-        md_rules_top(s, epot, ekin, len(mass))
+        md_rules_top(s, epot, ekin, len(mass), xyz)
     return s
 
 

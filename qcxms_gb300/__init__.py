@@ -91,6 +91,7 @@ def load_library(build_if_missing=True):
     lib.qcx_fragment_ips.argtypes = [c_int, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double),
                                      P(ctypes.c_int32), c_int, c_double, c_int, P(c_double), P(c_double),
                                      P(ctypes.c_int32)]
+    lib.qcx_batch_get_md_avg_xyz.argtypes = [ctypes.c_void_p, P(c_double)]
     lib.qcx_batch_set_cid_rules.argtypes = [ctypes.c_void_p, c_double, c_int]
     lib.qcx_batch_get_cid_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 7 + [P(c_double)] * 2
     lib.qcx_batch_set_md_heating.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double), c_double]
@@ -342,6 +343,12 @@ class Batch:
                                                       _ip(v["failed"]), _dp(avg_t), _dp(ecom)), "cid_state")
         v["avg_temp"], v["ecom_ev"] = avg_t, ecom
         return v
+
+    def md_avg_xyz(self):
+        """Averaged structure (src/md.f90:352-362, 695) of every trajectory, [natom][3]."""
+        out = np.zeros((self.natom, 3))
+        self._check(self._lib.qcx_batch_get_md_avg_xyz(self._h, _dp(out)), "md_avg_xyz")
+        return out
 
     def md_state(self):
         n = self.nmol

@@ -112,6 +112,7 @@ struct qcx_batch {
   MdState* d_md = nullptr;
   double* d_md_heat = nullptr;  // [nmol][3] eimp, fadd, nadd (qcx_batch_set_md_heating)
   double* d_velof = nullptr;    // [natom] velocity scaling weights of the heating
+  double* d_avxyz = nullptr;    // [natom][3] coordinate sums of the averaged structure
   bool md_heat = false;
   bool md_on = false;
   // collision MD stop rules on the device (qcx_batch_set_cid_rules)
@@ -202,6 +203,7 @@ void free_batch(qcx_batch* b) {
   if (b->d_gpairs) cudaFree(b->d_gpairs);
   if (b->d_md) cudaFree(b->d_md);
   if (b->d_md_heat) cudaFree(b->d_md_heat);
+  if (b->d_avxyz) cudaFree(b->d_avxyz);
   if (b->d_cid) cudaFree(b->d_cid);
   if (b->d_velof) cudaFree(b->d_velof);
   for (size_t g = 1; g < b->g_stream.size(); ++g)
@@ -513,15 +515,34 @@ int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps)
     return -1;
   }
   if (!b->d_md && dalloc(&b->d_md, b->nmol)) return -1;
+  if (!b->d_avxyz && dalloc(&b->d_avxyz, 3 * (size_t)b->natom)) return -1;
+  CK(cudaMemsetAsync(b->d_avxyz, 0, sizeof(double) * 3 * b->natom, b->stream));
   b->md_rules.nfragexit = nfragexit;
   b->md_rules.more = more;
   b->md_rules.max_steps = max_steps;
-  launch_md_begin(b->dev, b->d_md, b->md_heat ? b->d_md_heat : nullptr, b->stream);
+  launch_md_begin(b->dev, b->d_md, b->md_heat ? b->d_md_heat : nullptr, b->d_avxyz, b->stream);
   if (check_launch()) return -1;
   CK(cudaStreamSynchronize(b->stream));
   if (!b->md_on || b->cid_on) drop_graph(b);
   b->md_on = true;
   b->cid_on = false;
+  return 0;
+}
+
+int qcx_batch_get_md_avg_xyz(qcx_batch* b, double* axyz) {
+  if (!b || !b->d_md || !b->d_avxyz || !axyz) {
+    set_error("qcx_batch_get_md_avg_xyz: no MD rules set up (qcx_batch_set_md_rules)");
+    return -1;
+  }
+  std::vector<MdState> st(b->nmol);
+  CK(cudaMemcpyAsync(st.data(), b->d_md, sizeof(MdState) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaMemcpyAsync(axyz, b->d_avxyz, sizeof(double) * 3 * b->natom, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  // axyz = avxyz / kdump (src/md.f90:695)
+  for (int m = 0; m < b->nmol; ++m) {
+    const MolDesc& md = b->mol[m];
+    for (int k = 0; k < 3 * md.nat; ++k) axyz[3LL * md.atom_off + k] /= (double)st[m].kdump;
+  }
   return 0;
 }
 
@@ -695,7 +716,8 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
       launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream);
       MdRules r = b->md_rules;
       r.tstep = tstep;
-      launch_md_rules(b->dev, b->d_md, b->d_frag, b->d_nfrag, b->md_heat ? b->d_velof : nullptr, r, b->stream);
+      launch_md_rules(b->dev, b->d_md, b->d_frag, b->d_nfrag, b->md_heat ? b->d_velof : nullptr, b->d_avxyz, r,
+                      b->stream);
       n += 2;
     }
     if (n >= 0 && b->cid_on) {

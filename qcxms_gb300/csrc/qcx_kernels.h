@@ -27,7 +27,7 @@ void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double
 // Per-trajectory state of the MD bookkeeping and exit rules (src/md.f90:285-682)
 struct MdState {
   int nstep, nfrag, fconst, morestep, fragstate, mdok, done, heat_failed;
-  int nadd, pad;
+  int nadd, kdump;  // kdump: steps in the current window of the averaged structure (src/md.f90:352-362)
   double tav, epav, ekav, edum, eerror, ttime, dtime;
   double eimp, fadd, ekinstart;  // heating of the first nadd steps (impactscale)
   double fragT[10];
@@ -37,9 +37,10 @@ struct MdRules {
   double tstep;
 };
 // heat [nmol][3] = (eimp, fadd, nadd) or nullptr (no heating); velof [natom] or nullptr
-void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, cudaStream_t stream);
+// avxyz [natom][3]: running sum of the coordinates over the current window of avdump = 50 steps
+void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double* avxyz, cudaStream_t stream);
 void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
-                     const MdRules& r, cudaStream_t stream);
+                     double* avxyz, const MdRules& r, cudaStream_t stream);
 
 // Per-trajectory state of the collision MD stop rules (src/cid.f90:739-1052);
 // the last atom of every molecule is the collision gas atom

@@ -41,8 +41,12 @@ __device__ double epot_of(const DevBatch& bt, int mol) {
   return bt.energy[(long long)mol * kNumEnergy + kETotal];
 }
 
-// top of the loop (src/md.f90:286-342); returns true when the run ends here
-__device__ bool md_top(MdState& s, double epot, double ekin, int nuc) {
+// window of the averaged structure: avdump = 50 steps (src/md.f90:89)
+constexpr int kAvDump = 50;
+
+// top of the loop (src/md.f90:286-362); returns true when the run ends here.
+// xyz/avxyz: this molecule's coordinates and running coordinate sum.
+__device__ bool md_top(MdState& s, double epot, double ekin, int nuc, const double* xyz, double* avxyz) {
   s.nstep += 1;
   const double t = temp_of(ekin, nuc);
   s.tav = __dadd_rn(s.tav, t);
@@ -63,8 +67,15 @@ __device__ bool md_top(MdState& s, double epot, double ekin, int nuc) {
     // with fragments already formed the trajectory is taken anyway (isec = 1)
     s.mdok = (s.nfrag > 1 && s.nfrag <= 4) ? 1 : 0;
     s.done = 1;
+    return true;
   }
-  return err;
+  // averaged structure over the last avdump steps (src/md.f90:352-362)
+  if (s.kdump > kAvDump - 1) {
+    s.kdump = 0;
+    for (int k = 0; k < 3 * nuc; ++k) avxyz[k] = 0.0;
+  }
+  for (int k = 0; k < 3 * nuc; ++k) avxyz[k] = __dadd_rn(avxyz[k], xyz[k]);
+  return false;
 }
 
 // kinetic energy of the velocities v * (1 + velof * scal) (ekinet, src/mdinit.f90:57-76)
@@ -109,11 +120,12 @@ __device__ bool impact_scale(const DevBatch& bt, const MolDesc& md, const double
 
 // Start of the loop: Ekin of the current velocities (ekinet,
 // src/mdinit.f90:57-76), Epot of the last evaluation, then the first top.
-__global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat) {
+__global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat, double* avxyz) {
   const int mol = blockIdx.x * blockDim.x + threadIdx.x;
   if (mol >= bt.nmol) return;
   MdState s = {};
   s.nfrag = 1;
+  s.kdump = kAvDump;
   if (heat) {
     s.eimp = heat[3 * mol];
     s.fadd = heat[3 * mol + 1];
@@ -137,7 +149,7 @@ __global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat) {
   if (epot == 0.0) {
     s.done = 1;  // src/md.f90:185: no run without a starting energy
   } else {
-    md_top(s, epot, ek, md.nat);
+    md_top(s, epot, ek, md.nat, bt.xyz + 3LL * md.atom_off, avxyz + 3LL * md.atom_off);
   }
   if (s.done) bt.active[mol] = 0;
   st[mol] = s;
@@ -146,13 +158,14 @@ __global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat) {
 // After a step (leapfrog, egrad, fragment numbers of the new coordinates):
 // the end of the loop body, then the top of the next iteration.
 __global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
-                           MdRules r) {
+                           double* avxyz, MdRules r) {
   const int mol = blockIdx.x * blockDim.x + threadIdx.x;
   if (mol >= bt.nmol) return;
   MdState s = st[mol];
   if (s.done) return;
   const MolDesc md = bt.mol[mol];
   s.ttime = __dadd_rn(s.ttime, __ddiv_rn(r.tstep, QCX_FSTOAU));
+  s.kdump += 1;  // src/md.f90:400
   // src/md.f90:426-428, with the fragment count of the previous step
   if (s.nfrag == 1) s.morestep = 0;
   if (s.nfrag > 1 && s.dtime < 1.0e-6) s.dtime = __ddiv_rn(s.ttime, 1000.0);
@@ -216,19 +229,19 @@ __global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int*
   if (exit_now) {
     s.done = 1;
   } else {
-    md_top(s, epot_of(bt, mol), bt.ekin[mol], md.nat);
+    md_top(s, epot_of(bt, mol), bt.ekin[mol], md.nat, bt.xyz + 3LL * md.atom_off, avxyz + 3LL * md.atom_off);
   }
   if (s.done) bt.active[mol] = 0;
   st[mol] = s;
 }
 
-void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, cudaStream_t stream) {
-  k_md_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, heat);
+void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double* avxyz, cudaStream_t stream) {
+  k_md_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, heat, avxyz);
 }
 
 void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
-                     const MdRules& r, cudaStream_t stream) {
-  k_md_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, frag, nfrag, velof, r);
+                     double* avxyz, const MdRules& r, cudaStream_t stream) {
+  k_md_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, frag, nfrag, velof, avxyz, r);
 }
 
 }  // namespace qcx

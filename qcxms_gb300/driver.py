@@ -8,11 +8,12 @@ rules) and, when the ion has fragmented, the fragment IPs of ``analyse``
 1. ``read_ensemble`` loads ``start.xyz`` and ``qcxms.start`` of every trajectory;
 2. one batch runs the MD with the heating (``impactscale``) and the exit rules
    on the device, in blocks of steps, until every trajectory has ended;
-3. the final structures of the trajectories that ended in 2-10 fragments go
+3. the averaged structures of the trajectories that ended in 2-10 fragments go
    through ``fragment_ips`` in one batch (neutral and cation of every fragment).
 
-Differences from the reference: the IPs use the final structure, not the
-average over the last steps (``axyz``, ``src/md.f90:690-696``); the electronic
+As in the reference, the IPs use the structure averaged over the last steps
+(``axyz``, ``src/md.f90:352-362, 695``) with the fragment numbers of the final
+structure. Differences from the reference: the electronic
 temperature is the one given (the reference's default, ``ieetemp = 0``, gives
 the constant 5000 + 20000 ax); the charge assignment of ``write_fragments``
 and the output files are not written.
@@ -45,6 +46,7 @@ def run_ensemble(root, etemp, charge=1, nfragexit=2, more=250, max_steps=10000, 
         b.step(block, dt)
     st = b.md_state()
     r = b.get()
+    axyz = b.md_avg_xyz()
     frag, nfrag = b.fragments(3.0, 1, 0)
     off = np.concatenate([[0], np.cumsum([len(m["Z"]) for m in mols])])
     out = []
@@ -57,7 +59,8 @@ def run_ensemble(root, etemp, charge=1, nfragexit=2, more=250, max_steps=10000, 
                "status": int(r["status"][i])}
         out.append(res)
         if 2 <= nfrag[i] <= 10:
-            ends.append((i, {"Z": m["Z"], "xyz": r["xyz"][sl], "frag": frag[sl]}))
+            # analyse gets the averaged structure (src/md.f90:695, write_fragments.f90:102-106)
+            ends.append((i, {"Z": m["Z"], "xyz": axyz[sl], "frag": frag[sl]}))
     b.close()
     if ends:
         ip, ef, ok = fragment_ips([s for _, s in ends], 1, etemp=ip_etemp, precision=ip_precision)

@@ -61,6 +61,18 @@ def test_oracle_exit_rules_known_answers(oracle_lib):
     assert s["done"] and s["nstep"] == 0
 
 
+def test_oracle_averaged_structure_window(oracle_lib):
+    o = oracle_lib
+    mass, vel = [1.0, 1.0], [[0.0] * 3] * 2
+    pos = lambda k: [[float(k), 0.0, 0.0], [0.0, float(k), 0.0]]
+    s = o.md_rules_begin(vel, mass, -1.0, xyz=pos(0))
+    for k in range(1, 61):
+        o.md_rules_step(s, -1.0, 0.0, vel, mass, [1, 1], 1, DT, 2, 250, 60, xyz=pos(k))
+    # the run ends at the step limit (60 loop tops, positions 0..59); the window
+    # restarted after 50 tops, so it holds positions 50..59
+    assert s["done"] and s["kdump"] == 10 and o.md_avg_xyz(s)[0][0] == sum(range(50, 60)) / 10
+
+
 def test_oracle_temperatures(oracle_lib):
     o = oracle_lib
     mass = [2.0, 3.0, 4.0]
@@ -107,7 +119,8 @@ def test_gpu_md_rules_match_oracle(gpu, oracle_lib):
     ref = []
     for i, m in enumerate(mols):
         e = 0.0 if r0["status"][i] & fail else r0["energy"][i]
-        ref.append(o.md_rules_begin(r0["vel"][off[i]:off[i + 1]], list(m["mass"]), e))
+        ref.append(o.md_rules_begin(r0["vel"][off[i]:off[i + 1]], list(m["mass"]), e,
+                                    xyz=r0["xyz"][off[i]:off[i + 1]]))
     for step in range(max_steps + 2):
         st = b.md_state()
         for i in range(len(mols)):
@@ -125,9 +138,15 @@ def test_gpu_md_rules_match_oracle(gpu, oracle_lib):
         for i, m in enumerate(mols):
             e = 0.0 if r["status"][i] & fail else r["energy"][i]
             o.md_rules_step(ref[i], e, r["ekin"][i], r["vel"][off[i]:off[i + 1]], list(m["mass"]),
-                            list(frag[off[i]:off[i + 1]]), int(nf[i]), DT, nfragexit, more, max_steps)
+                            list(frag[off[i]:off[i + 1]]), int(nf[i]), DT, nfragexit, more, max_steps,
+                            xyz=r["xyz"][off[i]:off[i + 1]])
     st = b.md_state()
     assert st["done"].all()
+    # the averaged structures (src/md.f90:352-362, 695), bit for bit
+    axyz = b.md_avg_xyz()
+    for i in range(len(mols)):
+        if ref[i]["avxyz"] is not None:
+            assert np.array_equal(axyz[off[i]:off[i + 1]], np.array(o.md_avg_xyz(ref[i]))), i
     # the set exercises the fragment exits and the step limit
     assert (st["nfrag"] >= 2).sum() >= 3 and (st["nstep"] == max_steps).sum() >= 1
     active, _ = b.progress()
