@@ -716,6 +716,7 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
       launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream);
       MdRules r = b->md_rules;
       r.tstep = tstep;
+      r.max_nat = b->max_nat;
       launch_md_rules(b->dev, b->d_md, b->d_frag, b->d_nfrag, b->md_heat ? b->d_velof : nullptr, b->d_avxyz, r,
                       b->stream);
       n += 2;

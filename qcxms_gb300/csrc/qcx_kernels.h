@@ -34,6 +34,7 @@ struct MdState {
 };
 struct MdRules {
   int nfragexit, more, max_steps;
+  int max_nat;  // largest molecule (per-warp scratch of the heating)
   double tstep;
 };
 // heat [nmol][3] = (eimp, fadd, nadd) or nullptr (no heating); velof [natom] or nullptr

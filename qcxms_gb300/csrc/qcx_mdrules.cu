@@ -46,7 +46,8 @@ constexpr int kAvDump = 50;
 
 // top of the loop (src/md.f90:286-362); returns true when the run ends here.
 // xyz/avxyz: this molecule's coordinates and running coordinate sum.
-__device__ bool md_top(MdState& s, double epot, double ekin, int nuc, const double* xyz, double* avxyz) {
+__device__ bool md_top(MdState& s, double epot, double ekin, int nuc, const double* xyz, double* avxyz, int lane,
+                       int nlanes) {
   s.nstep += 1;
   const double t = temp_of(ekin, nuc);
   s.tav = __dadd_rn(s.tav, t);
@@ -72,47 +73,51 @@ __device__ bool md_top(MdState& s, double epot, double ekin, int nuc, const doub
   // averaged structure over the last avdump steps (src/md.f90:352-362)
   if (s.kdump > kAvDump - 1) {
     s.kdump = 0;
-    for (int k = 0; k < 3 * nuc; ++k) avxyz[k] = 0.0;
+    for (int k = lane; k < 3 * nuc; k += nlanes) avxyz[k] = 0.0;
   }
-  for (int k = 0; k < 3 * nuc; ++k) avxyz[k] = __dadd_rn(avxyz[k], xyz[k]);
+  for (int k = lane; k < 3 * nuc; k += nlanes) avxyz[k] = __dadd_rn(avxyz[k], xyz[k]);
   return false;
-}
-
-// kinetic energy of the velocities v * (1 + velof * scal) (ekinet, src/mdinit.f90:57-76)
-__device__ double ekin_scaled(const DevBatch& bt, const MolDesc& md, const double* velof, double scal) {
-  double ek = 0.0;
-  for (int i = 0; i < md.nat; ++i) {
-    const long long a = md.atom_off + i;
-    const double f = __dadd_rn(1.0, __dmul_rn(velof ? velof[a] : 1.0, scal));
-    const double* v = bt.vel + 3 * a;
-    const double x = __dmul_rn(v[0], f), y = __dmul_rn(v[1], f), z = __dmul_rn(v[2], f);
-    const double v2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
-    ek = __dadd_rn(ek, __dmul_rn(bt.mass[a], v2));
-  }
-  return __dmul_rn(ek, 0.5);
 }
 
 // impactscale (src/impact.f90:12-55): grow the scaling factor in steps of
 // 0.0002 until the kinetic energy reaches eimp * ff + e0 (within 0.001 Eh) or
 // 20000 steps pass, then scale the velocities. Returns false after 20000 steps
-// (the reference stops the program there).
+// (the reference stops the program there). One warp: the lanes form the
+// per-atom terms m |v (1 + velof scal)|^2 (ekinet, src/mdinit.f90:57-76) into
+// terms[], lane 0 adds them in atom order, so the sum rounds as the reference's.
 __device__ bool impact_scale(const DevBatch& bt, const MolDesc& md, const double* velof, double eimp, double ff,
-                             double e0) {
+                             double e0, double* terms, int lane) {
   const double esoll = __dadd_rn(__dmul_rn(eimp, ff), e0);
   double scal = 0.0;
   int k = 0;
   for (;;) {
     ++k;
-    const double e = ekin_scaled(bt, md, velof, scal);
+    for (int i = lane; i < md.nat; i += 32) {
+      const long long a = md.atom_off + i;
+      const double f = __dadd_rn(1.0, __dmul_rn(velof ? velof[a] : 1.0, scal));
+      const double* v = bt.vel + 3 * a;
+      const double x = __dmul_rn(v[0], f), y = __dmul_rn(v[1], f), z = __dmul_rn(v[2], f);
+      const double v2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+      terms[i] = __dmul_rn(bt.mass[a], v2);
+    }
+    __syncwarp();
+    double e = 0.0;
+    if (lane == 0) {
+      for (int i = 0; i < md.nat; ++i) e = __dadd_rn(e, terms[i]);
+      e = __dmul_rn(e, 0.5);
+    }
+    e = __shfl_sync(0xffffffffu, e, 0);
+    __syncwarp();  // terms[] is rewritten by the next pass
     scal = __dadd_rn(scal, (double)0.0002f);
     if (!(__dsub_rn(esoll, e) > (double)0.001f && k < 20000)) break;
   }
-  for (int i = 0; i < md.nat; ++i) {
+  for (int i = lane; i < md.nat; i += 32) {
     const long long a = md.atom_off + i;
     const double f = __dadd_rn(1.0, __dmul_rn(velof ? velof[a] : 1.0, scal));
     double* v = bt.vel + 3 * a;
     for (int d = 0; d < 3; ++d) v[d] = __dmul_rn(v[d], f);
   }
+  __syncwarp();
   return k < 20000;
 }
 
@@ -149,18 +154,27 @@ __global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat, double*
   if (epot == 0.0) {
     s.done = 1;  // src/md.f90:185: no run without a starting energy
   } else {
-    md_top(s, epot, ek, md.nat, bt.xyz + 3LL * md.atom_off, avxyz + 3LL * md.atom_off);
+    md_top(s, epot, ek, md.nat, bt.xyz + 3LL * md.atom_off, avxyz + 3LL * md.atom_off, 0, 1);
   }
   if (s.done) bt.active[mol] = 0;
   st[mol] = s;
 }
 
 // After a step (leapfrog, egrad, fragment numbers of the new coordinates):
-// the end of the loop body, then the top of the next iteration.
-__global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
-                           double* avxyz, MdRules r) {
-  const int mol = blockIdx.x * blockDim.x + threadIdx.x;
+// the end of the loop body, then the top of the next iteration. One warp per
+// trajectory: every lane keeps the same copy of the state (the scalar
+// bookkeeping runs redundantly), the per-atom work is split over the lanes and
+// lane 0 writes the state.
+constexpr int kRulesWarps = 4;
+
+__global__ void __launch_bounds__(32 * kRulesWarps) k_md_rules(DevBatch bt, MdState* st, const int* frag,
+                                                               const int* nfrag, const double* velof,
+                                                               double* avxyz, MdRules r) {
+  extern __shared__ double md_terms[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int mol = blockIdx.x * kRulesWarps + warp;
   if (mol >= bt.nmol) return;
+  double* terms = md_terms + (size_t)warp * r.max_nat;
   MdState s = st[mol];
   if (s.done) return;
   const MolDesc md = bt.mol[mol];
@@ -171,11 +185,13 @@ __global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int*
   if (s.nfrag > 1 && s.dtime < 1.0e-6) s.dtime = __ddiv_rn(s.ttime, 1000.0);
   // heating while not fragmented (src/md.f90:439-441), before the fragment check
   if (s.nstep <= s.nadd && s.nfrag == 1) {
-    if (!impact_scale(bt, md, velof, s.eimp, __dmul_rn(s.fadd, (double)s.nstep), s.ekinstart)) {
+    if (!impact_scale(bt, md, velof, s.eimp, __dmul_rn(s.fadd, (double)s.nstep), s.ekinstart, terms, lane)) {
       s.heat_failed = 1;
       s.done = 1;
-      bt.active[mol] = 0;
-      st[mol] = s;
+      if (lane == 0) {
+        bt.active[mol] = 0;
+        st[mol] = s;
+      }
       return;
     }
   }
@@ -229,10 +245,13 @@ __global__ void k_md_rules(DevBatch bt, MdState* st, const int* frag, const int*
   if (exit_now) {
     s.done = 1;
   } else {
-    md_top(s, epot_of(bt, mol), bt.ekin[mol], md.nat, bt.xyz + 3LL * md.atom_off, avxyz + 3LL * md.atom_off);
+    md_top(s, epot_of(bt, mol), bt.ekin[mol], md.nat, bt.xyz + 3LL * md.atom_off, avxyz + 3LL * md.atom_off, lane,
+           32);
   }
-  if (s.done) bt.active[mol] = 0;
-  st[mol] = s;
+  if (lane == 0) {
+    if (s.done) bt.active[mol] = 0;
+    st[mol] = s;
+  }
 }
 
 void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double* avxyz, cudaStream_t stream) {
@@ -241,7 +260,8 @@ void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double
 
 void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
                      double* avxyz, const MdRules& r, cudaStream_t stream) {
-  k_md_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, frag, nfrag, velof, avxyz, r);
+  k_md_rules<<<(bt.nmol + kRulesWarps - 1) / kRulesWarps, 32 * kRulesWarps,
+               sizeof(double) * kRulesWarps * r.max_nat, stream>>>(bt, st, frag, nfrag, velof, avxyz, r);
 }
 
 }  // namespace qcx
