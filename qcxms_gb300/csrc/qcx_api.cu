@@ -595,8 +595,8 @@ int qcx_batch_set_md_heating(qcx_batch* b, const double* eimp, const double* tad
   }
   std::vector<double> h(3 * (size_t)b->nmol);
   for (int m = 0; m < b->nmol; ++m) {
-    if (!(eimp[m] >= 0.0) || !(tadd[m] >= 0.0)) {
-      set_error("qcx_batch_set_md_heating: eimp and tadd must be >= 0");
+    if (!(eimp[m] >= 0.0) || !(tadd[m] >= 0.0) || !(tadd[m] / tstep < 1.0e9)) {
+      set_error("qcx_batch_set_md_heating: eimp and tadd must be >= 0 and tadd below 1e9 steps");
       return -1;
     }
     // src/md.f90:265-266: nadd = (tadd + tstep) / tstep - 1 (truncated), fadd = tstep / (tadd + tstep)

@@ -91,6 +91,10 @@ int qcx_fragment_ips(int method, int ntraj, const int32_t* nat, const int32_t* n
     }
     int nf = 0;
     for (int a = 0; a < nat[t]; ++a) {
+      if (num[aoff + a] < 1 || num[aoff + a] > 18) {
+        qcx::set_last_error("qcx_fragment_ips: atomic number outside the parameterised range 1..18");
+        return -1;
+      }
       int f = frag[aoff + a];
       if (f < 1 || f > QCX_MAX_FRAGMENTS) {
         qcx::set_last_error("qcx_fragment_ips: fragment numbers must lie in 1..QCX_MAX_FRAGMENTS");

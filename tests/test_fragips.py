@@ -90,7 +90,8 @@ def test_fragment_ips_host_checks_without_gpu():
            ({"Z": Zw, "xyz": xw, "frag": [0, 1, 1]}, 1),  # not 1-based
            ({"Z": Zw, "xyz": xw, "frag": [1, 1, 11]}, 1),  # beyond QCX_MAX_FRAGMENTS
            ({"Z": Zw, "xyz": xw, "frag": [1, 1, 2]}, 0),  # no charge
-           ({"Z": Zw, "xyz": xw, "frag": [1, 1, 2]}, 5)]  # beyond QCX_FRAGIP_MAX_CHARGE
+           ({"Z": Zw, "xyz": xw, "frag": [1, 1, 2]}, 5),  # beyond QCX_FRAGIP_MAX_CHARGE
+           ({"Z": [8, 1, 19], "xyz": xw, "frag": [1, 1, 2]}, 1)]  # element outside 1..18
     for s, mchrg in bad:
         with pytest.raises(RuntimeError):
             qg.fragment_ips([s], mchrg)
