@@ -41,3 +41,15 @@ def test_host_side_validation_without_gpu():
     h = lib.qcx_batch_create(1, qcxms_gb300._ip(nat), qcxms_gb300._ip(Z), qcxms_gb300._dp(ch), qcxms_gb300._dp(et))
     assert not h
     assert b"1..18" in lib.qcx_last_error()
+
+
+def test_batch_entry_points_reject_null_handles_without_gpu():
+    """The loop-rule and state entry points check their handle before any CUDA call."""
+    lib = qcxms_gb300.load_library()
+    assert lib.qcx_batch_set_md_rules(None, 2, 250, 100) == -1
+    assert lib.qcx_batch_get_md_state(None, None, None, None, None, None, None, None, None) == -1
+    assert lib.qcx_batch_get_md_avg_xyz(None, None) == -1
+    assert lib.qcx_batch_set_md_heating(None, None, None, None, 20.0) == -1
+    assert lib.qcx_batch_set_cid_rules(None, 300.0, 100) == -1
+    assert lib.qcx_batch_get_cid_state(None, *([None] * 9)) == -1
+    assert lib.qcx_boltz(2, 0, 1, 300.0, None, None) == -1
