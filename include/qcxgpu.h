@@ -280,6 +280,11 @@ int qcx_batch_get_cid_state(qcx_batch* b, int32_t* nstep, int32_t* nfrag, int32_
 int qcx_read_xyz(const char* path, int max_nat, int32_t* nat, int32_t* num, double* xyz);
 int qcx_read_start(const char* path, int nat, int32_t* itrj, double* eimp, double* tadd, double* vel,
                    double* velof);
+/* Writes qcxms.start in wrstart's layout (src/utility.f90:321-373): itrj as
+ * (i4), eimp and tadd as (D22.14), per atom vx vy vz velof as D22.14 fields
+ * (14 significant digits, as the Fortran edit descriptor prints them). */
+int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tadd, const double* vel,
+                    const double* velof);
 
 /*
  * Allocation-free variant of qcx_egrad for callers that cannot call

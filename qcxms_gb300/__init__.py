@@ -100,6 +100,7 @@ def load_library(build_if_missing=True):
     lib.qcx_read_xyz.argtypes = [ctypes.c_char_p, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double)]
     lib.qcx_read_start.argtypes = [ctypes.c_char_p, c_int, P(ctypes.c_int32), P(c_double), P(c_double),
                                    P(c_double), P(c_double)]
+    lib.qcx_write_start.argtypes = [ctypes.c_char_p, c_int, c_int, c_double, c_double, P(c_double), P(c_double)]
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
     _lib = lib
     return lib

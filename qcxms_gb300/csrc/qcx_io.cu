@@ -95,9 +95,51 @@ int symbol_to_z(const std::string& tok) {
   return -1;
 }
 
+// Fortran Dw.d edit descriptor (w = 22, d = 14): 0.<14 digits>D<sign><2 digits>,
+// right-justified; the mantissa digits are the value rounded to 14 significant
+// digits (the round-to-nearest of printf's %.13E).
+std::string fortran_d22_14(double x) {
+  char buf[64];
+  std::string out;
+  if (x == 0.0) {
+    out = "0.00000000000000D+00";
+  } else {
+    std::snprintf(buf, sizeof(buf), "%.13E", std::fabs(x));
+    std::string m(buf);
+    const size_t e = m.find('E');
+    const int ex = std::atoi(m.c_str() + e + 1) + 1;
+    std::string digits = m.substr(0, 1) + m.substr(2, e - 2);
+    char tail[16];
+    std::snprintf(tail, sizeof(tail), "D%c%02d", ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
+    out = std::string(x < 0 ? "-" : "") + "0." + digits + tail;
+  }
+  if (out.size() < 22) out = std::string(22 - out.size(), ' ') + out;
+  return out;
+}
+
 }  // namespace
 
 extern "C" {
+
+int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tadd, const double* vel,
+                    const double* velof) {
+  if (!path || nat < 1 || !vel || !velof || itrj < 0 || itrj > 9999) {
+    qcx::set_last_error("qcx_write_start: invalid arguments (0 <= itrj <= 9999, nat >= 1, vel and velof)");
+    return -1;
+  }
+  FILE* f = std::fopen(path, "w");
+  if (!f) {
+    qcx::set_last_error(std::string("qcx_write_start: cannot write ") + path);
+    return -1;
+  }
+  std::fprintf(f, "%4d\n%s\n%s\n", itrj, fortran_d22_14(eimp).c_str(), fortran_d22_14(tadd).c_str());
+  for (int a = 0; a < nat; ++a)
+    std::fprintf(f, "%s%s%s%s\n", fortran_d22_14(vel[3 * a]).c_str(), fortran_d22_14(vel[3 * a + 1]).c_str(),
+                 fortran_d22_14(vel[3 * a + 2]).c_str(), fortran_d22_14(velof[a]).c_str());
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) qcx::set_last_error(std::string("qcx_write_start: write error on ") + path);
+  return ok ? 0 : -1;
+}
 
 int qcx_read_xyz(const char* path, int max_nat, int32_t* nat, int32_t* num, double* xyz) {
   std::vector<std::string> lines;

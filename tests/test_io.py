@@ -40,6 +40,29 @@ def test_read_ensemble_matches_files():
         assert np.array_equal(m["mass"], [constants.MASS_AU[z] for z in m["Z"]])
 
 
+def test_write_start_reproduces_the_fixture(tmp_path):
+    """qcx_write_start (C) and the fixture generator (Python) restate wrstart's
+    D22.14 output independently: byte-identical files."""
+    lib = qg.load_library()
+    for m in qg.read_ensemble(GOLDEN):
+        out = tmp_path / ("start.%d" % m["itrj"])
+        vel = np.ascontiguousarray(m["vel"])
+        velof = np.ascontiguousarray(m["velof"])
+        assert lib.qcx_write_start(str(out).encode(), m["itrj"], len(m["Z"]), m["eimp"], m["tadd"], qg._dp(vel),
+                                   qg._dp(velof)) == 0
+        ref = open(os.path.join(GOLDEN, "TMP.%d" % m["itrj"], "qcxms.start")).read()
+        assert out.read_text() == ref
+    # zero, negative and large exponents
+    out = tmp_path / "edge"
+    vel = np.array([[0.0, -1.5e-12, 123456.789]])
+    assert lib.qcx_write_start(str(out).encode(), 7, 1, 1.0, 0.99999999999999999, qg._dp(vel),
+                               qg._dp(np.array([2.5]))) == 0
+    lines = out.read_text().splitlines()
+    assert lines[0] == "   7" and lines[1] == "  0.10000000000000D+01" and lines[2] == "  0.10000000000000D+01"
+    assert lines[3] == ("  0.00000000000000D+00 -0.15000000000000D-11  0.12345678900000D+06"
+                        "  0.25000000000000D+01")
+
+
 def test_readers_reject_bad_input(tmp_path):
     lib = qg.load_library()
     nat = np.zeros(1, dtype=np.int32)
