@@ -53,3 +53,22 @@ def test_batch_entry_points_reject_null_handles_without_gpu():
     assert lib.qcx_batch_set_cid_rules(None, 300.0, 100) == -1
     assert lib.qcx_batch_get_cid_state(None, *([None] * 9)) == -1
     assert lib.qcx_boltz(2, 0, 1, 300.0, None, None) == -1
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/qcxgpu.h compiles as C99 and a C program links against the
+    library and calls its host-side entry points (no GPU work)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        import pytest
+        pytest.skip("no gcc")
+    path = build.build()
+    exe = tmp_path / "abi_from_c"
+    src = os.path.join(ROOT, "tests", "c", "abi_from_c.c")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src, "-o", str(exe),
+                    path, "-lm", "-Wl,-rpath," + os.path.dirname(path)], check=True)
+    out = subprocess.run([str(exe), os.path.join(ROOT, "tests", "golden", "TMPQCXMS")], capture_output=True,
+                         text=True)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.startswith("ok nat=5 itrj=1")
