@@ -234,6 +234,17 @@ int qcx_fragment_ips(int method, int ntraj, const int32_t* nat, const int32_t* n
                      int32_t* ipok);
 
 /*
+ * Fragment masses and sum formulas, fragmass (src/fragments.f90:10-84), on
+ * the host: frag[nat] holds fragment numbers 1..QCX_MAX_FRAGMENTS, mass[nat]
+ * atomic masses in atomic units. Fragments with atoms are numbered in order
+ * (*nfrag of them); fragm_amu[k] is fragment k's mass in amu and formula +
+ * 80 k its formula with the elements in order of atomic number, each with its
+ * count ("H4C2", "H2O1"). fragm_amu or formula may be NULL.
+ */
+int qcx_fragment_formula(int nat, const int32_t* num, const int32_t* frag, const double* mass, int32_t* nfrag,
+                         double* fragm_amu, char* formula);
+
+/*
  * Boltzmann weights of fragment IPs, boltz (src/utility.f90:469-498):
  * fragchrg2(i,j) = exp(-ip(i,j)/f) / sum exp(-ip/f), f = temp * kB * (627.50947428
  * for units 1, kcal/mol; 27.21138505 for units 2, eV). ip and fragchrg2 are

@@ -25,7 +25,7 @@ import numpy as np
 
 from . import constants
 
-__all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "fragment_ips", "boltz", "read_ensemble", "load_library",
+__all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "fragment_ips", "fragment_formula", "boltz", "read_ensemble", "load_library",
            "library_path",
            "STATUS_SCC_NOT_CONVERGED", "STATUS_NON_FINITE", "STATUS_CHOLESKY_FAILED", "STATUS_EIGEN_NOT_CONVERGED"]
 
@@ -101,6 +101,8 @@ def load_library(build_if_missing=True):
     lib.qcx_read_start.argtypes = [ctypes.c_char_p, c_int, P(ctypes.c_int32), P(c_double), P(c_double),
                                    P(c_double), P(c_double)]
     lib.qcx_write_start.argtypes = [ctypes.c_char_p, c_int, c_int, c_double, c_double, P(c_double), P(c_double)]
+    lib.qcx_fragment_formula.argtypes = [c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double),
+                                         P(ctypes.c_int32), P(c_double), ctypes.c_char_p]
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
     _lib = lib
     return lib
@@ -203,6 +205,21 @@ def fragment_ips(structs, mchrg=1, etemp=300.0, precision=0, method=gfn2_xtb):
         raise RuntimeError("qcx_fragment_ips returned %d: %s" % (rc, _err(lib)))
     nf = [int(np.max(s["frag"])) for s in structs]
     return [ip[t, :nf[t]] for t in range(len(structs))], [ef[t, :nf[t]] for t in range(len(structs))], ok.astype(bool)
+
+
+def fragment_formula(Z, frag, mass):
+    """Fragment masses (amu) and sum formulas as fragmass (src/fragments.f90:10-84)."""
+    lib = load_library()
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    frag = np.ascontiguousarray(frag, dtype=np.int32)
+    mass = np.ascontiguousarray(mass, dtype=np.float64)
+    n = np.zeros(1, dtype=np.int32)
+    fm = np.zeros(MAX_FRAGMENTS)
+    buf = ctypes.create_string_buffer(80 * MAX_FRAGMENTS)
+    if lib.qcx_fragment_formula(len(Z), _ip(Z), _ip(frag), _dp(mass), _ip(n), _dp(fm), buf) != 0:
+        raise RuntimeError(_err(lib))
+    k = int(n[0])
+    return fm[:k], [buf.raw[80 * i:80 * (i + 1)].split(b"\0")[0].decode() for i in range(k)]
 
 
 def boltz(units, temp, ip):

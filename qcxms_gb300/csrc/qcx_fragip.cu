@@ -11,6 +11,7 @@
 // is one molecule of a single batch, so all of them run in one pass of the
 // batched kernels. boltz (src/utility.f90:469-498) turns IPs into weights.
 #include <cmath>
+#include <cstdio>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -180,6 +181,44 @@ int qcx_fragment_ips(int method, int ntraj, const int32_t* nat, const int32_t* n
       for (int k = 0; k < QCX_MAX_FRAGMENTS * (nch + 1); ++k) out[k] = e[k];
     }
   }
+  return 0;
+}
+
+int qcx_fragment_formula(int nat, const int32_t* num, const int32_t* frag, const double* mass, int32_t* nfrag,
+                         double* fragm_amu, char* formula) {
+  if (nat < 1 || !num || !frag || !mass || !nfrag) {
+    qcx::set_last_error("qcx_fragment_formula: invalid arguments");
+    return -1;
+  }
+  static const char* const sym[] = {"",  "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",
+                                    "Ne", "Na", "Mg", "Al", "Si", "P",  "S",  "Cl", "Ar"};
+  // src/xtb_mctc_convert.f90:47-52: autoamu = (1/amutokg) * metokg
+  constexpr double kgtoamu = 1.0 / 1.660539040e-27;
+  constexpr double autoamu = kgtoamu * 9.10938356e-31;
+  double fm[QCX_MAX_FRAGMENTS] = {0.0};
+  int el[QCX_MAX_FRAGMENTS][19] = {{0}};
+  for (int i = 0; i < nat; ++i) {
+    if (frag[i] < 1 || frag[i] > QCX_MAX_FRAGMENTS || num[i] < 1 || num[i] > 18) {
+      qcx::set_last_error("qcx_fragment_formula: fragment numbers 1..QCX_MAX_FRAGMENTS, elements 1..18");
+      return -1;
+    }
+    fm[frag[i] - 1] += mass[i];
+    el[frag[i] - 1][num[i]] += 1;
+  }
+  int n = 0;
+  for (int f = 0; f < QCX_MAX_FRAGMENTS; ++f) {
+    if (!(fm[f] > 0.0)) continue;
+    // elements in order of atomic number, each with its count
+    std::string s;
+    for (int z = 1; z <= 18; ++z)
+      if (el[f][z]) s += std::string(sym[z]) + std::to_string(el[f][z]);
+    if (fragm_amu) fragm_amu[n] = fm[f] * autoamu;
+    if (formula) {
+      std::snprintf(formula + 80 * n, 80, "%s", s.c_str());
+    }
+    ++n;
+  }
+  *nfrag = n;
   return 0;
 }
 

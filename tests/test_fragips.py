@@ -140,3 +140,23 @@ def test_gpu_fragment_ips_mixed_precision(gpu, oracle_lib):
     structs = [fragmented(100 + s, 2 + s % 3) for s in range(8)]
     ip, ef, ok = qg.fragment_ips(structs, 1, precision=1)
     _compare(ip, ef, ok, structs, oracle_lib, 1, 1e-6)
+
+
+def test_fragment_formula_known_answers():
+    """fragmass (src/fragments.f90:10-84): masses in amu and formulas with the
+    elements in order of atomic number, every count written."""
+    from qcxms_gb300 import constants
+    amu = [0.0, 1.00794075, 4.00260193, 6.94003660, 9.01218307, 10.81102805, 12.01073590, 14.00670321, 15.99940492]
+    Z = [6, 6, 8, 1, 1, 1, 1, 1, 1]
+    frag = [1, 1, 2, 1, 1, 1, 1, 2, 2]
+    fm, formula = qg.fragment_formula(Z, frag, [constants.MASS_AU[z] for z in Z])
+    assert formula == ["H4C2", "H2O1"]
+    assert abs(fm[0] - (2 * amu[6] + 4 * amu[1])) < 1e-9 and abs(fm[1] - (amu[8] + 2 * amu[1])) < 1e-9
+    # fragment numbers without atoms are skipped, the rest numbered in order
+    fm, formula = qg.fragment_formula([7, 1, 16], [3, 3, 5], [constants.MASS_AU[z] for z in (7, 1, 16)])
+    assert formula == ["H1N1", "S1"] and len(fm) == 2
+    # twelve H atoms: two-digit count
+    fm, formula = qg.fragment_formula([1] * 12, [1] * 12, [constants.MASS_AU[1]] * 12)
+    assert formula == ["H12"]
+    with pytest.raises(RuntimeError):
+        qg.fragment_formula([1, 1], [1, 11], [1.0, 1.0])
