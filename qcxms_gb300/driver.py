@@ -25,7 +25,7 @@ import json
 
 import numpy as np
 
-from . import Batch, constants, fragment_ips, read_ensemble
+from . import Batch, constants, fragment_formula, fragment_ips, read_ensemble
 
 
 def run_ensemble(root, etemp, charge=1, nfragexit=2, more=250, max_steps=10000, tstep_fs=0.5, block=100,
@@ -57,6 +57,10 @@ def run_ensemble(root, etemp, charge=1, nfragexit=2, more=250, max_steps=10000, 
                "nstep": int(st["nstep"][i]), "nfrag": int(nfrag[i]), "frag": frag[sl].tolist(),
                "fragT": st["fragT"][i, :max(1, min(int(nfrag[i]), 10))].tolist(), "energy": float(r["energy"][i]),
                "status": int(r["status"][i])}
+        if nfrag[i] <= 10:
+            # fragment masses and formulas (fragmass, src/fragments.f90:10-84)
+            fm, formula = fragment_formula(m["Z"], frag[sl], m["mass"])
+            res["fragm_amu"], res["formula"] = fm.tolist(), formula
         out.append(res)
         if 2 <= nfrag[i] <= 10:
             # analyse gets the averaged structure (src/md.f90:695, write_fragments.f90:102-106)
@@ -82,8 +86,8 @@ def main():
     a = ap.parse_args()
     res = run_ensemble(a.root, a.etemp, a.charge, a.nfragexit, max_steps=a.max_steps, precision=a.precision)
     for t in res:
-        print("traj %5d  mdok %d  fragstate %d  steps %6d  fragments %d  IPs %s" %
-              (t["itrj"], t["mdok"], t["fragstate"], t["nstep"], t["nfrag"],
+        print("traj %5d  mdok %d  fragstate %d  steps %6d  fragments %d  %s  IPs %s" %
+              (t["itrj"], t["mdok"], t["fragstate"], t["nstep"], t["nfrag"], " ".join(t.get("formula", [])),
                " ".join("%.2f" % x for x in t.get("fragip_eV", []))))
     if a.out:
         with open(a.out, "w") as f:
