@@ -31,8 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "GFN2-xTB trajectory-steps/s"
 # DRAM bytes of one k_scc launch per molecule, from an ncu capture of a launch over 8
-# molecules (5.37 MB; profiles/k_scc_mixed_64traj_group_full.md); a launch touches each
-# molecule's own data only.
+# molecules (5.37 MB); a launch touches each molecule's own data only.
 SCC_DRAM_BYTES_PER_MOLECULE = 5.37e6 / 8
 NTRAJ, NMIN, NMAX = 256, 5, 40
 DT_FS = 0.5
@@ -157,26 +156,58 @@ def measured_peak(torch, dtype):
     return best
 
 
-def cpu_sample(mols, seconds, nthreads):
-    """Time the oracle restatement on a bounded sample of the workload."""
+def stratified(mols, k):
+    """k molecules spread evenly over the size order of mols (largest first)."""
+    order = sorted(range(len(mols)), key=lambda i: -len(mols[i]["Z"]))
+    if k >= len(mols):
+        return [mols[i] for i in order]
+    pick = np.linspace(0, len(mols) - 1, k).round().astype(int)
+    return [mols[order[i]] for i in pick]
+
+
+def cpu_sample(mols, seconds, nthreads, chunk=10):
+    """Time the oracle restatement on a bounded sample of the workload: calls of
+    `chunk` MD steps each (trajectories largest first under a dynamic schedule,
+    all threads busy at once), until `seconds` have passed. A trajectory whose
+    calculation fails stops, as on the GPU. The rate is the accepted steps over
+    the threads' busy time divided by the thread count: the idle tail of a
+    call, when fewer trajectories than threads are left, is not counted,
+    because a full ensemble run (bin/pqcxms: one process per trajectory, as many
+    at once as cores) keeps every core busy with the next trajectory. Returns
+    (trajectory-steps/s, calls, seconds, accepted steps, wall-clock rate)."""
     import oracle
     from qcxms_gb300 import constants
     kT = ETEMP * constants.KB_AU
     dt = DT_FS * constants.FSTOAU
+    mols = [dict(m) for m in mols]
     # initial gradients (setup, untimed)
-    grads = [oracle.egrad(m["Z"], m["xyz"], m["charge"], kT=kT)[2] for m in mols]
-    done, steps, t0 = 0, 0, time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
-        fails, xyz, vel, g, ep, it = oracle.md_batch(mols, 1, dt, grads, kT, nthreads=nthreads)
+    rc, _, grads, _ = oracle.egrad_batch(mols, kT, nthreads=nthreads)
+    active = (rc == 0).astype(np.int32)
+    steps_done = np.zeros(len(mols), dtype=np.int32)
+    busy = np.zeros(len(mols))
+    done, calls, busy_sum, t0 = 0, 0, 0.0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds and active.any():
+        fails, xyz, vel, g, ep, it = oracle.md_batch(mols, chunk, dt, grads, kT, nthreads=nthreads, active=active,
+                                                     steps_done=steps_done, busy_s=busy)
+        busy_sum += float(busy.sum())
         off = 0
         for i, m in enumerate(mols):
             n = len(m["Z"])
             m["xyz"], m["vel"], grads[i] = xyz[off:off + n], vel[off:off + n], g[off:off + n]
             off += n
-        done += len(mols) - fails
-        steps += 1
+        done += int(steps_done.sum())
+        calls += 1
     el = time.perf_counter() - t0
-    return done / el, steps, el
+    return done / (busy_sum / nthreads), calls, el, done, done / el
+
+
+def cpu_sample_desc(sample, ntraj, calls, chunk, el, done, wall_rate):
+    nat = [len(m["Z"]) for m in sample]
+    return ("%d of the %d trajectories, stratified by size (%d-%d atoms, mean %.1f), %d calls of %d MD steps "
+            "(%d accepted trajectory-steps, %.1f s); CPU FP64 restatement of leapfrog + energy/gradient + checkqc, "
+            "OpenMP over trajectories, largest first, failed trajectories stop; rate over the threads' busy time "
+            "(wall-clock rate with the idle tails of the calls: %.1f)"
+            % (len(sample), ntraj, min(nat), max(nat), float(np.mean(nat)), calls, chunk, done, el, wall_rate))
 
 
 def plain_fp64_single(qg, constants, nsteps=6):
@@ -211,13 +242,13 @@ def run_reference(args):
         return
     mols = workload(0)
     ncpu = os.cpu_count() or 1
-    sample = mols[: min(len(mols), 4 * ncpu)]
-    for _ in range(args.warmup):
-        pass
+    sample = stratified(mols, 2 * ncpu)
     vals = []
+    desc = ""
     for _ in range(max(1, args.steps)):
-        v, nsteps, el = cpu_sample([dict(m) for m in sample], max(2.0, 20.0 / max(1, args.steps)), ncpu)
+        v, calls, el, done, wall = cpu_sample(sample, max(4.0, 20.0 / max(1, args.steps)), ncpu)
         vals.append(v)
+        desc = cpu_sample_desc(sample, NTRAJ, calls, 10, el, done, wall)
     v = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "trajectory-steps/s", "n_gpus": args.gpus,
@@ -225,12 +256,48 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD_NAMES["batch"], "ntraj_per_gpu": NTRAJ, "atoms": [NMIN, NMAX],
                    "etemp_K": ETEMP, "precision": "fp64 (CPU restatement)"},
-        "cpu_baseline": {"value": v, "unit": "trajectory-steps/s", "cores": ncpu, "kind": "port",
-                         "sample": "%d of the %d trajectories, leapfrog + CPU FP64 restatement of the energy/gradient, "
-                                   "OpenMP over trajectories, ~20 s" % (len(sample), NTRAJ)},
+        "cpu_baseline": {"value": v, "unit": "trajectory-steps/s", "cores": ncpu, "kind": "port", "sample": desc},
         "e2e": {"value": v, "unit": "trajectory-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def accuracy_check(b, mols, k=32):
+    """Energies and gradients of the batch's last evaluation against FP64 on a
+    stratified sample of k running trajectories at their current geometries:
+    the CPU FP64 oracle and the GPU FP64 path."""
+    import oracle
+    import qcxms_gb300 as qg
+    from qcxms_gb300 import constants
+    r = b.get()
+    act, _ = b.progress()
+    xyz = b.split(r["xyz"])
+    grad = b.split(r["grad"])
+    cand = [i for i in range(b.nmol) if act[i] and r["status"][i] == 0]
+    cand.sort(key=lambda i: -len(mols[i]["Z"]))
+    pick = [cand[j] for j in np.linspace(0, len(cand) - 1, min(k, len(cand))).round().astype(int)]
+    sub = [{"Z": mols[i]["Z"], "xyz": xyz[i], "charge": mols[i]["charge"]} for i in pick]
+    rc, e_o, g_o, _ = oracle.egrad_batch(sub, ETEMP * constants.KB_AU, nthreads=os.cpu_count() or 1)
+    b64 = qg.Batch(sub, etemp=ETEMP)
+    b64.set_precision("fp64")
+    b64.egrad()
+    r64 = b64.get()
+    g64 = b64.split(r64["grad"])
+    b64.close()
+    ok = [j for j in range(len(pick)) if rc[j] == 0 and r64["status"][j] == 0]
+    dE = np.array([abs(r["energy"][pick[j]] - e_o[j]) for j in ok])
+    dg = np.array([np.abs(grad[pick[j]] - g_o[j]).max() for j in ok])
+    dE64 = np.array([abs(r["energy"][pick[j]] - r64["energy"][j]) for j in ok])
+    dg64 = np.array([np.abs(grad[pick[j]] - g64[j]).max() for j in ok])
+    nat = [len(s["Z"]) for s in sub]
+    return {"sample": "%d running trajectories at their current geometries, stratified by size (%d-%d atoms)"
+                      % (len(ok), min(nat), max(nat)),
+            "vs_fp64_oracle": {"max_abs_dE_Eh": float(dE.max()), "max_abs_dg_Eh_per_bohr": float(dg.max()),
+                               "frac_dE_within_1e-6": float(np.mean(dE <= 1e-6)),
+                               "frac_dg_within_1e-5": float(np.mean(dg <= 1e-5))},
+            "vs_gpu_fp64": {"max_abs_dE_Eh": float(dE64.max()), "max_abs_dg_Eh_per_bohr": float(dg64.max())},
+            "note": "both sides at the default SCC thresholds (1e-7 Eh, 1e-6); differences include where "
+                    "two converged SCC runs stop"}
 
 
 def run_gpu(args):
@@ -267,15 +334,22 @@ def run_gpu(args):
             torch.cuda.synchronize()
 
     # ---- device-resident timing: graph replay, L2 flushed between steps ----
+    # Timing marks inside the step graph give the SCC phase of every timed step:
+    # from the first group's SCC start to the last group's SCC end.
+    b.set_timing(True)
     for _ in range(args.warmup):
         b.step(1, dt)
     barrier()
     _, steps0 = b.progress()
     total_ms = 0.0
     launches = 0
+    scc_flops_sum = scc_ms_sum = 0.0
+    scc_iters_all = []
+    phase = {"step": [], "scc_span": [], "scc_sum": [], "integrals_sum": [], "gradient_sum": []}
     with ClockSampler(local) as clk:
         barrier()
         for _ in range(args.steps):
+            act_before, _ = b.progress()
             l2_flush.zero_()
             torch.cuda.synchronize()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -285,23 +359,42 @@ def run_gpu(args):
             e.synchronize()
             total_ms += s.elapsed_time(e)
             launches += b.kernel_launches()
+            tm = b.timing()
+            _, it = b.status_iters()
+            ran = act_before > 0
+            scc_flops_sum += scc_flops(nao[ran], it[ran].astype(np.float64))
+            scc_ms_sum += tm["scc_span"]
+            scc_iters_all.append(it[ran])
+            mk = tm["marks"]
+            phase["step"].append(tm["step"])
+            phase["scc_span"].append(tm["scc_span"])
+            phase["scc_sum"].append(tm["scc_sum"])
+            phase["integrals_sum"].append(float(np.sum(mk[:, 1] - mk[:, 0])))
+            phase["gradient_sum"].append(float(np.sum(mk[:, 3] - mk[:, 2])))
         barrier()
-    _, steps1 = b.progress()
+    act_end, steps1 = b.progress()
     done = float(np.sum(steps1 - steps0))
     total_ms, done_all = reduce_over_ranks(total_ms, done, world, "cuda")
     value = done_all / (total_ms * 1e-3)
+    iters_cat = np.concatenate(scc_iters_all) if scc_iters_all else np.zeros(1)
 
     # ---- end to end through the public API with pinned host buffers ----
+    # every step: coordinates and velocities in (qcx_batch_load_state: running
+    # trajectories continue, stopped ones stay stopped), one step, coordinates,
+    # velocities and energies out
+    b.set_timing(False)
     r = b.get()
     hx = torch.from_numpy(r["xyz"]).pin_memory()
     hv = torch.from_numpy(r["vel"]).pin_memory()
     he = torch.zeros(b.nmol, dtype=torch.float64).pin_memory()
     e2e_steps = max(3, min(args.steps, 10))
+    b.step(1, dt)  # capture the graph without timing marks outside the timed region
+    b.sync()
     _, s0 = b.progress()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        b.set_state_ptr(hx.data_ptr(), hv.data_ptr())
+        b.load_state_ptr(hx.data_ptr(), hv.data_ptr())
         b.step(1, dt)
         b.get_ptr(hx.data_ptr(), hv.data_ptr(), he.data_ptr())
     barrier()
@@ -313,53 +406,59 @@ def run_gpu(args):
     h2d = 2 * 3 * 8 * b.natom
     d2h = 2 * 3 * 8 * b.natom + 8 * b.nmol
 
-    # ---- roofline of the dominant kernel (SCC), timed live on the batch stream ----
-    prof = [b.profile_egrad() for _ in range(3)]
-    scc_ms = statistics.median(p["scc"] for p in prof)
-    iters = b.get()["iters"].astype(np.float64)
-    it64 = np.array([b.energy_terms(i)["iters_fp64"] for i in range(b.nmol)])
-    act, _ = b.progress()
-    flops = scc_flops(nao[act > 0], iters[act > 0])
-    achieved = flops / (scc_ms * 1e-3) / 1e12
+    # ---- roofline of the dominant kernel (SCC) over the timed steps ----
+    achieved = scc_flops_sum / (scc_ms_sum * 1e-3) / 1e12
     # The mixed kernel runs its O(n^3) work on the FP32 pipes (FP32 iterations and
     # the double-float finishing iterations); the FP64 kernel on the FP64 pipe.
     mixed = args.precision == "mixed"
     peak = measured_peak(torch, torch.float32 if mixed else torch.float64)
     plain = plain_fp64_single(qg, constants) if rank == 0 and not args.no_plain else None
+    accuracy = accuracy_check(b, mols) if rank == 0 and mixed and not args.no_accuracy else None
 
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
             ncpu = os.cpu_count() or 1
-            sample = [dict(m) for m in workload(0)[: 2 * ncpu]]
-            v, nst, el = cpu_sample(sample, 12.0, ncpu)
+            sample = stratified(workload(0), 2 * ncpu)
+            v, calls, el, cdone, wall = cpu_sample(sample, 12.0, ncpu)
             cpu = {"value": v, "unit": "trajectory-steps/s", "cores": ncpu, "kind": "port",
-                   "sample": "%d of the %d trajectories x %d steps (%.1f s), CPU FP64 restatement, OpenMP over "
-                             "trajectories" % (len(sample), NTRAJ, nst, el)}
-        breakdown = {k: round(statistics.median(p[k] for p in prof), 4) for k in prof[0]}
+                   "sample": cpu_sample_desc(sample, NTRAJ, calls, 10, el, cdone, wall)}
+        med = {k: round(statistics.median(v), 3) for k, v in phase.items()}
         line = {
             "metric": METRIC, "value": value, "unit": "trajectory-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+df64" if mixed else "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD_NAMES[args.workload], "ntraj_per_gpu": b.nmol,
                        "atoms": [NMIN, NMAX] if args.workload == "batch" else [10, 81],
                        "etemp_K": ETEMP, "precision": args.precision, "scc_guess": args.guess,
+                       "arithmetic": ("FP32 SCC iterations, then double-float (hi+lo FP32) finishing iterations; "
+                                      "FP64 integrals, potentials of the finishing iterations, Fermi level, Broyden, "
+                                      "energies and gradient") if mixed else "FP64 throughout",
                        "md_rules_on_device": bool(args.md_rules),
-                       "execution": "one CUDA graph per MD step, 8 molecule groups on separate streams", "l2": "flushed between timed steps (256 MiB write)",
-                       "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters)),
-                       "mean_scc_iters_fp64": float(np.mean(it64)),
-                       "active_trajectories": int(np.sum(act))},
+                       "execution": "one CUDA graph per MD step, 8 molecule groups on separate streams",
+                       "l2": "flushed between timed steps (256 MiB write)",
+                       "mean_nao": float(np.mean(nao)), "mean_scc_iters": float(np.mean(iters_cat)),
+                       "active_trajectories_end": int(np.sum(act_end)),
+                       "stopped_trajectories": int(b.nmol - np.sum(act_end))},
             "e2e": {"value": e2e, "unit": "trajectory-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": SCC_DRAM_BYTES_PER_MOLECULE * b.nmol, "kernel": "k_scc",
-                         "peak_source": "measured in this run: cuBLAS %s GEMM 4096^3 on CUDA cores (MEASURED_PEAKS.json "
-                                        "holds only HBM and bf16 tensor peaks)" % ("FP32" if mixed else "FP64"),
+                         "frac": achieved / peak,
+                         "traffic": SCC_DRAM_BYTES_PER_MOLECULE * float(np.mean([len(x) for x in scc_iters_all])),
+                         "kernel": "k_scc",
+                         "launch_unit": "the SCC phase of one timed step: one k_scc launch per molecule group (8, "
+                                        "concurrent); time = first group's SCC start to last group's SCC end, from "
+                                        "event marks inside the step graph; FLOPs over the molecules that ran",
+                         "peak_source": "measured in this run: cuBLAS %s GEMM 4096^3 on CUDA cores "
+                                        "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)"
+                                        % ("FP32" if mixed else "FP64"),
                          "flops_convention": "algorithmic, per molecule: iters*(9n^3+2n^3)+2n^3"},
-            "kernel_ms": breakdown,
+            "kernel_ms": med,
             "clocks": clk.summary(),
         }
+        if accuracy:
+            line["accuracy"] = accuracy
         if cpu:
             line["cpu_baseline"] = cpu
         if plain:
@@ -438,6 +537,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="batch", choices=["batch", "cid", "fragip"])
     ap.add_argument("--no-plain", action="store_true", help="skip the single-trajectory FP64 reference leg")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 accuracy check after the timed steps")
     ap.add_argument("--md-rules", action="store_true",
                     help="run the MD heating, bookkeeping and exit rules on the device in the timed steps "
                          "(the end-to-end leg sets new coordinates, which switches them off)")

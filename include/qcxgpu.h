@@ -29,6 +29,10 @@ extern "C" {
 #define QCX_STATUS_NON_FINITE 2
 #define QCX_STATUS_CHOLESKY_FAILED 4
 #define QCX_STATUS_EIGEN_NOT_CONVERGED 8
+/* checkqc (src/iniqm.f90:684-715) rejected the result: |E| < 1e-8, gnorm
+ * outside [1e-8, 20], or a cation with max(qat) below 1e-5 in magnitude; the
+ * last two set the energy to 0, as the reference does */
+#define QCX_STATUS_CHECKQC 16
 
 /* Library version (major*10000 + minor*100 + patch). */
 int qcx_version(void);
@@ -46,9 +50,25 @@ const char* qcx_last_error(void);
  * the calculation is spin-restricted with Fermi smearing at etemp.
  * The device state for a given atom list is cached between calls.
  * Writes energy (Eh), grad [nat][3] (Eh/Bohr) and qat [nat] (Mulliken charges).
+ * The result then goes through checkqc as egrad does after the call
+ * (src/iniqm.f90:650, 684-715): a rejected result returns -1, with the energy
+ * set to 0 where checkqc sets it (a Fortran egrad that calls checkqc itself
+ * sees the same outcome).
  */
 int qcx_egrad(int method, int nat, const int32_t* num, const double* xyz, int charge, int multiplicity,
               double etemp, double* energy, double* grad, double* qat);
+
+/*
+ * checkqc (src/iniqm.f90:684-715) on the GPU for one result held by the
+ * caller: the device function that qcx_egrad and every batch evaluation apply
+ * (gnorm sums grad(1,i)**2 + grad(2,i)**2 + grad(2,i)**2 as the reference
+ * does, src/iniqm.f90:719-732). grad [nat][3], qat [nat]; *energy is set to 0
+ * where the reference sets it. Returns 0 when the result is accepted, 1 for
+ * |E| < 1e-8, 2 for a gradient norm outside [1e-8, 20], 3 for a cation
+ * (charge > 0) whose largest atomic charge is below 1e-5 in magnitude, -1 on
+ * invalid arguments or a CUDA error.
+ */
+int qcx_checkqc(int nat, const double* grad, const double* qat, int charge, double* energy);
 
 /*
  * Batched trajectories: nmol independent molecules advanced together on one
@@ -67,11 +87,16 @@ void qcx_batch_destroy(qcx_batch* b);
 /* SCC controls (defaults: 100, 1e-7 Eh, 1e-6, 0.25). max_iter <= 100. */
 int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, double mixing);
 
-/* Arithmetic of the SCC loop: 0 = FP64 throughout (default); 1 = mixed:
- * FP32 transforms, eigensolve and density until the moment residual drops
- * below 1e-4 (or stops improving below 1e-3), then FP64 iterations
- * warm-started from the FP32 eigenvectors to the same convergence thresholds. Integrals, potentials, Fermi level,
- * Broyden mixing, energies and the gradient are FP64 in both modes. */
+/* Arithmetic of the SCC loop: 0 = FP64 throughout (default); 1 = mixed.
+ * Mixed mode runs its first iterations in FP32: Fock build, potentials,
+ * transforms, eigensolve, Fermi level, density and moments, until the moment
+ * residual drops below 1e-4 (or stops improving below 1e-3). The remaining
+ * iterations (at least two) keep the coefficients and their O(n^3) products
+ * in double-float arithmetic (hi + lo FP32 pairs, about 48 significant bits)
+ * and their Fock build, potentials, Fermi level, energies and Broyden mixing
+ * in FP64, and meet the same convergence thresholds as mode 0. Integrals and
+ * the gradient are FP64 in both modes, except the three-body dispersion term,
+ * which is summed in FP32 per triple and accumulated in FP64. */
 #define QCX_PRECISION_FP64 0
 #define QCX_PRECISION_MIXED 1
 int qcx_batch_set_precision(qcx_batch* b, int precision);
@@ -90,6 +115,14 @@ int qcx_batch_set_guess(qcx_batch* b, int guess);
 /* Copy host state in. Any pointer may be NULL to keep the current value.
  * xyz, vel: [natom][3]; mass: [natom] (atomic units). */
 int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass);
+
+/* Copy coordinates and/or velocities ([natom][3], NULL keeps the current
+ * value) in without starting new runs: stopped trajectories stay stopped and
+ * the MD or collision rules stay on. For a host that reads the state after a
+ * step and writes it back (or changes it) before the next one. The copies are
+ * queued on the batch's stream; the host buffers must stay valid until the
+ * next call that synchronises (qcx_batch_get, qcx_batch_sync). */
+int qcx_batch_load_state(qcx_batch* b, const double* xyz, const double* vel);
 
 /* Energy and gradient at the current coordinates. */
 int qcx_batch_egrad(qcx_batch* b);
@@ -199,6 +232,17 @@ void* qcx_batch_stream(qcx_batch* b);
  * gradient reset, integral-derivative gradient, atom-pair gradient. */
 int qcx_batch_profile_egrad(qcx_batch* b, float* ms);
 
+/* Timing marks inside the captured step graph (on = 1; the next
+ * qcx_batch_step captures the graph again with them, on = 0 without). The
+ * step's kernels run in G molecule groups on parallel streams; after a step,
+ * qcx_batch_get_timing writes ms[0..1+4G] (n >= 2 + 4G floats): ms[0] = 0 at
+ * the start of the step, ms[1 + 4g + k] the time of mark k of group g (0
+ * integrals start, 1 SCC start, 2 SCC end, 3 gradient end) and ms[1 + 4G]
+ * the end of the step, all in ms from the start of the last replayed step.
+ * Returns G. */
+int qcx_batch_set_timing(qcx_batch* b, int on);
+int qcx_batch_get_timing(qcx_batch* b, float* ms, int n);
+
 /* Atomic-orbital and atom counts of every molecule (nao[nmol], nat[nmol]);
  * used to count algorithmic work. */
 int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat);
@@ -307,10 +351,12 @@ int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tad
  * GPU loading the library keeps until the process exits; nothing is
  * allocated on the device or the host heap. Limits: QCX_NOALLOC_MAX_ATOMS
  * atoms and QCX_NOALLOC_MAX_NAO atomic orbitals; larger inputs return -1
- * with the reason on stderr. The first call on a device looks up the array's
- * device address and uploads the parameters; make that first call before
- * any stream capture. Calls share the array: calls that overlap on the GPU
- * race (one process serialises its own calls on the host).
+ * with the reason on stderr and in qcx_last_error(). The first call on a
+ * device uploads the parameters into the array; make that first call before
+ * any stream capture. Every call looks up the array's device address and
+ * checks a marker word, so a call after cudaDeviceReset uploads them again.
+ * Calls share the array: calls that overlap on the GPU race (one process
+ * serialises its own calls on the host).
  */
 #define QCX_NOALLOC_MAX_ATOMS 64
 #define QCX_NOALLOC_MAX_NAO 160

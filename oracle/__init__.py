@@ -60,6 +60,7 @@ def lib():
         _lib.qcxo_checkqc.restype = ctypes.c_int
         _lib.qcxo_fragments.restype = ctypes.c_int
         _lib.qcxo_md_batch.restype = ctypes.c_int
+        _lib.qcxo_egrad_batch.restype = ctypes.c_int
         _lib.qcxo_eself.restype = ctypes.c_double
         _lib.qcxo_nel.restype = ctypes.c_int
     return _lib
@@ -490,8 +491,30 @@ def fragments(Z, xyz, rcut=3.0, at1=1, at2=0):
     return frag, nf
 
 
-def md_batch(mols, nsteps, tstep, grad0, kT, opts=None, nthreads=0):
-    """CPU MD over a list of molecules (dicts with Z, xyz, vel, mass, charge)."""
+def egrad_batch(mols, kT, opts=None, nthreads=0):
+    """Energies, gradients and charges of many structures (dicts with Z, xyz,
+    charge), OpenMP over structures. Returns (rc[n], energy[n], grads, qats)."""
+    off = np.zeros(len(mols) + 1, dtype=np.int32)
+    for i, m in enumerate(mols):
+        off[i + 1] = off[i] + len(m["Z"])
+    Z = np.ascontiguousarray(np.concatenate([m["Z"] for m in mols]), dtype=np.int32)
+    xyz = np.ascontiguousarray(np.concatenate([np.asarray(m["xyz"]).reshape(-1, 3) for m in mols]), dtype=np.float64)
+    charge = np.array([m["charge"] for m in mols], dtype=np.float64)
+    kTa = np.full(len(mols), kT, dtype=np.float64)
+    e = np.zeros(len(mols))
+    g = np.zeros((off[-1], 3))
+    q = np.zeros(off[-1])
+    rc = np.zeros(len(mols), dtype=np.int32)
+    o = opts if opts is not None else default_opts()
+    lib().qcxo_egrad_batch(len(mols), _p(off, ctypes.c_int), _p(Z, ctypes.c_int), _p(xyz), _p(charge), _p(kTa),
+                           ctypes.byref(o), int(nthreads), _p(e), _p(g), _p(q), _p(rc, ctypes.c_int))
+    return rc, e, [g[off[i]:off[i + 1]] for i in range(len(mols))], [q[off[i]:off[i + 1]] for i in range(len(mols))]
+
+
+def md_batch(mols, nsteps, tstep, grad0, kT, opts=None, nthreads=0, active=None, steps_done=None, busy_s=None):
+    """CPU MD over a list of molecules (dicts with Z, xyz, vel, mass, charge).
+    With ``active`` (int32 array, updated in place) failed trajectories stop;
+    ``steps_done`` (int32 array) receives the accepted steps per trajectory."""
     off = np.zeros(len(mols) + 1, dtype=np.int32)
     for i, m in enumerate(mols):
         off[i + 1] = off[i] + len(m["Z"])
@@ -507,5 +530,8 @@ def md_batch(mols, nsteps, tstep, grad0, kT, opts=None, nthreads=0):
     o = opts if opts is not None else default_opts()
     fails = lib().qcxo_md_batch(len(mols), _p(off, ctypes.c_int), _p(Z, ctypes.c_int), _p(xyz), _p(vel), _p(mass),
                                 _p(grad), _p(epot), _p(charge), _p(kTa), int(nsteps), ctypes.c_double(tstep),
-                                ctypes.byref(o), int(nthreads), _p(iters, ctypes.c_int))
+                                ctypes.byref(o), int(nthreads), _p(iters, ctypes.c_int),
+                                None if active is None else _p(active, ctypes.c_int),
+                                None if steps_done is None else _p(steps_done, ctypes.c_int),
+                                None if busy_s is None else _p(busy_s))
     return fails, xyz, vel, grad, epot, iters

@@ -15,6 +15,7 @@
 #include "qcx_oracle.h"
 
 #include <math.h>
+#include <time.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1343,7 +1344,7 @@ int qcxo_checkqc(int nat, double* e, const double* grad, const double* qat, int 
 
 int qcxo_md_batch(int ntraj, const int* off, const int* Z, double* xyz, double* vel, const double* mass, double* grad,
                   double* epot, const double* charge, const double* kT, int nsteps, double tstep, const qcxo_opts* opts,
-                  int nthreads, int* scc_iters) {
+                  int nthreads, int* scc_iters, int* active, int* steps_done, double* busy_s) {
   int fails = 0;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1351,18 +1352,48 @@ int qcxo_md_batch(int ntraj, const int* off, const int* Z, double* xyz, double* 
 #endif
   for (int t = 0; t < ntraj; ++t) {
     int a0 = off[t], nat = off[t + 1] - off[t];
-    int iters = 0;
+    int iters = 0, done = 0;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    double* qat = malloc(sizeof(double) * nat);
     for (int st = 0; st < nsteps; ++st) {
+      if (active && !active[t]) break;
       double ke;
       qcxo_leapfrog(nat, grad + 3 * a0, mass + a0, tstep, xyz + 3 * a0, vel + 3 * a0, &ke);
       qcxo_info info;
-      double* qat = malloc(sizeof(double) * nat);
       int rc = qcxo_egrad(nat, Z + a0, xyz + 3 * a0, charge[t], kT[t], opts, &epot[t], grad + 3 * a0, qat, &info);
-      free(qat);
       iters += info.iterations;
-      if (rc != 0) fails++;
+      /* a failed calculation, or a result checkqc rejects with E = 0, ends the
+       * run (src/md.f90:317); with active == NULL every step is taken */
+      if (rc == 0) qcxo_checkqc(nat, &epot[t], grad + 3 * a0, qat, (int)charge[t]);
+      if (rc != 0 || epot[t] == 0.0) {
+        fails++;
+        if (active) active[t] = 0;
+      } else {
+        ++done;
+      }
     }
+    free(qat);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
     if (scc_iters) scc_iters[t] = iters;
+    if (steps_done) steps_done[t] = done;
+    if (busy_s) busy_s[t] = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+  }
+  return fails;
+}
+
+int qcxo_egrad_batch(int nmol, const int* off, const int* Z, const double* xyz, const double* charge, const double* kT,
+                     const qcxo_opts* opts, int nthreads, double* energy, double* grad, double* qat, int* rc) {
+  int fails = 0;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : fails)
+#endif
+  for (int t = 0; t < nmol; ++t) {
+    int a0 = off[t], nat = off[t + 1] - off[t];
+    qcxo_info info;
+    rc[t] = qcxo_egrad(nat, Z + a0, xyz + 3 * a0, charge[t], kT[t], opts, &energy[t], grad + 3 * a0, qat + a0, &info);
+    if (rc[t] != 0) fails++;
   }
   return fails;
 }

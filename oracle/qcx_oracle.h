@@ -80,13 +80,24 @@ int qcxo_checkqc(int nat, double* e, const double* grad, const double* qat, int 
 int qcxo_fragments(int nat, const int* Z, const double* xyz, double rcut, int at1, int at2, int* frag);
 
 /* Batched MD on the CPU: ntraj independent trajectories, each advanced nsteps
- * leapfrog + egrad steps (OpenMP over trajectories). Arrays are concatenated
- * per trajectory using atom offsets off[ntraj+1]. grad must hold the gradient
- * at the initial geometry. Returns the number of failed trajectory-steps. */
+ * leapfrog + egrad steps (OpenMP over trajectories, dynamic schedule: pass them
+ * largest first). Arrays are concatenated per trajectory using atom offsets
+ * off[ntraj+1]. grad must hold the gradient at the initial geometry. With
+ * active[ntraj] given, a trajectory whose calculation fails or whose result
+ * checkqc rejects (E = 0) stops (active[t] = 0), as the MD run ends
+ * (src/md.f90:317); steps_done[t] (may be NULL) counts its accepted steps and
+ * busy_s[t] (may be NULL) the wall seconds its thread spent on it.
+ * Returns the number of failed trajectory-steps. */
 int qcxo_md_batch(int ntraj, const int* off, const int* Z, double* xyz, double* vel,
                   const double* mass, double* grad, double* epot, const double* charge,
                   const double* kT, int nsteps, double tstep, const qcxo_opts* opts,
-                  int nthreads, int* scc_iters);
+                  int nthreads, int* scc_iters, int* active, int* steps_done, double* busy_s);
+
+/* Energy + gradient of nmol structures (OpenMP over structures); rc[nmol] gets
+ * each qcxo_egrad return code. Returns the number of failures. */
+int qcxo_egrad_batch(int nmol, const int* off, const int* Z, const double* xyz, const double* charge,
+                     const double* kT, const qcxo_opts* opts, int nthreads, double* energy, double* grad,
+                     double* qat, int* rc);
 
 #ifdef __cplusplus
 }

@@ -27,7 +27,8 @@ from . import constants
 
 __all__ = ["gfn1_xtb", "gfn2_xtb", "ipea1_xtb", "get_xtb_egrad", "Batch", "fragment_ips", "fragment_formula", "boltz", "read_ensemble", "load_library",
            "library_path",
-           "STATUS_SCC_NOT_CONVERGED", "STATUS_NON_FINITE", "STATUS_CHOLESKY_FAILED", "STATUS_EIGEN_NOT_CONVERGED"]
+           "STATUS_SCC_NOT_CONVERGED", "STATUS_NON_FINITE", "STATUS_CHOLESKY_FAILED", "STATUS_EIGEN_NOT_CONVERGED",
+           "STATUS_CHECKQC", "checkqc"]
 
 # method selectors, src/tblite.f90:34-40
 gfn1_xtb = 1
@@ -38,6 +39,7 @@ STATUS_SCC_NOT_CONVERGED = 1
 STATUS_NON_FINITE = 2
 STATUS_CHOLESKY_FAILED = 4
 STATUS_EIGEN_NOT_CONVERGED = 8
+STATUS_CHECKQC = 16
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _lib = None
@@ -72,6 +74,10 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_set_scc.argtypes = [ctypes.c_void_p, c_int, c_double, c_double, c_double]
     lib.qcx_batch_set_state.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double)]
     lib.qcx_batch_egrad.argtypes = [ctypes.c_void_p]
+    lib.qcx_batch_set_timing.argtypes = [ctypes.c_void_p, c_int]
+    lib.qcx_batch_get_timing.argtypes = [ctypes.c_void_p, P(ctypes.c_float), c_int]
+    lib.qcx_checkqc.argtypes = [c_int, P(c_double), P(c_double), c_int, P(c_double)]
+    lib.qcx_batch_load_state.argtypes = [ctypes.c_void_p, P(c_double), P(c_double)]
     lib.qcx_batch_step.argtypes = [ctypes.c_void_p, c_int, c_double]
     lib.qcx_batch_get.argtypes = [ctypes.c_void_p] + [P(c_double)] * 6 + [P(ctypes.c_int32)] * 2
     lib.qcx_batch_get_energy_terms.argtypes = [ctypes.c_void_p, c_int, P(c_double)]
@@ -234,6 +240,19 @@ def boltz(units, temp, ip):
     return out
 
 
+def checkqc(energy, grad, qat, charge):
+    """checkqc (src/iniqm.f90:684-715) evaluated on the GPU: returns (code,
+    energy) with code 0 accepted, 1 |E| < 1e-8, 2 gradient norm, 3 charges."""
+    lib = load_library()
+    grad = np.ascontiguousarray(grad, dtype=np.float64).reshape(-1, 3)
+    qat = np.ascontiguousarray(qat, dtype=np.float64)
+    e = ctypes.c_double(energy)
+    code = lib.qcx_checkqc(grad.shape[0], _dp(grad), _dp(qat), int(charge), ctypes.byref(e))
+    if code < 0:
+        raise RuntimeError("qcx_checkqc failed: " + _err(lib))
+    return code, e.value
+
+
 class Batch:
     """Independent trajectories on one GPU (one molecule each)."""
 
@@ -284,6 +303,14 @@ class Batch:
         self._check(self._lib.qcx_batch_set_state(self._h, _dp(xyz), _dp(vel), _dp(mass)), "set_state")
         self._lib.qcx_batch_sync(self._h)
 
+    def load_state(self, xyz=None, vel=None):
+        """New coordinates/velocities for the running trajectories, without
+        starting new runs (qcx_batch_load_state)."""
+        c = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(self.natom, 3)
+        xyz, vel = c(xyz), c(vel)
+        self._check(self._lib.qcx_batch_load_state(self._h, _dp(xyz), _dp(vel)), "load_state")
+        self._lib.qcx_batch_sync(self._h)
+
     def egrad(self):
         self._check(self._lib.qcx_batch_egrad(self._h), "egrad")
 
@@ -301,6 +328,13 @@ class Batch:
                                             _ip(status), _ip(iters)), "get")
         return {"xyz": xyz, "vel": vel, "grad": grad, "energy": energy, "qat": qat, "ekin": ekin,
                 "status": status, "iters": iters}
+
+    def status_iters(self):
+        """Status words and SCC iteration counts of the last evaluation only."""
+        status = np.zeros(self.nmol, dtype=np.int32); iters = np.zeros(self.nmol, dtype=np.int32)
+        self._check(self._lib.qcx_batch_get(self._h, None, None, None, None, None, None, _ip(status), _ip(iters)),
+                    "get")
+        return status, iters
 
     def energy_terms(self, i):
         t = np.zeros(12)
@@ -395,6 +429,24 @@ class Batch:
                     "profile_egrad")
         return dict(zip(["cn", "integrals", "scc", "zero_grad", "grad_pairs", "grad_atoms"], ms.tolist()))
 
+    def set_timing(self, on=True):
+        """Record timing marks inside the captured step graph (per molecule group:
+        integrals start, SCC start, SCC end, gradient end)."""
+        self._check(self._lib.qcx_batch_set_timing(self._h, int(bool(on))), "set_timing")
+
+    def timing(self):
+        """Marks of the last replayed step in ms from its start: dict with
+        'step' (total), 'scc_span' (first SCC start to last SCC end over the
+        groups), 'scc_sum' (sum of the groups' SCC durations) and the raw marks
+        [G][4]."""
+        buf = np.zeros(2 + 4 * 64, dtype=np.float32)
+        g = self._lib.qcx_batch_get_timing(self._h, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(buf))
+        if g < 0:
+            raise RuntimeError("get_timing failed: " + _err(self._lib))
+        marks = buf[1:1 + 4 * g].reshape(g, 4).astype(np.float64)
+        return {"step": float(buf[1 + 4 * g]), "scc_span": float(marks[:, 2].max() - marks[:, 1].min()),
+                "scc_sum": float(np.sum(marks[:, 2] - marks[:, 1])), "marks": marks}
+
     def sizes(self):
         nao = np.zeros(self.nmol, dtype=np.int32)
         nat = np.zeros(self.nmol, dtype=np.int32)
@@ -405,6 +457,12 @@ class Batch:
         """set_state from raw host pointers (e.g. pinned buffers)."""
         c = lambda p: None if p is None else ctypes.cast(p, ctypes.POINTER(ctypes.c_double))
         self._check(self._lib.qcx_batch_set_state(self._h, c(xyz_ptr), c(vel_ptr), None), "set_state")
+
+    def load_state_ptr(self, xyz_ptr=None, vel_ptr=None):
+        """qcx_batch_load_state from raw host pointers: new coordinates and
+        velocities for the running trajectories (stopped ones stay stopped)."""
+        c = lambda p: None if p is None else ctypes.cast(p, ctypes.POINTER(ctypes.c_double))
+        self._check(self._lib.qcx_batch_load_state(self._h, c(xyz_ptr), c(vel_ptr)), "load_state")
 
     def get_ptr(self, xyz_ptr=None, vel_ptr=None, energy_ptr=None):
         """get into raw host pointers (e.g. pinned buffers)."""

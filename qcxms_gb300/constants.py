@@ -20,6 +20,20 @@ _AMU = [0.0, 1.00794075, 4.00260193, 6.94003660, 9.01218307, 10.81102805, 12.010
         26.98153853, 28.08549871, 30.97376200, 32.06478741, 35.45293758, 39.94779856]
 MASS_AU = [m * AMUTOAU for m in _AMU]
 
+# Mass of the collision gas atom of the CID runs, gas%mIatom (src/input.f90:512-557).
+# The reference writes it as a default-real literal times amutoau, e.g.
+# `39.948 * amutoau` for Ar (src/input.f90:531): the literal is a single-precision
+# number, promoted to double for the product (the build sets no -fdefault-real-8).
+# It is not the standard atomic weight of MASS_AU. Keys: atomic number (N2 counts
+# per atom, as cid.f90:660-666 places two N atoms of this mass).
+_GAS_AMU_LITERAL = {2: 4.002, 7: 14.007, 10: 20.18, 18: 39.948}
+
+
+def gas_mass_au(z):
+    import numpy as np
+    return float(np.float32(_GAS_AMU_LITERAL[z])) * AMUTOAU
+
+
 # Rad (Angstrom) of QCxMS for Z = 1..18, bond criterion r < rcut * (Rad_i + Rad_j) / 2
 _RAD_AA = [0.0, 0.32, 0.37, 1.30, 0.99, 0.84, 0.75, 0.71, 0.64, 0.60, 0.62,
            1.60, 1.40, 1.24, 1.14, 1.09, 1.04, 1.00, 1.01]

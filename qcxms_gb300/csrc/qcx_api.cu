@@ -24,9 +24,13 @@ using namespace qcx;
 
 namespace {
 
-thread_local std::string g_last_error;
+// Text of the last failure of the calling thread: a fixed buffer, so that
+// setting it allocates nothing (qcx_egrad_noalloc sets it too).
+constexpr size_t kErrLen = 512;
+thread_local char g_last_error[kErrLen] = {0};
 
-void set_error(const std::string& s) { g_last_error = s; }
+void set_error_text(const char* s) { std::snprintf(g_last_error, kErrLen, "%s", s ? s : ""); }
+void set_error(const std::string& s) { set_error_text(s.c_str()); }
 
 #define CK(call)                                                                   \
   do {                                                                             \
@@ -140,6 +144,11 @@ struct qcx_batch {
   std::vector<cudaStream_t> g_stream;     // g_stream[0] is the batch stream
   std::vector<cudaEvent_t> g_join;
   cudaEvent_t g_fork = nullptr;
+  // Timing marks recorded inside the captured step (qcx_batch_set_timing):
+  // t_ev[0] at the start of the step, per group g four marks (integrals start,
+  // SCC start, SCC end, gradient end) at t_ev[1 + 4 g + k], the end of the step last.
+  bool timing = false;
+  std::vector<cudaEvent_t> t_ev;
 };
 
 namespace {
@@ -155,19 +164,31 @@ DevBatch group_dev(const qcx_batch* b, int g) {
   return d;
 }
 
+// Records timing mark k into the step graph being captured (an event record
+// node; a plain cudaEventRecord during capture only orders streams).
+int mark(qcx_batch* b, bool marks, int k, cudaStream_t st) {
+  if (!marks) return 0;
+  return cudaEventRecordWithFlags(b->t_ev[k], st, cudaEventRecordExternal) == cudaSuccess ? 0 : -1;
+}
+
 // Enqueues one energy + gradient evaluation; returns the number of kernels
-// launched, or -1 on an error in the stream bookkeeping.
-int enqueue_egrad(qcx_batch* b) {
+// launched, or -1 on an error in the stream bookkeeping. marks: record the
+// per-group timing marks (only while capturing the step graph).
+int enqueue_egrad(qcx_batch* b, bool marks = false) {
   const DevBatch& d = b->dev;
   int n = 0;
   launch_cn(d, b->stream);
   launch_zero_grad(d, b->stream);
   n += 2;
   if (b->ngroup == 1) {
+    if (mark(b, marks, 1, b->stream)) return -1;
     n += launch_integrals(d, b->stream);
+    if (mark(b, marks, 2, b->stream)) return -1;
     launch_scc(d, b->precision, b->stream);
+    if (mark(b, marks, 3, b->stream)) return -1;
     n += 1 + launch_grad_pairs(d, b->stream);
     launch_grad_atoms(d, b->stream);
+    if (mark(b, marks, 4, b->stream)) return -1;
     return n + 1;
   }
   if (cudaEventRecord(b->g_fork, b->stream) != cudaSuccess) return -1;
@@ -175,10 +196,14 @@ int enqueue_egrad(qcx_batch* b) {
     cudaStream_t st = b->g_stream[g];
     if (g > 0 && cudaStreamWaitEvent(st, b->g_fork, 0) != cudaSuccess) return -1;
     DevBatch gd = group_dev(b, g);
+    if (mark(b, marks, 1 + 4 * g, st)) return -1;
     n += launch_integrals(gd, st);  // the group's shell pairs only
+    if (mark(b, marks, 2 + 4 * g, st)) return -1;
     launch_scc(gd, b->precision, st);
+    if (mark(b, marks, 3 + 4 * g, st)) return -1;
     n += 1 + launch_grad_pairs(gd, st);
     launch_grad_atoms(gd, st);
+    if (mark(b, marks, 4 + 4 * g, st)) return -1;
     ++n;
     if (g > 0) {
       if (cudaEventRecord(b->g_join[g], st) != cudaSuccess) return -1;
@@ -211,6 +236,8 @@ void free_batch(qcx_batch* b) {
   for (cudaEvent_t e : b->g_join)
     if (e) cudaEventDestroy(e);
   if (b->g_fork) cudaEventDestroy(b->g_fork);
+  for (cudaEvent_t e : b->t_ev)
+    if (e) cudaEventDestroy(e);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -427,6 +454,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   d.steps_done = b->d_steps;
   d.have_prev = b->d_have_prev;
   d.guess = 0;
+  d.checkqc = 1;
   d.order = b->d_order;
   d.max_nao = b->max_nao;
   d.smem_bytes = (int)scc_smem_bytes(b->max_nao, 0);
@@ -452,14 +480,19 @@ int check_launch() {
 namespace qcx {
 // error text for qcx_last_error, set by the other translation units
 void set_last_error(const std::string& s) { set_error(s); }
+void set_last_error_text(const char* s) { set_error_text(s); }
 void batch_set_mixed_min_nao(qcx_batch* b, int n) { b->dev.mixed_min_nao = n; }
+void batch_set_checkqc(qcx_batch* b, int on) {
+  if (b->dev.checkqc != on) drop_graph(b);
+  b->dev.checkqc = on;
+}
 }  // namespace qcx
 
 extern "C" {
 
 int qcx_version(void) { return 100; }
 
-const char* qcx_last_error(void) { return g_last_error.c_str(); }
+const char* qcx_last_error(void) { return g_last_error; }
 
 qcx_batch* qcx_batch_create(int nmol, const int32_t* nat, const int32_t* num, const double* charge,
                             const double* etemp) {
@@ -688,6 +721,14 @@ int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, cons
   return 0;
 }
 
+int qcx_batch_load_state(qcx_batch* b, const double* xyz, const double* vel) {
+  if (!b) return -1;
+  const size_t n3 = sizeof(double) * 3 * b->natom;
+  if (xyz) CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));
+  if (vel) CK(cudaMemcpyAsync(b->d_vel, vel, n3, cudaMemcpyHostToDevice, b->stream));
+  return 0;
+}
+
 int qcx_batch_egrad(qcx_batch* b) {
   if (!b) return -1;
   int n = enqueue_egrad(b);
@@ -709,8 +750,10 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
       b->graph = nullptr;
     }
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const bool marks = b->timing;
+    int n = mark(b, marks, 0, b->stream);
     launch_leapfrog(b->dev, tstep, b->stream);
-    int n = enqueue_egrad(b);
+    if (n >= 0) n = enqueue_egrad(b, marks);
     if (n >= 0 && b->md_on) {
       // fragment_structure(nuc, iat, xyz, 3.0, 1, 0, list) of src/md.f90:450, then the rules
       launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream);
@@ -729,6 +772,7 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
       launch_cid_rules(b->dev, b->d_cid, b->d_nfrag, r, b->stream);
       n += 2;
     }
+    if (n >= 0 && mark(b, marks, 1 + 4 * b->ngroup, b->stream)) n = -1;
     cudaError_t ce = cudaStreamEndCapture(b->stream, &b->graph);
     if (n < 0 || ce != cudaSuccess) {
       if (ce == cudaSuccess && b->graph) cudaGraphDestroy(b->graph);
@@ -827,6 +871,32 @@ int qcx_batch_profile_egrad(qcx_batch* b, float* ms) {
   return check_launch();
 }
 
+int qcx_batch_set_timing(qcx_batch* b, int on) {
+  if (!b || (on != 0 && on != 1)) {
+    set_error("qcx_batch_set_timing: on must be 0 or 1");
+    return -1;
+  }
+  if (on && b->t_ev.empty()) {
+    b->t_ev.assign(2 + 4 * (size_t)b->ngroup, nullptr);
+    for (auto& e : b->t_ev) CK(cudaEventCreate(&e));
+  }
+  if ((on != 0) != b->timing) drop_graph(b);
+  b->timing = on != 0;
+  return 0;
+}
+
+int qcx_batch_get_timing(qcx_batch* b, float* ms, int n) {
+  if (!b || !ms || !b->timing || n < 2 + 4 * b->ngroup) {
+    set_error("qcx_batch_get_timing: timing marks are off (qcx_batch_set_timing) or the output is too small");
+    return -1;
+  }
+  const int m = 2 + 4 * b->ngroup;
+  CK(cudaEventSynchronize(b->t_ev[m - 1]));
+  ms[0] = 0.0f;
+  for (int k = 1; k < m; ++k) CK(cudaEventElapsedTime(&ms[k], b->t_ev[0], b->t_ev[k]));
+  return b->ngroup;
+}
+
 int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat) {
   if (!b) return -1;
   for (int m = 0; m < b->nmol; ++m) {
@@ -834,6 +904,33 @@ int qcx_batch_get_sizes(qcx_batch* b, int32_t* nao, int32_t* nat) {
     if (nat) nat[m] = b->mol[m].nat;
   }
   return 0;
+}
+
+int qcx_checkqc(int nat, const double* grad, const double* qat, int charge, double* energy) {
+  if (nat < 1 || !grad || !qat || !energy) {
+    set_error("qcx_checkqc: invalid arguments");
+    return -1;
+  }
+  double* d = nullptr;
+  const size_t nd = 4 * (size_t)nat + 1;
+  CK(cudaMalloc((void**)&d, sizeof(double) * nd + sizeof(int)));
+  int* dcode = (int*)(d + nd);
+  int code = -1;
+  cudaError_t e = cudaMemcpy(d, grad, sizeof(double) * 3 * nat, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + 3 * nat, qat, sizeof(double) * nat, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + 4 * nat, energy, sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    launch_checkqc(nat, d, d + 3 * nat, (double)charge, d + 4 * nat, dcode, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(energy, d + 4 * nat, sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&code, dcode, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error(std::string("qcx_checkqc: ") + cudaGetErrorString(e));
+    return -1;
+  }
+  return code;
 }
 
 // ---------------------------------------------------------------------------
@@ -871,8 +968,11 @@ int qcx_egrad(int method, int nat, const int32_t* num, const double* xyz, int ch
   int32_t st = 0;
   if (qcx_batch_get(cached, nullptr, nullptr, grad, energy, qat, nullptr, &st, nullptr)) return -1;
   if (st != 0) {
-    char buf[96];
-    std::snprintf(buf, sizeof(buf), "calculation failed, status bits 0x%x", st);
+    char buf[128];
+    if (st == QCX_STATUS_CHECKQC)
+      std::snprintf(buf, sizeof(buf), "result rejected by checkqc (energy, gradient norm or charges out of range)");
+    else
+      std::snprintf(buf, sizeof(buf), "calculation failed, status bits 0x%x", st);
     set_error(buf);
     return -1;
   }

@@ -73,6 +73,41 @@ __device__ inline double block_sum(double v, double* red) {
   return s;
 }
 
+// gnorm (src/iniqm.f90:719-732): the reference sums grad(1,i)**2 and
+// grad(2,i)**2 twice (no z term) in atom order; kept as written, with explicit
+// roundings, because it decides which results checkqc accepts.
+__device__ double gnorm(int nat, const double* g) {
+  double gn = 0.0;
+  for (int a = 0; a < nat; ++a) {
+    const double x = g[3 * a], y = g[3 * a + 1];
+    gn = __dadd_rn(__dadd_rn(__dadd_rn(gn, __dmul_rn(x, x)), __dmul_rn(y, y)), __dmul_rn(y, y));
+  }
+  return __dsqrt_rn(gn);
+}
+
+// checkqc (src/iniqm.f90:684-715), which egrad applies to every GFN2 result
+// (src/iniqm.f90:650). Returns 0 when the result is accepted, else the failed
+// test: 1 |E| < 1e-8 (energy left as it is), 2 gnorm outside [1e-8, 20],
+// 3 a cation (mchrg > 0) with max(qat) below 1e-5 in magnitude; 2 and 3 set
+// e = 0 as the reference does. 20.0 is a default-real literal, exact in FP32.
+__device__ int checkqc(int nat, const double* grad, const double* qat, double charge, double& e) {
+  if (fabs(e) < 1.0e-8) return 1;
+  const double gn = gnorm(nat, grad);
+  if (gn < 1.0e-8 || gn > (double)20.0f) {
+    e = 0.0;
+    return 2;
+  }
+  if (charge > 0.0) {
+    double mx = qat[0];
+    for (int a = 1; a < nat; ++a) mx = qat[a] > mx ? qat[a] : mx;
+    if (fabs(mx) < 1.0e-5) {
+      e = 0.0;
+      return 3;
+    }
+  }
+  return 0;
+}
+
 __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
   extern __shared__ __align__(16) double sm[];
   const int mol = bt.order ? bt.order[blockIdx.x] : blockIdx.x;
@@ -312,17 +347,40 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
     for (int k = 0; k < 3; ++k) bt.grad[3LL * (off + a) + k] += g[3 * a + k];
   erep = block_sum(erep, red);
   eatm = block_sum(eatm, red);
+  __syncthreads();  // the gradient rows written above are read by checkqc
   if (threadIdx.x == 0) {
     double* E = bt.energy + (long long)mol * kNumEnergy;
     E[kEAtm] = eatm;
     E[kERep] = erep;
     E[kETotal] += eatm + erep;
     if (!isfinite(E[kETotal])) bt.status[mol] |= kNonFinite;
-    // a failed evaluation ends the trajectory, as QCxMS ends an MD run whose
-    // energy call failed (src/md.f90:317-344 via src/iniqm.f90:650-654)
-    if (bt.status[mol] & (kSccNotConverged | kNonFinite | kCholeskyFailed)) bt.active[mol] = 0;
+    if (bt.checkqc && !(bt.status[mol] & kFailedEval)) {
+      double e = E[kETotal];
+      if (checkqc(nat, bt.grad + 3LL * off, bt.qat + off, md.charge, e)) bt.status[mol] |= kCheckqcFailed;
+      E[kETotal] = e;
+    }
+    // A failed evaluation ends the trajectory, as QCxMS ends an MD run whose
+    // energy call failed (src/md.f90:317-344). checkqc's rejections zero the
+    // energy, and md.f90:317 ends the run on Epot == 0; a tiny energy
+    // (|E| < 1e-8) is reported but keeps its value, and that run goes on.
+    if ((bt.status[mol] & kFailedEval) || E[kETotal] == 0.0) bt.active[mol] = 0;
     else bt.steps_done[mol] += 1;
   }
+}
+
+// checkqc of one result held in device memory (qcx_checkqc): the same device
+// function the gradient kernel applies to every evaluation
+__global__ void k_checkqc(int nat, const double* grad, const double* qat, double charge, double* e, int* code) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double v = *e;
+    *code = checkqc(nat, grad, qat, charge, v);
+    *e = v;
+  }
+}
+
+void launch_checkqc(int nat, const double* grad, const double* qat, double charge, double* e, int* code,
+                    cudaStream_t st) {
+  k_checkqc<<<1, 32, 0, st>>>(nat, grad, qat, charge, e, code);
 }
 
 void launch_grad_atoms(const DevBatch& bt, cudaStream_t st) {

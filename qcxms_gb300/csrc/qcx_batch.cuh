@@ -37,7 +37,11 @@ enum Status : int {
   kNonFinite = 2,
   kCholeskyFailed = 4,
   kEigenNotConverged = 8,
+  // checkqc (src/iniqm.f90:684-715) rejected the result
+  kCheckqcFailed = 16,
 };
+// evaluations that end a trajectory whatever checkqc says
+constexpr int kFailedEval = kSccNotConverged | kNonFinite | kCholeskyFailed;
 
 struct MolDesc {
   int nat, nsh, nao, len;      // len = nsh + 9 nat (mixed moment vector)
@@ -135,6 +139,7 @@ struct DevBatch {
   long long* steps_done;  // [nmol] successful energy+gradient evaluations
   int* have_prev;    // [nmol] 1 when the moment vector of a converged SCC at an earlier geometry is kept
   int guess;         // SCC start: 0 = zero moments (a fresh wavefunction every call), 1 = the kept moments
+  int checkqc;       // 1: apply checkqc after every evaluation, as egrad does (src/iniqm.f90:650)
   const int* order;  // [nmol] molecules by decreasing size: CTA b of a per-molecule kernel takes order[b]
   int max_nao;
   int smem_bytes;  // dynamic shared memory granted to the SCC kernel

@@ -54,8 +54,10 @@ __device__ double gas_distance(const DevBatch& bt, const MolDesc& md, const doub
   return norm3(__dsub_rn(g[0], cm[0]), __dsub_rn(g[1], cm[1]), __dsub_rn(g[2], cm[2]));
 }
 
+// gradfail of egrad: a failed calculation or a result checkqc rejects in any of
+// its three tests (src/iniqm.f90:650-654); cid.f90:763-766 stops the run on it
 __device__ bool failed_eval(const DevBatch& bt, int mol) {
-  return (bt.status[mol] & (kSccNotConverged | kNonFinite | kCholeskyFailed)) != 0;
+  return (bt.status[mol] & (kFailedEval | kCheckqcFailed)) != 0;
 }
 
 }  // namespace

@@ -146,6 +146,7 @@ int qcx_fragment_ips(int method, int ntraj, const int32_t* nat, const int32_t* n
     qcx_batch* b = qcx_batch_create(np, pnat.data(), pnum.data(), pch.data(), pet.data());
     if (!b) return -1;
     qcx::batch_set_mixed_min_nao(b, kFragMixedMinNao);
+    qcx::batch_set_checkqc(b, 0);  // eqm (src/iniqm.f90:241-427) does not call checkqc
     int rc = qcx_batch_set_precision(b, precision);
     if (!rc) rc = qcx_batch_set_state(b, pxyz.data(), nullptr, nullptr);
     if (!rc) rc = qcx_batch_egrad(b);

@@ -19,6 +19,10 @@ int launch_grad_pairs(const DevBatch& bt, cudaStream_t st);
 void launch_grad_atoms(const DevBatch& bt, cudaStream_t st);
 void launch_leapfrog(const DevBatch& bt, double tstep, cudaStream_t st);
 void launch_zero_grad(const DevBatch& bt, cudaStream_t st);
+// checkqc (src/iniqm.f90:684-715) of one result in device memory: *code = 0
+// accepted, 1 |E| < 1e-8, 2 gradient norm, 3 charges; *e set to 0 for 2 and 3
+void launch_checkqc(int nat, const double* grad, const double* qat, double charge, double* e, int* code,
+                    cudaStream_t st);
 // fragment numbers of every molecule's atoms (frag[natom]) and fragment counts (nfrag[nmol])
 // skip_last = 1: the last atom of every molecule is left out (fragment 0)
 void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,
@@ -59,9 +63,14 @@ void launch_cid_rules(const DevBatch& bt, CidState* st, const int* nfrag, const 
 
 // sets the text qcx_last_error() returns
 void set_last_error(const std::string& s);
+// the same from a C string, without allocating
+void set_last_error_text(const char* s);
 // mixed mode: molecules with fewer atomic orbitals run FP64 SCC iterations only
 // (0 by default; set before the batch's first evaluation)
 void batch_set_mixed_min_nao(::qcx_batch* b, int n);
+// 0: results are not put through checkqc (the fragment single points of
+// analyse go through eqm, which does not call it); 1 (default): egrad's checks
+void batch_set_checkqc(::qcx_batch* b, int on);
 
 // dynamic shared memory the SCC kernel asks for, given the largest molecule
 size_t scc_smem_bytes(int max_nao, int precision);

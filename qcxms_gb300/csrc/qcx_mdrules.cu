@@ -35,9 +35,10 @@ __device__ double temp_of(double e, int n) {
 }
 
 // energy of molecule mol for the bookkeeping: 0 after a failed evaluation,
-// which is how the reference's loop sees a failed energy call
+// which is how the reference's loop sees a failed energy call (checkqc's
+// rejections have already set the energy to 0)
 __device__ double epot_of(const DevBatch& bt, int mol) {
-  if (bt.status[mol] & (kSccNotConverged | kNonFinite | kCholeskyFailed)) return 0.0;
+  if (bt.status[mol] & kFailedEval) return 0.0;
   return bt.energy[(long long)mol * kNumEnergy + kETotal];
 }
 

@@ -11,7 +11,9 @@
 // uses file-scope host buffers, inputs and outputs are plain host pointers.
 //
 // Limits: at most QCX_NOALLOC_MAX_ATOMS atoms and QCX_NOALLOC_MAX_NAO atomic
-// orbitals (64 and 160; about 6 MB of device memory).
+// orbitals (64 and 160; about 6 MB of device memory). After cudaDeviceReset the
+// next call finds the array without its parameters (a marker word is checked
+// on every call) and copies them in again.
 // The array is held by every GPU that loads the library until the process
 // exits. All calls share it: calls that overlap on the GPU race on it (within
 // one process the host side serialises calls with a mutex, so only work the
@@ -39,7 +41,7 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // byte offsets of every region inside the static array
 struct StaticLayout {
-  size_t prm, mol, Z, atom_mol, sh_atom, sh_k, sh_ao, pairs, xyz, grad, vel, mass, cn, cnd, dedcn, dedcnd, mrad,
+  size_t magic, prm, mol, Z, atom_mol, sh_atom, sh_k, sh_ao, pairs, xyz, grad, vel, mass, cn, cnd, dedcn, dedcnd, mrad,
       dmrad, w4, dw4, qat, mats, vecs, energy, ekin, status, iters, active, steps, total;
 };
 
@@ -56,6 +58,7 @@ constexpr StaticLayout make_layout() {
                                 r4((long long)na * na) * 7 + r4(na) * 2 + r4((long long)kStaticNmem * len) * 2 +
                                 r4((long long)kStaticNmem * kStaticNmem) + r4(len) * 2 + r4(kStaticNmem) +
                                 r4((long long)kStaticNmem * kStaticNmem + kStaticNmem);
+  L.magic = o; o = align256(o + sizeof(unsigned long long));
   L.prm = o; o = align256(o + sizeof(Params));
   L.mol = o; o = align256(o + sizeof(MolDesc));
   L.Z = o; o = align256(o + sizeof(int) * na);
@@ -115,10 +118,12 @@ long long h_zero_ll[1] = {0};
 double h_energy[kNumEnergy];
 Params h_params;
 
-// Failures are reported on stderr (formatting into a stack buffer; no heap use)
-// and by the return value -1.
+// Failures are reported by the return value -1, on stderr, and in the text
+// qcx_last_error() returns (a fixed per-thread buffer; formatting goes into
+// stack buffers, so reporting allocates nothing).
 int fail(const char* what) {
   std::fprintf(stderr, "%s\n", what);
+  qcx::set_last_error_text(what);
   return -1;
 }
 
@@ -168,24 +173,38 @@ void fill_params_static(Params& p) {
   do {                                                                  \
     cudaError_t e_ = (call);                                            \
     if (e_ != cudaSuccess) {                                            \
-      std::fprintf(stderr, "%s: %s\n", what, cudaGetErrorString(e_));   \
-      return -1;                                                        \
+      char m_[192];                                                     \
+      std::snprintf(m_, sizeof(m_), "%s: %s", what, cudaGetErrorString(e_)); \
+      return fail(m_);                                                  \
     }                                                                   \
   } while (0)
 
-// Once per device, with that device current: find the array's device address
-// and copy the parameter block into it.
+// Written after the parameter block once it is in place; a device reset (or a
+// context created anew) leaves the array zeroed, which the next call sees here.
+constexpr unsigned long long kParamsMagic = 0x51435847505531ull;
+unsigned long long h_magic = kParamsMagic;
+
+// With the device current: find the array's device address (every call, it is
+// a cheap lookup) and, on the first call on this device or when the array no
+// longer holds the parameters (after cudaDeviceReset), copy them in.
 int static_setup(int dev, unsigned char** base) {
   if (dev < 0 || dev >= kMaxDevices) return fail("qcx_egrad_noalloc: device index out of range");
-  if (g_static_base[dev]) {
-    *base = g_static_base[dev];
-    return 0;
-  }
   void* ptr = nullptr;
   SCK(cudaGetSymbolAddress(&ptr, g_static_scratch), "qcx_egrad_noalloc: cudaGetSymbolAddress");
-  fill_params_static(h_params);
   unsigned char* b = (unsigned char*)ptr;
+  if (g_static_base[dev] == b) {
+    unsigned long long magic = 0;
+    SCK(cudaMemcpy(&magic, b + kLayout.magic, sizeof(magic), cudaMemcpyDeviceToHost),
+        "qcx_egrad_noalloc: parameter check");
+    if (magic == kParamsMagic) {
+      *base = b;
+      return 0;
+    }
+  }
+  fill_params_static(h_params);
   SCK(cudaMemcpy(b + kLayout.prm, &h_params, sizeof(Params), cudaMemcpyHostToDevice),
+      "qcx_egrad_noalloc: parameter upload");
+  SCK(cudaMemcpy(b + kLayout.magic, &h_magic, sizeof(h_magic), cudaMemcpyHostToDevice),
       "qcx_egrad_noalloc: parameter upload");
   g_static_base[dev] = b;
   *base = b;
@@ -255,6 +274,16 @@ extern "C" int qcx_egrad_noalloc(int method, int nat, const int32_t* num, const 
   h_mol.kT = etemp * QCX_KTOAU;
   h_mol.charge = charge;
 
+  // The regions above were sized from the largest molecule the limits allow;
+  // check this molecule's real layout against them before any launch.
+  {
+    const long long vec_need = VecLayout::make(nat, nsh, nao, nsh + 9 * nat, kStaticNmem).total;
+    const long long np_ = nao + (nao & 1);
+    if ((size_t)vec_need * sizeof(double) > kLayout.energy - kLayout.vecs ||
+        (size_t)kNumMat * np_ * np_ * sizeof(double) > kLayout.vecs - kLayout.mats ||
+        (size_t)npair * sizeof(ShellPair) > kLayout.xyz - kLayout.pairs)
+      return fail("qcx_egrad_noalloc: internal error: the static scratch layout is too small for this molecule");
+  }
   int dev = 0;
   SCK(cudaGetDevice(&dev), "qcx_egrad_noalloc: cudaGetDevice");
   unsigned char* base = nullptr;
@@ -313,6 +342,7 @@ extern "C" int qcx_egrad_noalloc(int method, int nat, const int32_t* num, const 
   d.smem_bytes = (int)scc_smem_bytes(nao, 0);
   d.max_iter = QCX_SCC_MAXITER;
   d.mixed_min_nao = 0;
+  d.checkqc = 1;
   d.econv = QCX_SCC_ECONV;
   d.pconv = QCX_SCC_PCONV;
   d.mix_alpha = QCX_BROYDEN_ALPHA;
@@ -333,8 +363,11 @@ extern "C" int qcx_egrad_noalloc(int method, int nat, const int32_t* num, const 
   SCK(cudaMemcpy(qat, base + L.qat, sizeof(double) * nat, d2h), "qcx_egrad_noalloc: download");
   *energy = h_energy[kETotal];
   if (status != 0) {
-    char msg[96];
-    std::snprintf(msg, sizeof(msg), "qcx_egrad_noalloc: calculation failed, status bits 0x%x", status);
+    char msg[128];
+    if (status == QCX_STATUS_CHECKQC)
+      std::snprintf(msg, sizeof(msg), "qcx_egrad_noalloc: result rejected by checkqc");
+    else
+      std::snprintf(msg, sizeof(msg), "qcx_egrad_noalloc: calculation failed, status bits 0x%x", status);
     return fail(msg);
   }
   return 0;

@@ -10,6 +10,7 @@
 // refine the previous coefficients: B = C^T F C is nearly diagonal, and a
 // first-order (GEMM) refinement, exact rotations of hard pairs, or a warm
 // Jacobi sweep on B updates them.
+#include <atomic>
 #include <cfloat>
 #include <type_traits>
 
@@ -2369,11 +2370,17 @@ namespace qcx {
 #endif
 
 void launch_scc(const DevBatch& bt, int precision, cudaStream_t st) {
-  static int configured = 0;
-  if (!configured) {
+  // The shared-memory limit is a per-device attribute of each kernel: set it
+  // once on every device this process launches on (one bit per device index;
+  // two threads racing to set it both set the same value).
+  static std::atomic<unsigned long long> configured{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(configured.load(std::memory_order_acquire) & bit)) {
     cudaFuncSetAttribute(k_scc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
     cudaFuncSetAttribute(k_scc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
-    configured = 1;
+    configured.fetch_or(bit, std::memory_order_release);
   }
   if (precision == 1)
     k_scc<1><<<bt.nmol, kSccThreads, bt.smem_bytes, st>>>(bt);

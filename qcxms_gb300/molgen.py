@@ -6,6 +6,7 @@ are attached at 1.09 Angstrom, and every coordinate gets Gaussian jitter.
 """
 import numpy as np
 
+from . import constants
 from .constants import AATOAU, KB_AU, MASS_AU
 
 VALENCE = {1: 1, 6: 4, 7: 3, 8: 2, 9: 1, 15: 3, 16: 2, 17: 1, 14: 4, 5: 3}
@@ -139,8 +140,9 @@ def cid_workload(ntraj, nmin=10, nmax=80, seed0=0, e_lab_ev=40.0, bmax_aa=2.0, t
         vion = np.sqrt(2.0 * e_lab_ev * EVTOAU / m.sum())
         vel = vel + vion * u
         Zc = np.concatenate([Z, [AR_Z]]).astype(np.int32)
+        # the gas atom's mass is gas%mIatom (src/input.f90:531), placed at mass0(nuc0) (src/cid.f90:657)
         mols.append({"Z": Zc, "xyz": np.vstack([xyz, ar]), "vel": np.vstack([vel, np.zeros(3)]),
-                     "mass": np.concatenate([m, [MASS_AU[AR_Z]]]), "charge": 1, "temp": temp,
+                     "mass": np.concatenate([m, [constants.gas_mass_au(AR_Z)]]), "charge": 1, "temp": temp,
                      "impact_parameter": b})
     return mols
 

@@ -53,6 +53,36 @@ def test_oracle_collision_known_answers(oracle_lib):
     assert s["avgT"] == 450.0 and s["ecom"] == 0.0
 
 
+def test_gas_atom_mass_is_the_reference_literal(oracle_lib):
+    """gas%mIatom = 39.948 * amutoau (src/input.f90:531): a default-real literal
+    (single precision, promoted for the product) times amutoau = amutokg *
+    (1/metokg) (src/xtb_mctc_convert.f90:47-51). The workload places it at
+    mass0(nuc0) (src/cid.f90:657) and the collision rules take beta =
+    m_gas / (m_gas + summass) from it, summass summed in atom order
+    (src/cid.f90:342-347). All bit for bit."""
+    amutoau = 1.660539040e-27 * (1.0 / 9.10938356e-31)
+    m_ar = float(np.float32(39.948)) * amutoau
+    assert float(np.float32(39.948)) != 39.948  # the literal is not the double 39.948
+    assert constants.gas_mass_au(18) == m_ar and m_ar != constants.MASS_AU[18]
+    for m in molgen.cid_workload(5, 10, 14, seed0=31):
+        assert m["Z"][-1] == 18 and m["mass"][-1] == m_ar
+        summass = 0.0
+        for x in m["mass"][:-1]:
+            summass = summass + x
+        s = oracle_lib.cid_rules_begin(m["xyz"], m["mass"], 100)
+        assert s["summass"] == summass
+        # two steps of an ion moving by 0.01 Bohr per step along x: the collision
+        # energy is beta * E_velo in eV with beta = m_gas / (m_gas + summass)
+        x0 = np.asarray(m["xyz"], dtype=np.float64)
+        for k in (1, 2):
+            xk = x0.copy()
+            xk[:-1, 0] += 0.01 * k
+            oracle_lib.cid_rules_step(s, False, xk, np.zeros_like(x0), m["mass"], 1, DT, 300.0)
+        v = (0.01 / DT) / (1.0 / 2.18769126364e6) * (1.0 / 2.18769126364e6)
+        e_velo = (0.5 * summass) * (v * v)
+        assert abs(s["ecom"] - (m_ar / (m_ar + summass)) * e_velo * constants.AUTOEV) < 1e-12 * s["ecom"]
+
+
 @pytest.mark.gpu
 def test_gpu_cid_rules_match_oracle(gpu, oracle_lib):
     o = oracle_lib
@@ -64,7 +94,8 @@ def test_gpu_cid_rules_match_oracle(gpu, oracle_lib):
     r = b.get()
     off = np.concatenate([[0], np.cumsum([len(m["Z"]) for m in mols])])
     ref = [o.cid_rules_begin(r["xyz"][off[i]:off[i + 1]], list(m["mass"]), ntot) for i, m in enumerate(mols)]
-    fail = qg.STATUS_SCC_NOT_CONVERGED | qg.STATUS_NON_FINITE | qg.STATUS_CHOLESKY_FAILED
+    # gradfail of egrad ends a collision run: a failed calculation or any checkqc rejection (src/cid.f90:763)
+    fail = qg.STATUS_SCC_NOT_CONVERGED | qg.STATUS_NON_FINITE | qg.STATUS_CHOLESKY_FAILED | qg.STATUS_CHECKQC
     keys = ["nstep", "nfrag", "collided", "fragmented", "total_steps", "done", "failed"]
     for step in range(nsteps + 1):
         st = b.cid_state()

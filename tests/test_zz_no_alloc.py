@@ -54,6 +54,26 @@ def test_noalloc_matches_allocating_entry_point(gpu):
         assert np.abs(q - qr).max() < 1e-7
 
 
+def test_noalloc_near_its_size_limit_matches_oracle(gpu, oracle_lib):
+    """A 60-atom cation with 159 atomic orbitals, next to the limit of 160: the
+    largest static regions in use. Two calls in a row; both agree with the
+    allocating entry point and with the CPU oracle (default SCC thresholds on
+    both sides: energies within 1e-7 Eh, gradients within 5e-6 Eh/Bohr, the
+    spread of where two correct SCC runs stop)."""
+    from qcxms_gb300 import constants, molgen
+    f = _bind(gpu)
+    Z, xyz = molgen.random_chno(60, 6)
+    assert oracle_lib.nao(Z) == 159
+    rc_o, e_o, g_o, q_o, info = oracle_lib.egrad(Z, xyz, 1, kT=300.0 * constants.KB_AU)
+    assert rc_o == 0
+    for k in range(2):
+        rc, e, g, q = _call(f, Z, xyz, 1)
+        qr, er, gr, stat = qg.get_xtb_egrad(Z, xyz, 1, 2, qg.gfn2_xtb, 300.0)
+        assert rc == 0 and stat == 0, k
+        assert abs(e - er) < 1e-8 and np.abs(g - gr).max() < 1e-7
+        assert abs(e - e_o) < 1e-7 and np.abs(g - g_o).max() < 5e-6 and np.abs(q - q_o).max() < 1e-5
+
+
 def test_noalloc_rejects_oversized_input(gpu, capfd):
     f = _bind(gpu)
     Z = np.array([6] * 70, dtype=np.int32)
@@ -61,3 +81,5 @@ def test_noalloc_rejects_oversized_input(gpu, capfd):
     rc, e, g, q = _call(f, Z, xyz, 1)
     assert rc == -1
     assert "static scratch limit" in capfd.readouterr().err
+    gpu.qcx_last_error.restype = ctypes.c_char_p
+    assert b"static scratch limit" in gpu.qcx_last_error()
