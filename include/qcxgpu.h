@@ -184,8 +184,9 @@ int qcx_batch_fragments(qcx_batch* b, double rcut, int at1, int at2, int32_t* fr
  * the first loop top uses that energy and the kinetic energy of the current
  * velocities (ekinet, src/mdinit.f90:57-76). New coordinates through
  * qcx_batch_set_state switch the rules off. The heating of the first steps is
- * set up by qcx_batch_set_md_heating. Not covered: a per-step electronic
- * temperature (ieetemp != 0), the CID branch, the output-file averages.
+ * set up by qcx_batch_set_md_heating, the per-step electronic temperature
+ * by qcx_batch_set_md_etemp. Not covered: the CID branch, the output-file
+ * averages.
  */
 int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps);
 
@@ -206,11 +207,24 @@ int qcx_batch_get_md_avg_xyz(qcx_batch* b, double* axyz);
  * before qcx_batch_set_md_rules, which reads these values. The running mean of
  * the total energy starts after the nadd steps (src/md.f90:304-309). A run whose
  * scaling needs 20000 increments ends (the reference stops the program). The
- * electronic temperature stays the batch's: with the default ieetemp = 0,
- * setetemp (src/utility.f90:69-86) gives the constant 5000 + 20000 ax, which is
- * the etemp to create the batch with. */
+ * electronic temperature follows qcx_batch_set_md_etemp when that is on. */
 int qcx_batch_set_md_heating(qcx_batch* b, const double* eimp, const double* tadd, const double* velof,
                              double tstep);
+
+/* Electronic temperature of every MD step (EI runs): setetemp
+ * (src/utility.f90:69-86), which src/md.f90:443-446 calls after every step
+ * with dum = eimp - eimp*nstep/nadd and the step's fragment count before
+ * fragment_structure: etemp = 5000 + 20000 ax, plus dum * ieetemp while
+ * dum > 0 and the molecule is one fragment. The next evaluation runs at
+ * kT = etemp * ktoau (src/tblite.f90:133). The start uses setetemp(1, eimp)
+ * (src/md.f90:167-168), which this call sets right away, so call it after
+ * qcx_batch_set_md_heating (eimp) and before the qcx_batch_egrad of the start
+ * geometry, then qcx_batch_set_md_rules. ax and ieetemp are the input's (0
+ * and 0 by default, src/input.f90:199). New coordinates through
+ * qcx_batch_set_state switch it off and restore the batch's temperatures. */
+int qcx_batch_set_md_etemp(qcx_batch* b, double ax, double ieetemp);
+/* Electronic temperature (K) of every trajectory's next evaluation. */
+int qcx_batch_get_md_etemp(qcx_batch* b, double* etemp);
 
 /* State of the MD rules per trajectory (any pointer may be NULL): nstep,
  * nfrag (fragments at the last step), fragstate (1: exit on fragment count or

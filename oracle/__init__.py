@@ -309,14 +309,26 @@ def md_heating(eimp, tadd, tstep):
     return eimp, tstep / (tadd + tstep), int((tadd + tstep) / tstep - 1.0)
 
 
-def md_rules_begin(vel, mass, epot, heat=None, xyz=None):
+def setetemp(nfrag, eimp, ax, ieetemp):
+    """setetemp (src/utility.f90:69-86): 5000. + 20000.*ax, plus max(eimp, 0)*ieetemp
+    while eimp > 0 and nfrag <= 1 (5000. and 20000. are exact single-precision literals)."""
+    etemp = 5000.0 + 20000.0 * ax
+    if eimp > 0 and nfrag <= 1:
+        etemp = etemp + max(eimp, 0.0) * ieetemp
+    return etemp
+
+
+def md_rules_begin(vel, mass, epot, heat=None, xyz=None, etemp=None):
     """State before the loop: ekinet (src/mdinit.f90:57-76) and the first top.
-    heat = (eimp, fadd, nadd) of md_heating, or None."""
+    heat = (eimp, fadd, nadd) of md_heating, or None; etemp = (ax, ieetemp) for the
+    per-step electronic temperature, or None."""
     s = {"nstep": 0, "nfrag": 1, "fconst": 0, "morestep": 0, "fragstate": 0, "mdok": 0, "done": 0, "tav": 0.0,
          "epav": 0.0, "ekav": 0.0, "edum": 0.0, "eerror": 0.0, "ttime": 0.0, "dtime": 0.0, "fragT": [0.0] * 10,
-         "eimp": 0.0, "fadd": 0.0, "nadd": 0, "heat_failed": 0, "kdump": 50, "avxyz": None}
+         "eimp": 0.0, "fadd": 0.0, "nadd": 0, "heat_failed": 0, "kdump": 50, "avxyz": None, "etemp": -1.0}
     if heat is not None:
         s["eimp"], s["fadd"], s["nadd"] = heat
+    if etemp is not None:
+        s["etemp"] = setetemp(1, s["eimp"], *etemp)  # src/md.f90:167-168
     ek = _ekinet(vel, mass)
     s["ekinstart"] = ek
     if epot == 0:
@@ -326,10 +338,13 @@ def md_rules_begin(vel, mass, epot, heat=None, xyz=None):
     return s
 
 
-def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more, max_steps, velof=None, xyz=None):
+def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more, max_steps, velof=None, xyz=None,
+                  etemp=None):
     """Rest of one loop iteration after leapfrog + egrad (src/md.f90:426-679,
     electron-impact branch), then the next top. epot = 0 for a failed call.
-    vel (the velocities after leapfrog) is scaled in place while heating."""
+    vel (the velocities after leapfrog) is scaled in place while heating.
+    etemp = (ax, ieetemp): s["etemp"] becomes the next evaluation's electronic
+    temperature (src/md.f90:443-446)."""
     if s["done"]:
         return s
     s["ttime"] = s["ttime"] + tstep / FSTOAU
@@ -342,6 +357,10 @@ def md_rules_step(s, epot, ekin, vel, mass, frag, nfrag, tstep, nfragexit, more,
         if not impactscale(vel, mass, velof, s["eimp"], s["fadd"] * s["nstep"], s["ekinstart"]):
             s["heat_failed"], s["done"] = 1, 1
             return s
+    if etemp is not None:  # src/md.f90:443-446, with the previous step's fragment count
+        dum = s["eimp"] - s["eimp"] * float(np.float32(s["nstep"])) / float(np.float32(s["nadd"])) \
+            if s["nadd"] != 0 else float("nan")
+        s["etemp"] = setetemp(s["nfrag"], dum, *etemp)
     s["nfrag"] = nfrag
     if nfrag > 1:  # intenergy, src/md.f90:715-741
         eint, cnt = [0.0] * 10, [0] * 10

@@ -101,6 +101,8 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_set_cid_rules.argtypes = [ctypes.c_void_p, c_double, c_int]
     lib.qcx_batch_get_cid_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 7 + [P(c_double)] * 2
     lib.qcx_batch_set_md_heating.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double), c_double]
+    lib.qcx_batch_set_md_etemp.argtypes = [ctypes.c_void_p, c_double, c_double]
+    lib.qcx_batch_get_md_etemp.argtypes = [ctypes.c_void_p, P(c_double)]
     lib.qcx_batch_set_md_rules.argtypes = [ctypes.c_void_p, c_int, c_int, c_int]
     lib.qcx_batch_get_md_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 5 + [P(c_double)] * 3
     lib.qcx_read_xyz.argtypes = [ctypes.c_char_p, c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double)]
@@ -379,6 +381,16 @@ class Batch:
         vf = None if velof is None else np.ascontiguousarray(velof, dtype=np.float64)
         self._check(self._lib.qcx_batch_set_md_heating(self._h, _dp(eimp), _dp(tadd), _dp(vf), float(tstep)),
                     "set_md_heating")
+
+    def set_md_etemp(self, ax=0.0, ieetemp=0.0):
+        """Per-step electronic temperature of EI runs (setetemp after every step).
+        Call after set_md_heating and before the start's egrad."""
+        self._check(self._lib.qcx_batch_set_md_etemp(self._h, float(ax), float(ieetemp)), "set_md_etemp")
+
+    def md_etemp(self):
+        e = np.zeros(self.nmol)
+        self._check(self._lib.qcx_batch_get_md_etemp(self._h, _dp(e)), "md_etemp")
+        return e
 
     def set_cid_rules(self, tinit, ntot):
         """Stop rules of the collision MD (src/cid.f90:739-1052) on the device;

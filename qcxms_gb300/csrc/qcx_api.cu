@@ -118,6 +118,10 @@ struct qcx_batch {
   double* d_velof = nullptr;    // [natom] velocity scaling weights of the heating
   double* d_avxyz = nullptr;    // [natom][3] coordinate sums of the averaged structure
   bool md_heat = false;
+  std::vector<double> h_eimp;   // eimp of every trajectory (qcx_batch_set_md_heating)
+  // per-step electronic temperature (qcx_batch_set_md_etemp)
+  bool md_etemp = false;
+  double* d_etemp0 = nullptr;   // [nmol] the start's electronic temperature (K)
   bool md_on = false;
   // collision MD stop rules on the device (qcx_batch_set_cid_rules)
   CidState* d_cid = nullptr;
@@ -228,6 +232,7 @@ void free_batch(qcx_batch* b) {
   if (b->d_gpairs) cudaFree(b->d_gpairs);
   if (b->d_md) cudaFree(b->d_md);
   if (b->d_md_heat) cudaFree(b->d_md_heat);
+  if (b->d_etemp0) cudaFree(b->d_etemp0);
   if (b->d_avxyz) cudaFree(b->d_avxyz);
   if (b->d_cid) cudaFree(b->d_cid);
   if (b->d_velof) cudaFree(b->d_velof);
@@ -553,7 +558,9 @@ int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps)
   b->md_rules.nfragexit = nfragexit;
   b->md_rules.more = more;
   b->md_rules.max_steps = max_steps;
-  launch_md_begin(b->dev, b->d_md, b->md_heat ? b->d_md_heat : nullptr, b->d_avxyz, b->stream);
+  b->md_rules.etemp_on = b->md_etemp ? 1 : 0;
+  launch_md_begin(b->dev, b->d_md, b->md_heat ? b->d_md_heat : nullptr, b->d_avxyz,
+                  b->md_etemp ? b->d_etemp0 : nullptr, b->stream);
   if (check_launch()) return -1;
   CK(cudaStreamSynchronize(b->stream));
   if (!b->md_on || b->cid_on) drop_graph(b);
@@ -645,6 +652,43 @@ int qcx_batch_set_md_heating(qcx_batch* b, const double* eimp, const double* tad
   CK(cudaMemcpy(b->d_md_heat, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b->d_velof, vf.data(), sizeof(double) * vf.size(), cudaMemcpyHostToDevice));
   b->md_heat = true;
+  b->h_eimp.assign(eimp, eimp + b->nmol);
+  return 0;
+}
+
+int qcx_batch_set_md_etemp(qcx_batch* b, double ax, double ieetemp) {
+  if (!b || !std::isfinite(ax) || !std::isfinite(ieetemp)) {
+    set_error("qcx_batch_set_md_etemp: invalid arguments");
+    return -1;
+  }
+  // the start (src/md.f90:167-168): setetemp(nfrag = 1, eimp, etemp)
+  std::vector<double> et(b->nmol);
+  std::vector<MolDesc> md = b->mol;
+  for (int m = 0; m < b->nmol; ++m) {
+    const double eimp = b->md_heat ? b->h_eimp[m] : 0.0;
+    et[m] = setetemp(1, eimp, ax, ieetemp);
+    md[m].kT = et[m] * QCX_KTOAU;
+  }
+  if (!b->d_etemp0 && dalloc(&b->d_etemp0, (size_t)b->nmol)) return -1;
+  CK(cudaMemcpyAsync(b->d_etemp0, et.data(), sizeof(double) * b->nmol, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->d_mol, md.data(), sizeof(MolDesc) * b->nmol, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  b->md_rules.ax = ax;
+  b->md_rules.ieetemp = ieetemp;
+  b->md_etemp = true;
+  drop_graph(b);
+  return 0;
+}
+
+int qcx_batch_get_md_etemp(qcx_batch* b, double* etemp) {
+  if (!b || !b->d_md || !etemp) {
+    set_error("qcx_batch_get_md_etemp: no MD rules set up (qcx_batch_set_md_rules)");
+    return -1;
+  }
+  std::vector<MdState> st(b->nmol);
+  CK(cudaMemcpyAsync(st.data(), b->d_md, sizeof(MdState) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  for (int m = 0; m < b->nmol; ++m) etemp[m] = st[m].etemp;
   return 0;
 }
 
@@ -704,10 +748,14 @@ int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, cons
   if (!b) return -1;
   size_t n3 = sizeof(double) * 3 * b->natom;
   if (xyz) {
-    if (b->md_on || b->cid_on) {
-      // new coordinates start new runs: the MD or collision rules must be set up again
+    if (b->md_on || b->cid_on || b->md_etemp) {
+      // new coordinates start new runs: the MD or collision rules must be set up
+      // again, and the electronic temperatures return to the batch's
       b->md_on = false;
       b->cid_on = false;
+      if (b->md_etemp)
+        CK(cudaMemcpyAsync(b->d_mol, b->mol.data(), sizeof(MolDesc) * b->nmol, cudaMemcpyHostToDevice, b->stream));
+      b->md_etemp = false;
       drop_graph(b);
     }
     CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));

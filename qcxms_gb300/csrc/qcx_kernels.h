@@ -35,15 +35,30 @@ struct MdState {
   double tav, epav, ekav, edum, eerror, ttime, dtime;
   double eimp, fadd, ekinstart;  // heating of the first nadd steps (impactscale)
   double fragT[10];
+  double etemp;  // electronic temperature (K) of the next evaluation when the per-step etemp is on
 };
 struct MdRules {
   int nfragexit, more, max_steps;
   int max_nat;  // largest molecule (per-warp scratch of the heating)
   double tstep;
+  // per-step electronic temperature (setetemp, src/utility.f90:69-86, called by
+  // src/md.f90:443-446 after every step): on, ax and ieetemp of the input
+  int etemp_on;
+  double ax, ieetemp;
 };
+// setetemp (src/utility.f90:69-86): 5000 + 20000 ax, plus eimp * ieetemp while
+// eimp > 0 and the molecule is one fragment (5000. and 20000. are
+// default-real literals, exact in FP32)
+__host__ __device__ inline double setetemp(int nfrag, double eimp, double ax, double ieetemp) {
+  double etemp = 5000.0 + 20000.0 * ax;
+  if (eimp > 0.0 && nfrag <= 1) etemp = etemp + (eimp > 0.0 ? eimp : 0.0) * ieetemp;
+  return etemp;
+}
 // heat [nmol][3] = (eimp, fadd, nadd) or nullptr (no heating); velof [natom] or nullptr
 // avxyz [natom][3]: running sum of the coordinates over the current window of avdump = 50 steps
-void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double* avxyz, cudaStream_t stream);
+// etemp0 [nmol] (or nullptr): the electronic temperature of the start (set by qcx_batch_set_md_etemp)
+void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double* avxyz, const double* etemp0,
+                     cudaStream_t stream);
 void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,
                      double* avxyz, const MdRules& r, cudaStream_t stream);
 

@@ -15,9 +15,9 @@
 // needed per step. The arithmetic keeps the reference's operation order and
 // its single-precision literals (0.5*3*n, 0.1, float(nstep)) with explicit
 // roundings. The heating of the first nadd steps (impactscale, src/md.f90:439-441)
-// runs here too; the electronic temperature stays the batch's (setetemp with
-// ieetemp = 0, the default, gives the constant 5000 + 20000 ax). Not covered:
-// ieetemp != 0, the CID branch, averages for the output files.
+// runs here too, and, when switched on, the electronic temperature of every
+// next evaluation (setetemp, src/md.f90:443-446). Not covered: the CID branch,
+// averages for the output files.
 #include <cuda_runtime.h>
 
 #include "qcx_consts.h"
@@ -126,11 +126,12 @@ __device__ bool impact_scale(const DevBatch& bt, const MolDesc& md, const double
 
 // Start of the loop: Ekin of the current velocities (ekinet,
 // src/mdinit.f90:57-76), Epot of the last evaluation, then the first top.
-__global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat, double* avxyz) {
+__global__ void k_md_begin(DevBatch bt, MdState* st, const double* heat, double* avxyz, const double* etemp0) {
   const int mol = blockIdx.x * blockDim.x + threadIdx.x;
   if (mol >= bt.nmol) return;
   MdState s = {};
   s.nfrag = 1;
+  s.etemp = etemp0 ? etemp0[mol] : -1.0;
   s.kdump = kAvDump;
   if (heat) {
     s.eimp = heat[3 * mol];
@@ -196,6 +197,16 @@ __global__ void __launch_bounds__(32 * kRulesWarps) k_md_rules(DevBatch bt, MdSt
       return;
     }
   }
+  // electronic temperature of the next evaluation (src/md.f90:443-446), with
+  // the previous step's fragment count: dum = eimp - eimp*float(nstep)/float(nadd),
+  // evaluated left to right in double (float(n) converts exactly);
+  // kT = etemp * ktoau (src/tblite.f90:133)
+  if (r.etemp_on) {
+    const double a = __dmul_rn(s.eimp, (double)(float)s.nstep);
+    const double dum = __dsub_rn(s.eimp, __ddiv_rn(a, (double)(float)s.nadd));
+    s.etemp = setetemp(s.nfrag, dum, r.ax, r.ieetemp);
+    if (lane == 0) const_cast<MolDesc*>(bt.mol)[mol].kT = __dmul_rn(s.etemp, QCX_KTOAU);
+  }
   const int nf = nfrag[mol];
   s.nfrag = nf;
   if (nf > 1) {
@@ -255,8 +266,9 @@ __global__ void __launch_bounds__(32 * kRulesWarps) k_md_rules(DevBatch bt, MdSt
   }
 }
 
-void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double* avxyz, cudaStream_t stream) {
-  k_md_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, heat, avxyz);
+void launch_md_begin(const DevBatch& bt, MdState* st, const double* heat, double* avxyz, const double* etemp0,
+                     cudaStream_t stream) {
+  k_md_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, heat, avxyz, etemp0);
 }
 
 void launch_md_rules(const DevBatch& bt, MdState* st, const int* frag, const int* nfrag, const double* velof,

@@ -226,3 +226,83 @@ def test_gpu_md_heating_match_oracle(gpu, oracle_lib):
             assert np.array_equal(np.array(vpre), r["vel"][sl]), (step, i)
             heated += scaled
     assert heated >= 8 * 8
+
+
+def test_oracle_setetemp_known_answers(oracle_lib):
+    o = oracle_lib
+    assert o.setetemp(1, 0.2, 0.0, 0.0) == 5000.0
+    assert o.setetemp(1, 0.2, 0.05, 20000.0) == 5000.0 + 1000.0 + 0.2 * 20000.0
+    assert o.setetemp(2, 0.2, 0.05, 20000.0) == 6000.0  # fragmented: no IEE term
+    assert o.setetemp(1, -0.1, 0.05, 20000.0) == 6000.0
+    # along the heating: dum = eimp - eimp*nstep/nadd falls to 0 at nstep = nadd
+    v = [[0.02, 0.0, 0.0]]
+    s = o.md_rules_begin(v, [1837.0], -1.0, heat=(0.3, 0.05, 10), etemp=(0.0, 10000.0))
+    assert s["etemp"] == 5000.0 + 0.3 * 10000.0
+    temps = []
+    for k in range(12):
+        o.md_rules_step(s, -1.0, o._ekinet(v, [1837.0]), v, [1837.0], [1], 1, DT, 3, 250, 1000, etemp=(0.0, 10000.0))
+        assert not s["done"]
+        temps.append(s["etemp"])
+    assert temps[0] == 5000.0 + (0.3 - 0.3 * 1.0 / 10.0) * 10000.0
+    assert temps[9] == 5000.0 and temps[11] == 5000.0  # nstep >= nadd: dum <= 0
+
+
+@pytest.mark.gpu
+def test_gpu_md_etemp_match_oracle(gpu, oracle_lib):
+    """Per-step electronic temperature (setetemp after every step): the device
+    value equals the oracle's bit for bit after every step, and every
+    evaluation runs at the temperature set after the previous step (energies
+    against the oracle at that kT)."""
+    o = oracle_lib
+    mols = []
+    for k in range(4):
+        Z, xyz = molgen.random_chno(6 + 2 * k, 800 + k)
+        Z = np.asarray(Z)
+        mols.append({"Z": Z, "xyz": np.asarray(xyz, dtype=np.float64).reshape(-1, 3),
+                     "vel": molgen.maxwell_boltzmann(Z, 500.0, 800 + k), "mass": molgen.masses(Z), "charge": 1})
+    b = qg.Batch(mols)
+    eimp = np.array([0.1, 0.2, 0.25, 0.3])
+    tadd = np.array([6 * DT, 8 * DT, 10 * DT, 12 * DT])
+    ax, ieet = 0.05, 20000.0
+    b.set_md_heating(eimp, tadd, DT)
+    b.set_md_etemp(ax, ieet)
+    b.egrad()
+    r = b.get()
+    off = np.concatenate([[0], np.cumsum([len(m["Z"]) for m in mols])])
+    # the start's evaluation ran at setetemp(1, eimp)
+    for i, m in enumerate(mols):
+        sl = slice(off[i], off[i + 1])
+        et0 = o.setetemp(1, eimp[i], ax, ieet)
+        rc, e, g, q, info = o.egrad(m["Z"], r["xyz"][sl], 1, kT=et0 * constants.KB_AU)
+        assert rc == 0 and abs(r["energy"][i] - e) < 1e-7, i
+    nfragexit, more, max_steps = 3, 20, 14
+    b.set_md_rules(nfragexit, more, max_steps)
+    fail = qg.STATUS_SCC_NOT_CONVERGED | qg.STATUS_NON_FINITE | qg.STATUS_CHOLESKY_FAILED
+    ref = [o.md_rules_begin(r["vel"][off[i]:off[i + 1]], list(m["mass"]),
+                            0.0 if r["status"][i] & fail else r["energy"][i], o.md_heating(eimp[i], tadd[i], DT),
+                            etemp=(ax, ieet)) for i, m in enumerate(mols)]
+    et = b.md_etemp()
+    assert all(et[i] == ref[i]["etemp"] for i in range(len(mols)))
+    for step in range(max_steps):
+        if all(s["done"] for s in ref):
+            break
+        prev, et_prev = r, b.md_etemp()
+        b.step(1, DT)
+        r = b.get()
+        frag, nf = b.fragments(3.0, 1, 0)
+        for i, m in enumerate(mols):
+            if ref[i]["done"]:
+                continue
+            sl = slice(off[i], off[i + 1])
+            if step in (0, 5) and not r["status"][i] & fail:
+                rc, e, g, q, info = o.egrad(m["Z"], r["xyz"][sl], 1, kT=et_prev[i] * constants.KB_AU)
+                assert rc != 0 or abs(r["energy"][i] - e) < 1e-7, (step, i)
+            _, vpre, _ = o.leapfrog(prev["grad"][sl], m["mass"], DT, prev["xyz"][sl], prev["vel"][sl])
+            vpre = [list(x) for x in vpre]
+            e = 0.0 if r["status"][i] & fail else r["energy"][i]
+            o.md_rules_step(ref[i], e, r["ekin"][i], vpre, list(m["mass"]), list(frag[sl]), int(nf[i]), DT,
+                            nfragexit, more, max_steps, etemp=(ax, ieet))
+        et = b.md_etemp()
+        for i in range(len(mols)):
+            if not ref[i]["done"]:
+                assert et[i] == ref[i]["etemp"], (step, i, et[i], ref[i]["etemp"])
