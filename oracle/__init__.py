@@ -19,7 +19,8 @@ def build(force=False):
     src = os.path.join(HERE, "qcx_oracle.c")
     deps = [src, os.path.join(HERE, "qcx_oracle.h"),
             os.path.join(HERE, "..", "qcxms_gb300", "csrc", "qcx_params.h"),
-            os.path.join(HERE, "..", "qcxms_gb300", "csrc", "qcx_consts.h")]
+            os.path.join(HERE, "..", "qcxms_gb300", "csrc", "qcx_consts.h"),
+            os.path.join(HERE, "..", "qcxms_gb300", "csrc", "qcx_d4ref.h")]
     if not force and os.path.exists(LIB_PATH) and \
             os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(d) for d in deps):
         return LIB_PATH
@@ -62,6 +63,7 @@ def lib():
         _lib.qcxo_md_batch.restype = ctypes.c_int
         _lib.qcxo_egrad_batch.restype = ctypes.c_int
         _lib.qcxo_eself.restype = ctypes.c_double
+        _lib.qcxo_d4_c6ref.restype = ctypes.c_double
         _lib.qcxo_nel.restype = ctypes.c_int
     return _lib
 
@@ -484,6 +486,21 @@ def cid_rules_step(s, failed, xyz, vel, mass, nfrag, tstep, tinit):
     if s["nstep"] >= s["total_steps"]:
         s["done"] = 1
     return s
+
+
+def d4_c6ref(za, i, zb, j):
+    """C6 of D4 reference pair (za, i; zb, j), 0-based reference indices."""
+    return lib().qcxo_d4_c6ref(int(za), int(i), int(zb), int(j))
+
+
+def d4_c6(Z, xyz, q=None):
+    """Molecular D4 C6 [nat][nat] at the covalent CNs and charges q (zero if None)."""
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(len(Z), 3)
+    c6 = np.zeros((len(Z), len(Z)))
+    qq = None if q is None else np.ascontiguousarray(q, dtype=np.float64)
+    lib().qcxo_d4_c6(len(Z), _p(Z, ctypes.c_int), _p(xyz), None if qq is None else _p(qq), _p(c6))
+    return c6
 
 
 def gnorm(grad):

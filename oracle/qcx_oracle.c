@@ -21,6 +21,7 @@
 
 #include "../qcxms_gb300/csrc/qcx_consts.h"
 #include "../qcxms_gb300/csrc/qcx_params.h"
+#include "../qcxms_gb300/csrc/qcx_d4ref.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -112,23 +113,38 @@ static void cn_exp_pair(double r, double rc, double* f, double* df) {
   *df = -(*f) * (*f) * e * QCX_KCN * rc / (r * r);
 }
 
-/* erf counting function (dispersion reference weights) */
-static void cn_erf_pair(double r, double rc, double* f, double* df) {
-  double t = QCX_KERF * (r / rc - 1.0);
-  *f = 0.5 * erfc(t);
-  *df = -QCX_KERF / (rc * sqrt(QCX_PI)) * exp(-t * t);
+/* Covalent coordination number of the D4 model, covncoord / gcovncoord
+ * (src/dftd4.f90:292-325, 1033-1068): pairs within r^2 <= 1600 Bohr^2 add
+ * den / (1 + exp(-k1 (rcov_ij / r - 1))) with den = k4 exp(-(|EN_i - EN_j| + k5)^2 / k6),
+ * k1 = 16, k4 = 4.10451, k5 = 19.08857, k6 = 2 * 11.28174^2 (src/dftd4.f90:10-19),
+ * the D3 covalent radii and Pauling electronegativities of src/dftd4.f90.
+ * *df = d(contribution)/dr. */
+#define D4_K1 16.0
+#define D4_K4 4.10451
+#define D4_K5 19.08857
+#define D4_K6 (2 * 11.28174 * 11.28174)
+#define D4_CN_THR 1600.0
+static void d4_cn_pair(int za, int zb, double r2, double* f, double* df) {
+  *f = 0.0; *df = 0.0;
+  if (r2 > D4_CN_THR) return;
+  double r = sqrt(r2);
+  double den = D4_K4 * exp(-pow(fabs(qcx_d4_en[za] - qcx_d4_en[zb]) + D4_K5, 2) / D4_K6);
+  double rco = qcx_d4_rcov[za] + qcx_d4_rcov[zb];
+  double ex = exp(-D4_K1 * (rco / r - 1.0));
+  *f = den / (1.0 + ex);
+  *df = (-D4_K1 * rco * ex * den) / (r2 * ((1.0 + ex) * (1.0 + ex)));
 }
 
 static void compute_cn(const mol_t* m, double* cn, double* cnd) {
   for (int a = 0; a < m->nat; ++a) { cn[a] = 0.0; cnd[a] = 0.0; }
   for (int a = 0; a < m->nat; ++a)
     for (int b = 0; b < a; ++b) {
-      double d[3], r = 0;
-      for (int k = 0; k < 3; ++k) { d[k] = m->xyz[3 * a + k] - m->xyz[3 * b + k]; r += d[k] * d[k]; }
-      r = sqrt(r);
+      double d[3], r2 = 0;
+      for (int k = 0; k < 3; ++k) { d[k] = m->xyz[3 * a + k] - m->xyz[3 * b + k]; r2 += d[k] * d[k]; }
+      double r = sqrt(r2);
       double rc = qcx_rcov[m->Z[a]] + qcx_rcov[m->Z[b]], f, df;
       cn_exp_pair(r, rc, &f, &df); cn[a] += f; cn[b] += f;
-      cn_erf_pair(r, rc, &f, &df); cnd[a] += f; cnd[b] += f;
+      d4_cn_pair(m->Z[a], m->Z[b], r2, &f, &df); cnd[a] += f; cnd[b] += f;
     }
 }
 
@@ -536,13 +552,14 @@ typedef struct {
   double* gam;      /* [nsh][nsh] */
   double* mrad;     /* [nat] multipole radius */
   double* dmrad;    /* [nat] d mrad / d CN */
-  double* c6;       /* [nat][nat] C6 at zero charge (CN weighted) */
-  double* zeta;     /* [nat] charge scaling at the current charges */
-  double* dzeta;    /* [nat] */
+  double* c6;       /* [nat][nat] C6 at zero charge (CN weighted): the three-body term's */
   double* gdisp;    /* [nat][nat] BJ-damped kernel g_AB(R) */
   double* dgdisp;   /* [nat][nat] dg/dR */
-  double* w;        /* [nat][MAXREF] reference weights */
-  double* dw;       /* [nat][MAXREF] d w / d CN' */
+  double* gw;       /* [nat][D4_MAXREF] reference weights at the covalent CN */
+  double* dgw;      /* [nat][D4_MAXREF] d gw / d CN */
+  double* z0;       /* [nat][D4_MAXREF] charge scaling of the references at zero charge */
+  double* zq;       /* [nat][D4_MAXREF] charge scaling at the current atomic charges */
+  double* dzq;      /* [nat][D4_MAXREF] d zq / d q */
 } es_t;
 
 static void es_alloc(es_t* e, int nat, int nsh) {
@@ -550,52 +567,172 @@ static void es_alloc(es_t* e, int nat, int nsh) {
   e->gam = calloc((size_t)nsh * nsh, sizeof(double));
   e->mrad = calloc(nat, sizeof(double)); e->dmrad = calloc(nat, sizeof(double));
   e->c6 = calloc((size_t)nat * nat, sizeof(double));
-  e->zeta = calloc(nat, sizeof(double)); e->dzeta = calloc(nat, sizeof(double));
   e->gdisp = calloc((size_t)nat * nat, sizeof(double)); e->dgdisp = calloc((size_t)nat * nat, sizeof(double));
-  e->w = calloc((size_t)nat * QCX_MAXREF, sizeof(double)); e->dw = calloc((size_t)nat * QCX_MAXREF, sizeof(double));
+  size_t nr = (size_t)nat * QCX_D4_MAXREF;
+  e->gw = calloc(nr, sizeof(double)); e->dgw = calloc(nr, sizeof(double)); e->z0 = calloc(nr, sizeof(double));
+  e->zq = calloc(nr, sizeof(double)); e->dzq = calloc(nr, sizeof(double));
 }
 static void es_free(es_t* e) {
-  free(e->gam); free(e->mrad); free(e->dmrad); free(e->c6); free(e->zeta); free(e->dzeta);
-  free(e->gdisp); free(e->dgdisp); free(e->w); free(e->dw);
+  free(e->gam); free(e->mrad); free(e->dmrad); free(e->c6);
+  free(e->gdisp); free(e->dgdisp); free(e->gw); free(e->dgw); free(e->z0); free(e->zq); free(e->dzq);
 }
 
-static double c6ref(int za, int i, int zb, int j) {
-  double aa = qcx_d4_alpha0[za][i], ab = qcx_d4_alpha0[zb][j];
-  double wa = qcx_d4_omega[za][i], wb = qcx_d4_omega[zb][j];
-  return 1.5 * aa * ab * wa * wb / (wa + wb);
+/* ------------------------------------------------------------------------ */
+/* D4 dispersion model of QCxMS's src/dftd4.f90 with its reference data      */
+/* (include/param_d4.fh, converted to qcx_d4ref.h)                            */
+/* ------------------------------------------------------------------------ */
+/* zeta / dzeta (src/dftd4.f90:423-450): charge scaling of a reference */
+static double d4_zeta_fn(double a, double c, double qref, double qmod) {
+  if (qmod < 0.0) return exp(a);
+  return exp(a * (1.0 - exp(c * (1.0 - qref / qmod))));
+}
+static double d4_dzeta_fn(double a, double c, double qref, double qmod) {
+  if (qmod < 0.0) return 0.0;
+  return -a * c * exp(c * (1.0 - qref / qmod)) * d4_zeta_fn(a, c, qref, qmod) * qref / (qmod * qmod);
 }
 
-static void d4_weights(int z, double cn, double* w, double* dw) {
-  int nr = qcx_d4_nref[z];
-  double ex[QCX_MAXREF], mx = -1e300;
-  for (int i = 0; i < nr; ++i) {
-    double t = cn - qcx_d4_cnref[z][i];
-    ex[i] = -QCX_D4_WF * t * t;
-    if (ex[i] > mx) mx = ex[i];
+/* trapzd (src/dftd4.f90:452-497): Casimir-Polder integral over the 23
+ * imaginary frequencies, the mean of the two staggered trapezoid sums */
+static double d4_trapzd(const double* pol) {
+  static const double freq[23] = {0.000001, 0.050000, 0.100000, 0.200000, 0.300000, 0.400000, 0.500000, 0.600000,
+                                  0.700000, 0.800000, 0.900000, 1.000000, 1.200000, 1.400000, 1.600000, 1.800000,
+                                  2.000000, 2.500000, 3.000000, 4.000000, 5.000000, 7.500000, 10.00000};
+  double t1 = 0.0, t2 = 0.0;
+  for (int k = 0; k < 22; k += 2) t1 = t1 + (freq[k + 1] - freq[k]) * (pol[k + 1] + pol[k]);
+  for (int k = 1; k < 22; k += 2) t2 = t2 + (freq[k + 1] - freq[k]) * (pol[k + 1] + pol[k]);
+  return 0.5 * t1 + 0.5 * t2;
+}
+
+static int d4_refc[QCX_MAXZ + 1][QCX_D4_MAXREF];                       /* Gaussians per reference */
+static double d4_refal[QCX_MAXZ + 1][QCX_D4_MAXREF][QCX_D4_NFREQ];     /* reference alpha(i omega) */
+static double d4_c6r[QCX_MAXZ + 1][QCX_MAXZ + 1][QCX_D4_MAXREF][QCX_D4_MAXREF];
+
+/* d4dim (src/dftd4.f90:531-595): polarisabilities of the references with the
+ * hydrogen (secondary system) contributions removed, and the number of
+ * Gaussians of each reference; then C6 of every reference pair,
+ * 3/pi * trapzd(alpha_i alpha_j) (src/dftd4.f90:665). Filled at load. */
+__attribute__((constructor)) static void d4_tables(void) {
+  const double thopi = 3.0 / 3.141592653589793238462643383279502884197;
+  for (int z = 1; z <= QCX_MAXZ; ++z) {
+    int cncount[16] = {0};
+    cncount[0] = 1;
+    for (int j = 0; j < qcx_d4_refn[z]; ++j) {
+      int is = qcx_d4_refsys[z][j];
+      double iz = (double)qcx_d4_zeff[is];
+      double zs = d4_zeta_fn(QCX_D4_GA, qcx_d4_gam[is] * QCX_D4_GC, qcx_d4_secq[is] + iz, qcx_d4_refh[z][j] + iz);
+      for (int k = 0; k < QCX_D4_NFREQ; ++k) {
+        double sec_al = qcx_d4_sscale[is] * qcx_d4_secaiw[is][k] * zs;
+        double v = qcx_d4_ascale[z][j] * (qcx_d4_alphaiw[z][j][k] - qcx_d4_hcount[z][j] * sec_al);
+        d4_refal[z][j][k] = v > 0.0 ? v : 0.0;
+      }
+      cncount[(int)lround(qcx_d4_refcn[z][j])] += 1;
+    }
+    for (int j = 0; j < qcx_d4_refn[z]; ++j) {
+      int icn = cncount[(int)lround(qcx_d4_refcn[z][j])];
+      d4_refc[z][j] = icn * (icn + 1) / 2;
+    }
   }
-  double sum = 0.0, dsum = 0.0;
-  double g[QCX_MAXREF], dg[QCX_MAXREF];
+  for (int za = 1; za <= QCX_MAXZ; ++za)
+    for (int zb = 1; zb <= QCX_MAXZ; ++zb)
+      for (int i = 0; i < qcx_d4_refn[za]; ++i)
+        for (int j = 0; j < qcx_d4_refn[zb]; ++j) {
+          double pol[QCX_D4_NFREQ];
+          for (int k = 0; k < QCX_D4_NFREQ; ++k) pol[k] = d4_refal[za][i][k] * d4_refal[zb][j][k];
+          d4_c6r[za][zb][i][j] = thopi * d4_trapzd(pol);
+        }
+}
+
+/* Reference weights of one atom at covalent CN cn (src/dftd4.f90:1150-1193):
+ * gw_i = sum_{k<=refc_i} exp(-k wf (cn - cn_i)^2) / norm, and d gw / d cn;
+ * a weight that overflows to NaN becomes 1 for the reference with the largest
+ * CN and 0 otherwise (its derivative 0). */
+static void d4_weights(int z, double cn, double* gw, double* dgw) {
+  int nr = qcx_d4_refn[z];
+  double norm = 0.0, dnorm = 0.0, maxcn = -1e300;
   for (int i = 0; i < nr; ++i) {
-    g[i] = exp(ex[i] - mx);
-    dg[i] = -2.0 * QCX_D4_WF * (cn - qcx_d4_cnref[z][i]) * g[i];
-    sum += g[i]; dsum += dg[i];
+    if (qcx_d4_refcovcn[z][i] > maxcn) maxcn = qcx_d4_refcovcn[z][i];
+    for (int k = 1; k <= d4_refc[z][i]; ++k) {
+      double twf = k * QCX_D4_WF, d = cn - qcx_d4_refcovcn[z][i];
+      double tgw = exp(-twf * d * d);
+      norm = norm + tgw;
+      dnorm = dnorm + 2 * twf * (qcx_d4_refcovcn[z][i] - cn) * tgw;
+    }
   }
-  for (int i = 0; i < QCX_MAXREF; ++i) { w[i] = 0.0; dw[i] = 0.0; }
+  norm = 1.0 / norm;
+  for (int i = 0; i < QCX_D4_MAXREF; ++i) { gw[i] = 0.0; dgw[i] = 0.0; }
   for (int i = 0; i < nr; ++i) {
-    w[i] = g[i] / sum;
-    dw[i] = (dg[i] * sum - g[i] * dsum) / (sum * sum);
+    double expw = 0.0, dexpw = 0.0;
+    for (int k = 1; k <= d4_refc[z][i]; ++k) {
+      double twf = QCX_D4_WF * k, d = cn - qcx_d4_refcovcn[z][i];
+      double tgw = exp(-twf * d * d);
+      expw = expw + tgw;
+      dexpw = dexpw + 2 * twf * (qcx_d4_refcovcn[z][i] - cn) * tgw;
+    }
+    gw[i] = expw * norm;
+    if (gw[i] != gw[i]) gw[i] = qcx_d4_refcovcn[z][i] == maxcn ? 1.0 : 0.0;
+    dgw[i] = dexpw * norm - expw * dnorm * norm * norm;
+    if (dgw[i] != dgw[i]) dgw[i] = 0.0;
   }
 }
 
-static void d4_zeta(int z, double q, double* zeta, double* dzeta) {
-  double t = QCX_D4_GC * qcx_d4_eta[z] / (double)z;
-  double ex = exp(t * q);
-  *zeta = exp(QCX_D4_GA * (1.0 - ex));
-  *dzeta = *zeta * (-QCX_D4_GA * ex * t);
+/* charge scaling of atom z's references at atomic charge q: zeta(g_a, gam*g_c,
+ * refq_i + zeff, q + zeff) and its q derivative (src/dftd4.f90:1181-1190) */
+static void d4_zeta_atom(int z, double q, double* zt, double* dzt) {
+  double iz = (double)qcx_d4_zeff[z], c = qcx_d4_gam[z] * QCX_D4_GC;
+  for (int i = 0; i < QCX_D4_MAXREF; ++i) {
+    zt[i] = 0.0;
+    if (dzt) dzt[i] = 0.0;
+  }
+  for (int i = 0; i < qcx_d4_refn[z]; ++i) {
+    zt[i] = d4_zeta_fn(QCX_D4_GA, c, qcx_d4_refq[z][i] + iz, q + iz);
+    if (dzt) dzt[i] = d4_dzeta_fn(QCX_D4_GA, c, qcx_d4_refq[z][i] + iz, q + iz);
+  }
 }
 
+/* sum_ij (wa_i) (wb_j) C6(za, i, zb, j) */
+static double d4_c6(int za, const double* wa, int zb, const double* wb) {
+  double s = 0.0;
+  for (int i = 0; i < qcx_d4_refn[za]; ++i)
+    for (int j = 0; j < qcx_d4_refn[zb]; ++j) s += wa[i] * wb[j] * d4_c6r[za][zb][i][j];
+  return s;
+}
+
+/* C6 of one reference pair (exported for the data tests) */
+double qcxo_d4_c6ref(int za, int i, int zb, int j) {
+  if (za < 1 || za > QCX_MAXZ || zb < 1 || zb > QCX_MAXZ || i < 0 || j < 0 || i >= qcx_d4_refn[za] ||
+      j >= qcx_d4_refn[zb])
+    return -1.0;
+  return d4_c6r[za][zb][i][j];
+}
+
+/* molecular C6 of every atom pair at covalent CNs and charges q (zero charges
+ * if q == NULL), c6 [nat][nat]; exported for the data tests */
+void qcxo_d4_c6(int nat, const int* Z, const double* xyz, const double* q, double* c6) {
+  double* w = calloc((size_t)nat * QCX_D4_MAXREF, sizeof(double));
+  double gw[QCX_D4_MAXREF], dgw[QCX_D4_MAXREF], zt[QCX_D4_MAXREF];
+  for (int a = 0; a < nat; ++a) {
+    double cn = 0.0;
+    for (int b = 0; b < nat; ++b) {
+      if (b == a) continue;
+      double r2 = 0.0, f, df;
+      for (int k = 0; k < 3; ++k) { double d = xyz[3 * b + k] - xyz[3 * a + k]; r2 += d * d; }
+      d4_cn_pair(Z[a], Z[b], r2, &f, &df);
+      cn += f;
+    }
+    d4_weights(Z[a], cn, gw, dgw);
+    d4_zeta_atom(Z[a], q ? q[a] : 0.0, zt, NULL);
+    for (int i = 0; i < QCX_D4_MAXREF; ++i) w[a * QCX_D4_MAXREF + i] = gw[i] * zt[i];
+  }
+  for (int a = 0; a < nat; ++a)
+    for (int b = 0; b < nat; ++b)
+      c6[a * nat + b] = a == b ? 0.0 : d4_c6(Z[a], w + a * QCX_D4_MAXREF, Z[b], w + b * QCX_D4_MAXREF);
+  free(w);
+}
+
+/* Becke-Johnson kernel of a pair (src/dftd4.f90:386-409, 1250-1258):
+ * g = s6 / (r^6 + R0^6) + s8 * 3 r4r2_a r4r2_b / (r^8 + R0^8), R0 = a1 sqrt(3 r4r2_a r4r2_b) + a2 */
 static void bj_kernel(int za, int zb, double r, double* g, double* dg) {
-  double qq = 3.0 * qcx_r4r2[za] * qcx_r4r2[zb];
+  double qq = 3.0 * qcx_d4_r4r2[za] * qcx_d4_r4r2[zb];
   double r0 = QCX_D4_A1 * sqrt(qq) + QCX_D4_A2;
   double r2 = r * r, r6 = r2 * r2 * r2, r8 = r6 * r2;
   double r06 = pow(r0, 6), r08 = r06 * r0 * r0;
@@ -605,7 +742,7 @@ static void bj_kernel(int za, int zb, double r, double* g, double* dg) {
 }
 
 static double bj_radius(int za, int zb) {
-  return QCX_D4_A1 * sqrt(3.0 * qcx_r4r2[za] * qcx_r4r2[zb]) + QCX_D4_A2;
+  return QCX_D4_A1 * sqrt(3.0 * qcx_d4_r4r2[za] * qcx_d4_r4r2[zb]) + QCX_D4_A2;
 }
 
 static void mpole_radius(int z, double cn, double* r, double* dr) {
@@ -638,24 +775,26 @@ static void es_setup(const mol_t* m, const double* cn, const double* cnd, es_t* 
       for (int k = 0; k < 3; ++k) { double d = m->xyz[3 * A + k] - m->xyz[3 * B + k]; r2 += d * d; }
       e->gam[s * nsh + t] = 1.0 / sqrt(r2 + 1.0 / (eta * eta));
     }
+  double w0[QCX_D4_MAXREF * 2];
+  double* wz = calloc((size_t)nat * QCX_D4_MAXREF, sizeof(double)); /* gw * z0 */
   for (int a = 0; a < nat; ++a) {
     mpole_radius(m->Z[a], cn[a], &e->mrad[a], &e->dmrad[a]);
-    d4_weights(m->Z[a], cnd[a], &e->w[a * QCX_MAXREF], &e->dw[a * QCX_MAXREF]);
+    d4_weights(m->Z[a], cnd[a], &e->gw[a * QCX_D4_MAXREF], &e->dgw[a * QCX_D4_MAXREF]);
+    d4_zeta_atom(m->Z[a], 0.0, &e->z0[a * QCX_D4_MAXREF], w0);
+    for (int i = 0; i < QCX_D4_MAXREF; ++i)
+      wz[a * QCX_D4_MAXREF + i] = e->gw[a * QCX_D4_MAXREF + i] * e->z0[a * QCX_D4_MAXREF + i];
   }
   for (int a = 0; a < nat; ++a)
     for (int b = 0; b < nat; ++b) {
       int za = m->Z[a], zb = m->Z[b];
-      double c6 = 0.0;
-      for (int i = 0; i < qcx_d4_nref[za]; ++i)
-        for (int j = 0; j < qcx_d4_nref[zb]; ++j)
-          c6 += e->w[a * QCX_MAXREF + i] * e->w[b * QCX_MAXREF + j] * c6ref(za, i, zb, j);
-      e->c6[a * nat + b] = c6;
+      e->c6[a * nat + b] = d4_c6(za, wz + a * QCX_D4_MAXREF, zb, wz + b * QCX_D4_MAXREF);
       if (a != b) {
         double r2 = 0;
         for (int k = 0; k < 3; ++k) { double d = m->xyz[3 * a + k] - m->xyz[3 * b + k]; r2 += d * d; }
         bj_kernel(za, zb, sqrt(r2), &e->gdisp[a * nat + b], &e->dgdisp[a * nat + b]);
       }
     }
+  free(wz);
 }
 
 /* moment vector layout: [qsh (nsh) | dipm (3 nat) | qp (6 nat)] */
@@ -722,17 +861,31 @@ static void es_potential(const mol_t* m, es_t* e, const double* x, double* vsh, 
     for (int q = 0; q < 3; ++q) vqp[6 * a + q] += 2.0 * fq * ta[q];
     for (int q = 3; q < 6; ++q) vqp[6 * a + q] += 4.0 * fq * ta[q];
   }
-  /* self-consistent dispersion: E = -sum_{A<B} zeta_A zeta_B C6_AB g_AB */
-  for (int a = 0; a < nat; ++a) d4_zeta(m->Z[a], qat[a], &e->zeta[a], &e->dzeta[a]);
-  for (int a = 0; a < nat; ++a) {
-    double s = 0.0;
-    for (int b = 0; b < nat; ++b) {
-      if (b == a) continue;
-      double t = e->c6[a * nat + b] * e->gdisp[a * nat + b];
-      s += e->zeta[b] * t;
-      if (b < a) edisp -= e->zeta[a] * e->zeta[b] * t;
+  /* self-consistent dispersion (edisp / disppot, src/dftd4.f90:807-1034):
+   * E = -sum_{A<B} g_AB sum_ij (gw zeta(q_A))_i (gw zeta(q_B))_j C6_ij, and its
+   * derivative with respect to the atomic charges as potential */
+  {
+    const int R = QCX_D4_MAXREF;
+    double* wq = calloc((size_t)nat * R, sizeof(double));
+    double* dwq = calloc((size_t)nat * R, sizeof(double));
+    for (int a = 0; a < nat; ++a) {
+      d4_zeta_atom(m->Z[a], qat[a], &e->zq[a * R], &e->dzq[a * R]);
+      for (int i = 0; i < R; ++i) {
+        wq[a * R + i] = e->gw[a * R + i] * e->zq[a * R + i];
+        dwq[a * R + i] = e->gw[a * R + i] * e->dzq[a * R + i];
+      }
     }
-    vat[a] += -e->dzeta[a] * s;
+    for (int a = 0; a < nat; ++a) {
+      double v = 0.0;
+      for (int b = 0; b < nat; ++b) {
+        if (b == a) continue;
+        double g = e->gdisp[a * nat + b];
+        v -= g * d4_c6(m->Z[a], dwq + a * R, m->Z[b], wq + b * R);
+        if (b < a) edisp -= g * d4_c6(m->Z[a], wq + a * R, m->Z[b], wq + b * R);
+      }
+      vat[a] += v;
+    }
+    free(wq); free(dwq);
   }
   for (int s = 0; s < nsh; ++s) vsh[s] += vat[m->sh_atom[s]];
   en->e_ies = eies; en->e_3 = e3; en->e_aes = eaes; en->e_axc = eaxc; en->e_disp = edisp;
@@ -759,7 +912,10 @@ static double rep_energy_grad(const mol_t* m, double* grad) {
   return e;
 }
 
-/* Axilrod-Teller-Muto three-body term with zero-charge C6 (CN dependent).
+/* Axilrod-Teller-Muto three-body term with zero-charge C6 (CN dependent),
+ * as apprabc / dabcappr (src/dftd4.f90:1339-1400, 1610-1780) with the zero-charge
+ * weights of dispgrad (src/dftd4.f90:1181-1190): C9 = s9 sqrt(C6_ab C6_bc C6_ca),
+ * damping 1 / (1 + 6 ((R0_ab R0_bc R0_ca / (r_ab r_bc r_ca))^(1/3))^alp).
  * Adds dE/dCN' to dedcnd when grad != NULL. */
 static double atm_energy_grad(const mol_t* m, const es_t* e, double* grad, double* dedcnd) {
   int nat = m->nat;
@@ -781,7 +937,7 @@ static double atm_energy_grad(const mol_t* m, const es_t* e, double* grad, doubl
         double rab_ = sqrt(ab2), rbc_ = sqrt(bc2), rca_ = sqrt(ca2);
         double rrr = rab_ * rbc_ * rca_;
         double rbar = cbrt(rrr);
-        double t = 6.0 * pow(r0 / rbar, QCX_ATM_ALP / 3.0);
+        double t = 6.0 * pow(r0 / rbar, QCX_ATM_ALP);
         double fd = 1.0 / (1.0 + t);
         /* angular factor in distances: 3 cos a cos b cos c + 1 */
         double num = (ab2 + ca2 - bc2) * (ab2 + bc2 - ca2) * (bc2 + ca2 - ab2);
@@ -801,7 +957,7 @@ static double atm_energy_grad(const mol_t* m, const es_t* e, double* grad, doubl
           double dang_dy = 3.0 * (dnum_dy / den - num / (den * y));
           double dang_dz = 3.0 * (dnum_dz / den - num / (den * z));
           /* radial part h = fd / rrr^3 with rrr^2 = x y z; d/dx of ln(rrr) = 1/(2x) */
-          double alp3 = QCX_ATM_ALP / 3.0;
+          double alp3 = QCX_ATM_ALP;
           /* d fd / d ln(rbar) = fd^2 * t * alp3 ; d ln rbar / d x = 1/(6x) */
           double dlnh_dlnr = (fd * t * alp3) - 9.0; /* d ln(h)/d ln(rbar) */
           double dh_dx = fd / r3 * dlnh_dlnr / (6.0 * x);
@@ -828,10 +984,13 @@ static double atm_energy_grad(const mol_t* m, const es_t* e, double* grad, doubl
               if (jj == ii) continue;
               int o = atoms[jj], zo = m->Z[o];
               double c6po = e->c6[p * nat + o];
-              double dc6 = 0.0;
-              for (int i = 0; i < qcx_d4_nref[zp]; ++i)
-                for (int j = 0; j < qcx_d4_nref[zo]; ++j)
-                  dc6 += e->dw[p * QCX_MAXREF + i] * e->w[o * QCX_MAXREF + j] * c6ref(zp, i, zo, j);
+              const int R = QCX_D4_MAXREF;
+              double wp[QCX_D4_MAXREF], wo[QCX_D4_MAXREF];
+              for (int i = 0; i < R; ++i) {
+                wp[i] = e->dgw[p * R + i] * e->z0[p * R + i];
+                wo[i] = e->gw[o * R + i] * e->z0[o * R + i];
+              }
+              double dc6 = d4_c6(zp, wp, zo, wo);
               dsum += 0.5 * dc6 / c6po;
             }
             dedcnd[p] += ec * dsum;
@@ -1184,18 +1343,21 @@ int qcxo_egrad(int nat, const int* Z, const double* xyz, double charge, double k
           double ga = c.es.gam[s * nsh + t];
           dEdR += qsh[s] * qsh[t] * (-R * ga * ga * ga);
         }
-      /* dispersion */
-      double zz = c.es.zeta[a] * c.es.zeta[b];
-      dEdR += -zz * c.es.c6[a * nat + b] * c.es.dgdisp[a * nat + b];
-      double gdis = c.es.gdisp[a * nat + b];
-      for (int ii = 0; ii < 2; ++ii) {
-        int p = ii == 0 ? a : b, o2 = ii == 0 ? b : a;
-        int zp = Z[p], zo = Z[o2];
-        double dc6 = 0.0;
-        for (int i = 0; i < qcx_d4_nref[zp]; ++i)
-          for (int j = 0; j < qcx_d4_nref[zo]; ++j)
-            dc6 += c.es.dw[p * QCX_MAXREF + i] * c.es.w[o2 * QCX_MAXREF + j] * c6ref(zp, i, zo, j);
-        dedcnd[p] += -zz * gdis * dc6;
+      /* dispersion at the converged charges (dispgrad, src/dftd4.f90:1198-1262):
+       * radial term -C6_AB(q) dg/dR, and dE/dCN through the reference weights */
+      {
+        const int R = QCX_D4_MAXREF;
+        double wa[QCX_D4_MAXREF], wb[QCX_D4_MAXREF], dwa[QCX_D4_MAXREF], dwb[QCX_D4_MAXREF];
+        for (int i = 0; i < R; ++i) {
+          wa[i] = c.es.gw[a * R + i] * c.es.zq[a * R + i];
+          wb[i] = c.es.gw[b * R + i] * c.es.zq[b * R + i];
+          dwa[i] = c.es.dgw[a * R + i] * c.es.zq[a * R + i];
+          dwb[i] = c.es.dgw[b * R + i] * c.es.zq[b * R + i];
+        }
+        double gdis = c.es.gdisp[a * nat + b];
+        dEdR += -d4_c6(Z[a], wa, Z[b], wb) * c.es.dgdisp[a * nat + b];
+        dedcnd[a] += -gdis * d4_c6(Z[a], dwa, Z[b], wb);
+        dedcnd[b] += -gdis * d4_c6(Z[b], dwb, Z[a], wa);
       }
       /* multipoles */
       double r0 = 0.5 * (c.es.mrad[a] + c.es.mrad[b]);
@@ -1241,7 +1403,7 @@ int qcxo_egrad(int nat, const int* Z, const double* xyz, double charge, double k
       for (int k = 0; k < 3; ++k) { r[k] = xyz[3 * a + k] - xyz[3 * b + k]; r2 += r[k] * r[k]; }
       double R = sqrt(r2), rc = qcx_rcov[Z[a]] + qcx_rcov[Z[b]], f, df1, df2;
       cn_exp_pair(R, rc, &f, &df1);
-      cn_erf_pair(R, rc, &f, &df2);
+      d4_cn_pair(Z[a], Z[b], r2, &f, &df2);
       double s = (dedcn[a] + dedcn[b]) * df1 + (dedcnd[a] + dedcnd[b]) * df2;
       for (int k = 0; k < 3; ++k) { g[3 * a + k] += s * r[k] / R; g[3 * b + k] -= s * r[k] / R; }
     }

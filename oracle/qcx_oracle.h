@@ -62,6 +62,13 @@ int qcxo_scc(int nat, const int* Z, const double* xyz, double charge, double kT,
  * A [n][n] is destroyed; V [n][n] holds eigenvectors as columns. */
 int qcxo_syev(int n, double* A, double* w, double* V);
 
+/* D4 data checks: C6 of reference pair (za, i; zb, j) built from QCxMS's
+ * reference polarisabilities (src/dftd4.f90:531-595, 665), -1 outside the
+ * table; and the molecular C6 [nat][nat] at the covalent CNs and charges q
+ * (zero charges if q is NULL). */
+double qcxo_d4_c6ref(int za, int i, int zb, int j);
+void qcxo_d4_c6(int nat, const int* Z, const double* xyz, const double* q, double* c6);
+
 /* Reference MD helpers. */
 void qcxo_leapfrog(int nat, const double* grad, const double* mass, double tstep,
                    double* xyz, double* vel, double* ke);

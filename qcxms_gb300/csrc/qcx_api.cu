@@ -7,12 +7,14 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/qcxgpu.h"
 #include "qcx_batch.cuh"
+#include "qcx_d4host.h"
 #include "qcx_kernels.h"
 
 using namespace qcx;
@@ -72,15 +74,8 @@ void fill_params(Params& p) {
     p.aes_qk[z] = qcx_aes_qkernel[z];
     p.aes_rad0[z] = qcx_aes_rad0[z];
     p.aes_valcn[z] = qcx_aes_valcn[z];
-    p.d4_nref[z] = qcx_d4_nref[z];
-    for (int i = 0; i < kMaxRef; ++i) {
-      p.d4_cnref[z][i] = qcx_d4_cnref[z][i];
-      p.d4_alpha0[z][i] = qcx_d4_alpha0[z][i];
-      p.d4_omega[z][i] = qcx_d4_omega[z][i];
-    }
-    p.d4_eta[z] = qcx_d4_eta[z];
-    p.r4r2[z] = qcx_r4r2[z];
   }
+  fill_d4_params(p);
 }
 
 template <typename T>
@@ -322,8 +317,8 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   }
   b->npair = (int)pairs.size();
   CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-  Params hp;
-  fill_params(hp);
+  std::unique_ptr<Params> hp(new Params);  // ~230 KB: not on the stack
+  fill_params(*hp);
   int na = b->natom;
   if (dalloc(&b->d_prm, 1) || dalloc(&b->d_mol, nmol) || dalloc(&b->d_Z, na) || dalloc(&b->d_atom_mol, na) ||
       dalloc(&b->d_sh_atom, b->nshell) || dalloc(&b->d_sh_k, b->nshell) || dalloc(&b->d_sh_ao, b->nshell) ||
@@ -381,7 +376,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
     CK(cudaEventCreateWithFlags(&b->g_fork, cudaEventDisableTiming));
   }
   b->bytes = sizeof(double) * ((size_t)mat_off + (size_t)vec_off);
-  CK(cudaMemcpy(b->d_prm, &hp, sizeof(Params), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_prm, hp.get(), sizeof(Params), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b->d_mol, b->mol.data(), sizeof(MolDesc) * nmol, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b->d_Z, b->Z.data(), sizeof(int) * na, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b->d_atom_mol, atom_mol.data(), sizeof(int) * na, cudaMemcpyHostToDevice));

@@ -16,15 +16,16 @@ __global__ void k_cn(DevBatch bt) {
   const MolDesc md = bt.mol[bt.atom_mol[a]];
   int za = bt.Z[a];
   double xa = bt.xyz[3 * a], ya = bt.xyz[3 * a + 1], zz = bt.xyz[3 * a + 2];
-  double cn = 0.0, cnd = 0.0;
+  double cn = 0.0, cnd = 0.0;  // the H0 / multipole CN and the D4 covalent CN
   for (int b = md.atom_off; b < md.atom_off + md.nat; ++b) {
     if (b == a) continue;
     double dx = xa - bt.xyz[3 * b], dy = ya - bt.xyz[3 * b + 1], dz = zz - bt.xyz[3 * b + 2];
-    double r = sqrt(dx * dx + dy * dy + dz * dz);
+    double r2 = dx * dx + dy * dy + dz * dz;
+    double r = sqrt(r2);
     double rc = P.rcov[za] + P.rcov[bt.Z[b]], f, df;
     cn_exp_pair(r, rc, f, df);
     cn += f;
-    cn_erf_pair(r, rc, f, df);
+    d4_cn_pair(P, za, bt.Z[b], r2, f, df);
     cnd += f;
   }
   bt.cn[a] = cn;
@@ -127,12 +128,16 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
   const double* dp = xout + nsh;
   const double* qp = xout + nsh + 3 * nat;
   const double* qa = vec + vl.qat;
-  const double* zeta = vec + vl.zeta;
+  const double* wq = vec + vl.wq;  // gw zeta(q) per atom and reference, at the final charges
+  const double* zq = vec + vl.zq;  // zeta(q)
   const double* gam = vec + vl.gam;
   double* g = sm;                // [3 nat]
   double* dcn = sm + 3 * nat;    // [nat]
   double* dcnd = sm + 4 * nat;   // [nat]
   double* red = sm + 5 * nat;    // [32]
+  // zero-charge reference weights of the three-body term (gw zeta(0), dgw zeta(0)), FP32
+  float* w0 = (float*)(sm + 6 * nat + 32);  // [nat][kMaxRef], after the int scratch below
+  float* dw0 = w0 + kMaxRef * nat;
   const double* xyz = bt.xyz + 3LL * off;
   const int* Z = bt.Z + off;
   const int* sh_atom = bt.sh_atom + md.sh_off;
@@ -155,6 +160,13 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
     }
     dcn[a] = d;
     dcnd[a] = 0.0;
+    const int z = Z[a];
+    for (int i = 0; i < kMaxRef; ++i) {
+      double zt = 0.0, dzt;
+      if (i < P.d4_refn[z]) d4_zeta(P, z, i, 0.0, zt, dzt);
+      w0[kMaxRef * a + i] = (float)(bt.w4[(long long)(off + a) * kMaxRef + i] * zt);
+      dw0[kMaxRef * a + i] = (float)(bt.dw4[(long long)(off + a) * kMaxRef + i] * zt);
+    }
   }
   __syncthreads();
   // (a) pair terms over all ordered atom pairs (b-major, so that consecutive
@@ -189,22 +201,20 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
           double gm = gam[s * nsh + t];
           dEdR += qsh[s] * qsh[t] * (-R * gm * gm * gm);
         }
-      // dispersion (two-body): E = -zeta_a zeta_b C6_ab g_ab
+      // dispersion (two-body) at the converged charges, as dispgrad
+      // (src/dftd4.f90:1198-1262): E_ab = -C6_ab(q) g_ab with
+      // C6_ab(q) = sum_ij (gw zeta(q))_ai (gw zeta(q))_bj C6_ij; the CN derivative
+      // goes through the weights of atom a
       double gd, dgd;
       bj_kernel(P, za, zb, R, gd, dgd);
-      double c6 = 0.0, dc6a = 0.0;
-      const double* wa = bt.w4 + (long long)(off + a) * kMaxRef;
-      const double* dwa = bt.dw4 + (long long)(off + a) * kMaxRef;
-      const double* wb = bt.w4 + (long long)(off + b) * kMaxRef;
-      for (int i = 0; i < P.d4_nref[za]; ++i)
-        for (int j = 0; j < P.d4_nref[zb]; ++j) {
-          double cr = c6ref(P, za, i, zb, j);
-          c6 += wa[i] * wb[j] * cr;
-          dc6a += dwa[i] * wb[j] * cr;
-        }
-      double zz = zeta[a] * zeta[b];
-      dEdR += -zz * c6 * dgd;
-      dcda += -zz * gd * dc6a;
+      const double* wqa = wq + (long long)kMaxRef * a;
+      const double* wqb = wq + (long long)kMaxRef * b;
+      const double* zqa = zq + (long long)kMaxRef * a;
+      const double* dgwa = bt.dw4 + (long long)(off + a) * kMaxRef;
+      double dwa[kMaxRef];
+      for (int i = 0; i < kMaxRef; ++i) dwa[i] = dgwa[i] * zqa[i];
+      dEdR += -d4_c6(P, za, wqa, zb, wqb) * dgd;
+      dcda += -gd * d4_c6(P, za, dwa, zb, wqb);
       // repulsion
       {
         double al = sqrt(P.rep_alpha[za] * P.rep_alpha[zb]);
@@ -267,34 +277,27 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
       y += rbc[k] * rbc[k];
       z += rca[k] * rca[k];
     }
-    const double* w[3] = {bt.w4 + (long long)(off + a) * kMaxRef, bt.w4 + (long long)(off + b) * kMaxRef,
-                          bt.w4 + (long long)(off + c) * kMaxRef};
-    const double* dw[3] = {bt.dw4 + (long long)(off + a) * kMaxRef, bt.dw4 + (long long)(off + b) * kMaxRef,
-                           bt.dw4 + (long long)(off + c) * kMaxRef};
+    const int at3[3] = {a, b, c};
     int zs[3] = {za, zb, zc};
-    // C6 of the three pairs and their CN' derivatives: pair (i,j) for (0,1),(1,2),(2,0)
+    // zero-charge C6 of the three pairs and their CN derivatives: pair (i,j) for (0,1),(1,2),(2,0)
     float c6p[3], dc6[3][2];
     const int pi[3] = {0, 1, 2}, pj[3] = {1, 2, 0};
     for (int pr = 0; pr < 3; ++pr) {
-      int i0 = pi[pr], j0 = pj[pr];
-      float s = 0.0f, di = 0.0f, dj = 0.0f;
-      for (int ii = 0; ii < P.d4_nref[zs[i0]]; ++ii)
-        for (int jj = 0; jj < P.d4_nref[zs[j0]]; ++jj) {
-          float cr = (float)c6ref(P, zs[i0], ii, zs[j0], jj);
-          float wi = (float)w[i0][ii], wj = (float)w[j0][jj];
-          s += wi * wj * cr;
-          di += (float)dw[i0][ii] * wj * cr;
-          dj += wi * (float)dw[j0][jj] * cr;
-        }
-      c6p[pr] = s;
-      dc6[pr][0] = di;
-      dc6[pr][1] = dj;
+      const int i0 = pi[pr], j0 = pj[pr];
+      const float* wi = w0 + kMaxRef * at3[i0];
+      const float* wj = w0 + kMaxRef * at3[j0];
+      c6p[pr] = d4_c6(P, zs[i0], wi, zs[j0], wj);
+      dc6[pr][0] = d4_c6(P, zs[i0], dw0 + kMaxRef * at3[i0], zs[j0], wj);
+      dc6[pr][1] = d4_c6(P, zs[j0], dw0 + kMaxRef * at3[j0], zs[i0], wi);
     }
+    // C9 = s9 sqrt(C6_ab C6_bc C6_ca); damping 1/(1 + 6 (R0/rbar)^alp) with the
+    // geometric means R0, rbar of the three BJ radii and distances (apprabc,
+    // src/dftd4.f90:1339-1400)
     float c9 = (float)QCX_D4_S9 * sqrtf(c6p[0] * c6p[1] * c6p[2]);
     float r0 = cbrtf((float)(bj_radius(P, za, zb) * bj_radius(P, zb, zc) * bj_radius(P, zc, za)));
     float rrr = sqrtf(x) * sqrtf(y) * sqrtf(z);
     float rbar = cbrtf(rrr);
-    const float alp3 = (float)(QCX_ATM_ALP / 3.0);
+    const float alp3 = (float)QCX_ATM_ALP;
     float tt = 6.0f * powf(r0 / rbar, alp3);
     float fd = 1.0f / (1.0f + tt);
     float u1 = x + z - y, u2 = x + y - z, u3 = y + z - x;
@@ -335,10 +338,11 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
     int b = idx / nat, a = idx - b * nat;
     if (b == a) continue;
     double r[3] = {xyz[3 * a] - xyz[3 * b], xyz[3 * a + 1] - xyz[3 * b + 1], xyz[3 * a + 2] - xyz[3 * b + 2]};
-    double R = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    double R = sqrt(r2);
     double rc = P.rcov[Z[a]] + P.rcov[Z[b]], f, df1, df2;
     cn_exp_pair(R, rc, f, df1);
-    cn_erf_pair(R, rc, f, df2);
+    d4_cn_pair(P, Z[a], Z[b], r2, f, df2);
     double s = (dcn[a] + dcn[b]) * df1 + (dcnd[a] + dcnd[b]) * df2;
     for (int k = 0; k < 3; ++k) atomicAdd(&g[3 * a + k], s * r[k] / R);
   }
@@ -384,8 +388,9 @@ void launch_checkqc(int nat, const double* grad, const double* qat, double charg
 }
 
 void launch_grad_atoms(const DevBatch& bt, cudaStream_t st) {
-  // largest molecule bounds the shared memory: 5 nat + 32 doubles + 2 nat ints
-  size_t smem = sizeof(double) * (6 * (size_t)bt.max_nao + 64);
+  // largest molecule bounds the shared memory (nat <= nao): 5 nat + 32 doubles,
+  // 2 nat ints, 2 kMaxRef nat floats
+  size_t smem = sizeof(double) * ((6 + kMaxRef) * (size_t)bt.max_nao + 64);
   k_grad_atoms<<<bt.nmol, kAtomThreads, smem, st>>>(bt);
 }
 

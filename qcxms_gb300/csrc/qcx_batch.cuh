@@ -55,7 +55,9 @@ struct MolDesc {
 
 // offsets inside a molecule's vector block
 struct VecLayout {
-  long long eps, focc, xin, xout, vsh, vdp, vqp, qat, vat, gam, c6g, f3, f5, d3r, d3r0, d5r, d5r0, zeta, dzeta,
+  // gdisp: BJ kernel g_AB of every atom pair; wq, dwq, zq: per atom and D4
+  // reference, gw zeta(q), gw dzeta/dq and zeta(q) at the last potentials' charges
+  long long eps, focc, xin, xout, vsh, vdp, vqp, qat, vat, gam, gdisp, f3, f5, d3r, d3r0, d5r, d5r0, wq, dwq, zq,
       bdf, bu, ba, bxl, bfl, bc, bm, total;
   __host__ __device__ static VecLayout make(int nat, int nsh, int nao, int len, int nmem) {
     VecLayout v;
@@ -75,15 +77,16 @@ struct VecLayout {
     v.qat = take(nat);
     v.vat = take(nat);
     v.gam = take((long long)nsh * nsh);
-    v.c6g = take((long long)nat * nat);
+    v.gdisp = take((long long)nat * nat);
     v.f3 = take((long long)nat * nat);
     v.f5 = take((long long)nat * nat);
     v.d3r = take((long long)nat * nat);
     v.d3r0 = take((long long)nat * nat);
     v.d5r = take((long long)nat * nat);
     v.d5r0 = take((long long)nat * nat);
-    v.zeta = take(nat);
-    v.dzeta = take(nat);
+    v.wq = take((long long)kMaxRef * nat);
+    v.dwq = take((long long)kMaxRef * nat);
+    v.zq = take((long long)kMaxRef * nat);
     v.bdf = take((long long)nmem * len);
     v.bu = take((long long)nmem * len);
     v.ba = take((long long)nmem * nmem);
@@ -118,8 +121,8 @@ struct DevBatch {
   double* dedcnd;
   double* mrad;
   double* dmrad;
-  double* w4;      // [natom][kMaxRef]
-  double* dw4;     // [natom][kMaxRef]
+  double* w4;      // [natom][kMaxRef] D4 reference weights at the covalent CN
+  double* dw4;     // [natom][kMaxRef] their CN derivatives
   double* qat;     // output atomic charges
   // shells (global index)
   const int* sh_atom;  // global atom index

@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "qcx_consts.h"
+#include "qcx_d4ref.h"
 #include "qcx_params.h"
 
 namespace qcx {
@@ -16,7 +17,7 @@ namespace qcx {
 constexpr int kMaxZ = QCX_MAXZ;
 constexpr int kMaxSh = QCX_MAXSH;
 constexpr int kMaxPrim = QCX_MAXPRIM;
-constexpr int kMaxRef = QCX_MAXREF;
+constexpr int kMaxRef = QCX_D4_MAXREF;  // D4 reference systems per element
 
 // Flattened copy of qcx_params.h that lives in device memory.
 struct Params {
@@ -40,12 +41,18 @@ struct Params {
   double aes_qk[kMaxZ + 1];
   double aes_rad0[kMaxZ + 1];
   double aes_valcn[kMaxZ + 1];
-  int d4_nref[kMaxZ + 1];
-  double d4_cnref[kMaxZ + 1][kMaxRef];
-  double d4_alpha0[kMaxZ + 1][kMaxRef];
-  double d4_omega[kMaxZ + 1][kMaxRef];
-  double d4_eta[kMaxZ + 1];
-  double r4r2[kMaxZ + 1];
+  // D4 model of QCxMS's src/dftd4.f90 with its reference data (qcx_d4ref.h)
+  int d4_refn[kMaxZ + 1];                 // reference systems per element
+  int d4_refc[kMaxZ + 1][kMaxRef];        // Gaussians per reference (d4dim)
+  double d4_refcovcn[kMaxZ + 1][kMaxRef];  // covalent CN of each reference
+  double d4_refq[kMaxZ + 1][kMaxRef];      // charge of each reference
+  double d4_gam[kMaxZ + 1];                // chemical hardness (charge scaling)
+  double d4_zeff[kMaxZ + 1];               // effective nuclear charge
+  double d4_en[kMaxZ + 1];                 // Pauling electronegativity (covalent CN)
+  double d4_rcov[kMaxZ + 1];               // covalent radius (Bohr, covalent CN)
+  double r4r2[kMaxZ + 1];                  // <r^4>/<r^2> expectation ratio (C8, damping)
+  double d4_c6r[kMaxZ + 1][kMaxZ + 1][kMaxRef][kMaxRef];  // C6 of every reference pair
+  float d4_c6r32[kMaxZ + 1][kMaxZ + 1][kMaxRef][kMaxRef]; // the same in FP32 (FP32 iterations)
 };
 
 __host__ __device__ inline int nsph(int l) { return 2 * l + 1; }
@@ -60,10 +67,23 @@ __device__ inline void cn_exp_pair(double r, double rc, double& f, double& df) {
   df = -f * f * e * QCX_KCN * rc / (r * r);
 }
 
-__device__ inline void cn_erf_pair(double r, double rc, double& f, double& df) {
-  double t = QCX_KERF * (r / rc - 1.0);
-  f = 0.5 * erfc(t);
-  df = -QCX_KERF / (rc * sqrt(QCX_PI)) * exp(-t * t);
+// Covalent coordination number of the D4 model (covncoord / gcovncoord,
+// src/dftd4.f90:292-325, 1033-1068): a pair within r^2 <= 1600 Bohr^2 adds
+// den / (1 + exp(-k1 (rcov_ab / r - 1))), den = k4 exp(-(|EN_a - EN_b| + k5)^2 / k6);
+// df = d(contribution)/dr.
+constexpr double kD4K1 = 16.0, kD4K4 = 4.10451, kD4K5 = 19.08857, kD4K6 = 2 * 11.28174 * 11.28174;
+constexpr double kD4CnThr = 1600.0;
+__device__ inline void d4_cn_pair(const Params& p, int za, int zb, double r2, double& f, double& df) {
+  f = 0.0;
+  df = 0.0;
+  if (r2 > kD4CnThr) return;
+  const double r = sqrt(r2);
+  const double x = fabs(p.d4_en[za] - p.d4_en[zb]) + kD4K5;
+  const double den = kD4K4 * exp(-(x * x) / kD4K6);
+  const double rco = p.d4_rcov[za] + p.d4_rcov[zb];
+  const double ex = exp(-kD4K1 * (rco / r - 1.0));
+  f = den / (1.0 + ex);
+  df = (-kD4K1 * rco * ex * den) / (r2 * ((1.0 + ex) * (1.0 + ex)));
 }
 
 // ---------------------------------------------------------------------------
@@ -115,42 +135,77 @@ __device__ inline void mp_kernel(int n, double a, double r, double r0, double& f
   dfr0 = dfd_r0 / rn;
 }
 
-__device__ inline double c6ref(const Params& p, int za, int i, int zb, int j) {
-  double aa = p.d4_alpha0[za][i], ab = p.d4_alpha0[zb][j];
-  double wa = p.d4_omega[za][i], wb = p.d4_omega[zb][j];
-  return 1.5 * aa * ab * wa * wb / (wa + wb);
-}
-
+// Reference weights of an atom at covalent CN cn (src/dftd4.f90:1150-1193):
+// gw_i = sum_{k <= refc_i} exp(-k wf (cn - cn_i)^2) / norm and d gw_i / d cn; a
+// weight that overflows to NaN becomes 1 for the reference with the largest CN
+// and 0 otherwise (derivative 0).
 __device__ inline void d4_weights(const Params& p, int z, double cn, double* w, double* dw) {
-  int nr = p.d4_nref[z];
-  double ex[kMaxRef], mx = -1e300;
+  const int nr = p.d4_refn[z];
+  double norm = 0.0, dnorm = 0.0, maxcn = -1e300;
   for (int i = 0; i < nr; ++i) {
-    double t = cn - p.d4_cnref[z][i];
-    ex[i] = -QCX_D4_WF * t * t;
-    mx = ex[i] > mx ? ex[i] : mx;
+    const double cr = p.d4_refcovcn[z][i], d = cn - cr;
+    maxcn = cr > maxcn ? cr : maxcn;
+    for (int k = 1; k <= p.d4_refc[z][i]; ++k) {
+      const double twf = k * QCX_D4_WF, t = exp(-twf * d * d);
+      norm += t;
+      dnorm += 2.0 * twf * (cr - cn) * t;
+    }
   }
-  double sum = 0.0, dsum = 0.0, g[kMaxRef], dg[kMaxRef];
-  for (int i = 0; i < nr; ++i) {
-    g[i] = exp(ex[i] - mx);
-    dg[i] = -2.0 * QCX_D4_WF * (cn - p.d4_cnref[z][i]) * g[i];
-    sum += g[i];
-    dsum += dg[i];
-  }
+  norm = 1.0 / norm;
   for (int i = 0; i < kMaxRef; ++i) {
     w[i] = 0.0;
     dw[i] = 0.0;
   }
   for (int i = 0; i < nr; ++i) {
-    w[i] = g[i] / sum;
-    dw[i] = (dg[i] * sum - g[i] * dsum) / (sum * sum);
+    const double cr = p.d4_refcovcn[z][i], d = cn - cr;
+    double e = 0.0, de = 0.0;
+    for (int k = 1; k <= p.d4_refc[z][i]; ++k) {
+      const double twf = k * QCX_D4_WF, t = exp(-twf * d * d);
+      e += t;
+      de += 2.0 * twf * (cr - cn) * t;
+    }
+    double wi = e * norm, dwi = de * norm - e * dnorm * norm * norm;
+    if (wi != wi) wi = cr == maxcn ? 1.0 : 0.0;
+    if (dwi != dwi) dwi = 0.0;
+    w[i] = wi;
+    dw[i] = dwi;
   }
 }
 
-__device__ inline void d4_zeta(const Params& p, int z, double q, double& zeta, double& dzeta) {
-  double t = QCX_D4_GC * p.d4_eta[z] / (double)z;
-  double ex = exp(t * q);
-  zeta = exp(QCX_D4_GA * (1.0 - ex));
-  dzeta = zeta * (-QCX_D4_GA * ex * t);
+// Charge scaling of reference i of element z at atomic charge q
+// (zeta / dzeta, src/dftd4.f90:423-450): exp(ga (1 - exp(c (1 - qref/qmod))))
+// with c = gam * gc, qref = refq_i + zeff, qmod = q + zeff; exp(ga) for qmod < 0.
+__device__ inline void d4_zeta(const Params& p, int z, int i, double q, double& zeta, double& dzeta) {
+  const double iz = p.d4_zeff[z], c = p.d4_gam[z] * QCX_D4_GC;
+  const double qref = p.d4_refq[z][i] + iz, qmod = q + iz;
+  if (qmod < 0.0) {
+    zeta = exp(QCX_D4_GA);
+    dzeta = 0.0;
+    return;
+  }
+  const double t = exp(c * (1.0 - qref / qmod));
+  zeta = exp(QCX_D4_GA * (1.0 - t));
+  dzeta = -QCX_D4_GA * c * t * zeta * qref / (qmod * qmod);
+}
+
+// sum_ij wa_i wb_j C6(za, i, zb, j)
+__device__ inline double d4_c6(const Params& p, int za, const double* wa, int zb, const double* wb) {
+  double s = 0.0;
+  for (int i = 0; i < p.d4_refn[za]; ++i) {
+    double t = 0.0;
+    for (int j = 0; j < p.d4_refn[zb]; ++j) t += wb[j] * p.d4_c6r[za][zb][i][j];
+    s += wa[i] * t;
+  }
+  return s;
+}
+__device__ inline float d4_c6(const Params& p, int za, const float* wa, int zb, const float* wb) {
+  float s = 0.0f;
+  for (int i = 0; i < p.d4_refn[za]; ++i) {
+    float t = 0.0f;
+    for (int j = 0; j < p.d4_refn[zb]; ++j) t += wb[j] * p.d4_c6r32[za][zb][i][j];
+    s += wa[i] * t;
+  }
+  return s;
 }
 
 __device__ inline double bj_radius(const Params& p, int za, int zb) {

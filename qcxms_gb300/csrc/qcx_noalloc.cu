@@ -27,6 +27,7 @@
 
 #include "../../include/qcxgpu.h"
 #include "qcx_batch.cuh"
+#include "qcx_d4host.h"
 #include "qcx_kernels.h"
 
 namespace qcx {
@@ -55,7 +56,8 @@ constexpr StaticLayout make_layout() {
   auto r4 = [](long long n) { return (n + 3) & ~3LL; };
   const long long vec_doubles = r4(kStaticMaxNao) * 2 + r4(len) * 2 + r4(kStaticMaxShells) + r4(3 * na) +
                                 r4(6 * na) + r4(na) * 2 + r4((long long)kStaticMaxShells * kStaticMaxShells) +
-                                r4((long long)na * na) * 7 + r4(na) * 2 + r4((long long)kStaticNmem * len) * 2 +
+                                r4((long long)na * na) * 7 + r4((long long)kMaxRef * na) * 3 +
+                                r4((long long)kStaticNmem * len) * 2 +
                                 r4((long long)kStaticNmem * kStaticNmem) + r4(len) * 2 + r4(kStaticNmem) +
                                 r4((long long)kStaticNmem * kStaticNmem + kStaticNmem);
   L.magic = o; o = align256(o + sizeof(unsigned long long));
@@ -158,15 +160,8 @@ void fill_params_static(Params& p) {
     p.aes_qk[z] = qcx_aes_qkernel[z];
     p.aes_rad0[z] = qcx_aes_rad0[z];
     p.aes_valcn[z] = qcx_aes_valcn[z];
-    p.d4_nref[z] = qcx_d4_nref[z];
-    for (int i = 0; i < kMaxRef; ++i) {
-      p.d4_cnref[z][i] = qcx_d4_cnref[z][i];
-      p.d4_alpha0[z][i] = qcx_d4_alpha0[z][i];
-      p.d4_omega[z][i] = qcx_d4_omega[z][i];
-    }
-    p.d4_eta[z] = qcx_d4_eta[z];
-    p.r4r2[z] = qcx_r4r2[z];
   }
+  fill_d4_params(p);
 }
 
 #define SCK(call, what)                                                 \

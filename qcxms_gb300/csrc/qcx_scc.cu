@@ -243,25 +243,32 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
   double* vsh = vec + mv.vl.vsh;
   double* vdp = vec + mv.vl.vdp;
   double* vqp = vec + mv.vl.vqp;
-  double* zeta = vec + mv.vl.zeta;
-  double* dzeta = vec + mv.vl.dzeta;
+  double* wq = vec + mv.vl.wq;    // [nat][kMaxRef] gw zeta(q)
+  double* dwq = vec + mv.vl.dwq;  // [nat][kMaxRef] gw dzeta/dq
+  double* zq = vec + mv.vl.zq;    // [nat][kMaxRef] zeta(q)
   const double* gam = vec + mv.vl.gam;
-  const double* c6g = vec + mv.vl.c6g;
+  const double* gdm = vec + mv.vl.gdisp;
   const double* f3m = vec + mv.vl.f3;
   const double* f5m = vec + mv.vl.f5;
   const int* sh_k = mv.bt->sh_k + mv.md.sh_off;
   const int* sh_atom = mv.bt->sh_atom + mv.md.sh_off;
   const int aoff = mv.md.atom_off;
-  // atomic charges and charge scaling
+  // atomic charges and the charge scaling of every D4 reference (edisp /
+  // disppot, src/dftd4.f90:807-1034)
   for (int a = threadIdx.x; a < nat; a += blockDim.x) {
     double q = 0.0;
     for (int s = 0; s < nsh; ++s)
       if (sh_atom[s] - aoff == a) q += qsh[s];
     qat[a] = q;
-    double zt, dzt;
-    d4_zeta(P, mv.Z[a], q, zt, dzt);
-    zeta[a] = zt;
-    dzeta[a] = dzt;
+    const int z = mv.Z[a];
+    const double* gw = mv.bt->w4 + (long long)(aoff + a) * kMaxRef;
+    for (int i = 0; i < kMaxRef; ++i) {
+      double zt = 0.0, dzt = 0.0;
+      if (i < P.d4_refn[z]) d4_zeta(P, z, i, q, zt, dzt);
+      zq[kMaxRef * a + i] = zt;
+      wq[kMaxRef * a + i] = gw[i] * zt;
+      dwq[kMaxRef * a + i] = gw[i] * dzt;
+    }
   }
   __syncthreads();
   double e[5] = {0, 0, 0, 0, 0};
@@ -301,10 +308,14 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
       rta += ta[q] * rr[q];
       rtb += tb[q] * rr[q];
     }
-    double cg = c6g[a * nat + b];
+    // dispersion: E_ab = -g_ab sum_ij wq_ai wq_bj C6_ij; the a-side charge derivative
+    const double gd = gdm[a * nat + b];
+    const int za = mv.Z[a], zb = mv.Z[b];
+    const double c6 = d4_c6(P, za, wq + kMaxRef * a, zb, wq + kMaxRef * b);
+    const double dc6 = d4_c6(P, za, dwq + kMaxRef * a, zb, wq + kMaxRef * b);
     e[2] += 0.5 * (f3 * (qat[a] * mbr - qat[b] * mar) + f5 * (qat[a] * rtb + qat[b] * rta + mab * r2 - 3.0 * mar * mbr));
-    e[4] += -0.5 * zeta[a] * zeta[b] * cg;
-    atomicAdd(&vat[a], f3 * mbr + f5 * rtb - dzeta[a] * zeta[b] * cg);
+    e[4] += -0.5 * gd * c6;
+    atomicAdd(&vat[a], f3 * mbr + f5 * rtb - gd * dc6);
     for (int k = 0; k < 3; ++k) atomicAdd(&vdp[3 * a + k], -f3 * qat[b] * r[k] + f5 * (mb[k] * r2 - 3.0 * mbr * r[k]));
     for (int q = 0; q < 6; ++q) atomicAdd(&vqp[6 * a + q], f5 * qat[b] * rr[q]);
   }
@@ -329,14 +340,16 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
 // FP32, written to shared memory for the FP32 Fock build, with shared-memory
 // atomics for the pair sums. Layout of v32: shell potentials [nsh], dipole
 // [3 nat] and quadrupole [6 nat] potentials, atom positions [3 nat], then
-// scratch (dipoles, quadrupoles, charges, zeta, dzeta, atom potentials).
-// Returns false, writing nothing, when the scratch (nsh + 25 nat floats)
+// scratch (dipoles, quadrupoles, charges, atom potentials); the D4 reference
+// weights times the charge scaling and its derivative go to the vector block
+// (as FP32, in the space of the FP64 weights, which the FP64 potentials rewrite).
+// Returns false, writing nothing, when the scratch (nsh + 23 nat floats)
 // exceeds the 20 n floats available.
 // ---------------------------------------------------------------------------
 __device__ bool potentials32(const MolView& mv, const double* x, float* v32, int n) {
   const Params& P = *mv.bt->prm;
   const int nat = mv.md.nat, nsh = mv.md.nsh;
-  if (nsh + 25 * nat > 20 * n) return false;
+  if (nsh + 23 * nat > 20 * n) return false;
   float* vs32 = v32;
   float* vd32 = vs32 + nsh;
   float* vq32 = vd32 + 3 * nat;
@@ -344,15 +357,15 @@ __device__ bool potentials32(const MolView& mv, const double* x, float* v32, int
   float* m32 = r32 + 3 * nat;
   float* t32 = m32 + 3 * nat;
   float* q32 = t32 + 6 * nat;
-  float* z32 = q32 + nat;
-  float* dz32 = z32 + nat;
-  float* va32 = dz32 + nat;
+  float* va32 = q32 + nat;
   const double* qsh = x;
   const double* dp = x + nsh;
   const double* qp = x + nsh + 3 * nat;
-  const double* vec = mv.vec;
+  double* vec = mv.vec;
+  float* wq32 = (float*)(vec + mv.vl.wq);  // [nat][kMaxRef]
+  float* dwq32 = wq32 + kMaxRef * nat;     // [nat][kMaxRef]
   const double* gam = vec + mv.vl.gam;
-  const double* c6g = vec + mv.vl.c6g;
+  const double* gdm = vec + mv.vl.gdisp;
   const double* f3m = vec + mv.vl.f3;
   const double* f5m = vec + mv.vl.f5;
   const int* sh_k = mv.bt->sh_k + mv.md.sh_off;
@@ -362,11 +375,15 @@ __device__ bool potentials32(const MolView& mv, const double* x, float* v32, int
     double q = 0.0;
     for (int t = 0; t < nsh; ++t)
       if (sh_atom[t] - aoff == a) q += qsh[t];
-    double zt, dzt;
-    d4_zeta(P, mv.Z[a], q, zt, dzt);
+    const int z = mv.Z[a];
+    const double* gw = mv.bt->w4 + (long long)(aoff + a) * kMaxRef;
+    for (int i = 0; i < kMaxRef; ++i) {
+      double zt = 0.0, dzt = 0.0;
+      if (i < P.d4_refn[z]) d4_zeta(P, z, i, q, zt, dzt);
+      wq32[kMaxRef * a + i] = (float)(gw[i] * zt);
+      dwq32[kMaxRef * a + i] = (float)(gw[i] * dzt);
+    }
     q32[a] = (float)q;
-    z32[a] = (float)zt;
-    dz32[a] = (float)dzt;
     va32[a] = 0.f;
     const float fd = (float)P.aes_dk[mv.Z[a]], fq = (float)P.aes_qk[mv.Z[a]];
     for (int k = 0; k < 3; ++k) {
@@ -386,7 +403,8 @@ __device__ bool potentials32(const MolView& mv, const double* x, float* v32, int
     if (b == a) continue;
     float r[3] = {r32[3 * a] - r32[3 * b], r32[3 * a + 1] - r32[3 * b + 1], r32[3 * a + 2] - r32[3 * b + 2]};
     float r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-    float f3 = (float)f3m[a * nat + b], f5 = (float)f5m[a * nat + b], cg = (float)c6g[a * nat + b];
+    float f3 = (float)f3m[a * nat + b], f5 = (float)f5m[a * nat + b], gd = (float)gdm[a * nat + b];
+    const float dc6 = d4_c6(P, mv.Z[a], dwq32 + kMaxRef * a, mv.Z[b], wq32 + kMaxRef * b);
     const float* mb = m32 + 3 * b;
     const float* tb = t32 + 6 * b;
     float mbr = mb[0] * r[0] + mb[1] * r[1] + mb[2] * r[2];
@@ -394,7 +412,7 @@ __device__ bool potentials32(const MolView& mv, const double* x, float* v32, int
     float rtb = 0.f;
     for (int c = 0; c < 6; ++c) rtb += tb[c] * rr[c];
     const float qb = q32[b];
-    atomicAdd(&va32[a], f3 * mbr + f5 * rtb - dz32[a] * z32[b] * cg);
+    atomicAdd(&va32[a], f3 * mbr + f5 * rtb - gd * dc6);
     for (int k = 0; k < 3; ++k) atomicAdd(&vd32[3 * a + k], -f3 * qb * r[k] + f5 * (mb[k] * r2 - 3.f * mbr * r[k]));
     for (int c = 0; c < 6; ++c) atomicAdd(&vq32[6 * a + c], f5 * qb * rr[c]);
   }
@@ -1650,7 +1668,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   }
   for (int i = threadIdx.x; i < nat * nat; i += blockDim.x) {
     int a = i / nat, b = i % nat;
-    double c6g = 0.0, f3 = 0.0, f5 = 0.0, d3r = 0, d3r0 = 0, d5r = 0, d5r0 = 0;
+    double gd = 0.0, f3 = 0.0, f5 = 0.0, d3r = 0, d3r0 = 0, d5r = 0, d5r0 = 0;
     if (a != b) {
       int za = mv.Z[a], zb = mv.Z[b];
       int ga = md.atom_off + a, gb = md.atom_off + b;
@@ -1660,18 +1678,13 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         r2 += d * d;
       }
       double r = sqrt(r2);
-      double c6 = 0.0;
-      for (int ii = 0; ii < P.d4_nref[za]; ++ii)
-        for (int jj = 0; jj < P.d4_nref[zb]; ++jj)
-          c6 += bt.w4[ga * kMaxRef + ii] * bt.w4[gb * kMaxRef + jj] * c6ref(P, za, ii, zb, jj);
-      double g, dg;
-      bj_kernel(P, za, zb, r, g, dg);
-      c6g = c6 * g;
+      double dg;
+      bj_kernel(P, za, zb, r, gd, dg);
       double r0 = 0.5 * (bt.mrad[ga] + bt.mrad[gb]);
       mp_kernel(3, QCX_AES_A3, r, r0, f3, d3r, d3r0);
       mp_kernel(5, QCX_AES_A5, r, r0, f5, d5r, d5r0);
     }
-    vec[mv.vl.c6g + i] = c6g;
+    vec[mv.vl.gdisp + i] = gd;
     vec[mv.vl.f3 + i] = f3;
     vec[mv.vl.f5 + i] = f5;
     vec[mv.vl.d3r + i] = d3r;

