@@ -356,6 +356,30 @@ int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tad
                     const double* velof);
 
 /*
+ * Ground-state sampling file qcxms.gs, as md writes it during the sampling run
+ * (it = 0, src/md.f90:150-153, 379-385): the first line is nmax (list-directed,
+ * a blank and 11 columns), then one record per MD loop top, each a line per
+ * atom with x y z vx vy vz in Bohr and atomic units, format (6d16.8). xyz and
+ * vel are [nrec][nat][3].
+ */
+int qcx_write_gs(const char* path, int nmax, int nat, int nrec, const double* xyz, const double* vel);
+
+/*
+ * One line of the fragment results file qcxms.res, as manage_fragments writes
+ * it (src/write_fragments.f90:392-447, format (F10.7,i3,2i5,2i2,2x,i3,2x,
+ * 20(i4,i3))): the fragment's assigned charge fragchrg3, the charge mchrg,
+ * the trajectory number, for collision runs (cid != 0) the collision number,
+ * the secondary-fragmentation number isec, the fragment number, and its
+ * composition: nel elements in order of atomic number z[] with their counts
+ * count[] (fragmass, src/fragments.f90:10-84). Electron-impact records have
+ * no collision number, so the same format takes their items one position
+ * earlier, as the reference's output does. Writes a NUL-terminated line of at
+ * most len bytes and returns its length, or -1.
+ */
+int qcx_format_res(int cid, double fragchrg3, int mchrg, int itrj, int icoll, int isec, int ifrag, int nel,
+                   const int32_t* z, const int32_t* count, char* line, int len);
+
+/*
  * Allocation-free variant of qcx_egrad for callers that cannot call
  * cudaMalloc (for example a host program whose device memory belongs to
  * another runtime's capped pool, or a path that must not trigger the device

@@ -111,6 +111,9 @@ def load_library(build_if_missing=True):
     lib.qcx_write_start.argtypes = [ctypes.c_char_p, c_int, c_int, c_double, c_double, P(c_double), P(c_double)]
     lib.qcx_fragment_formula.argtypes = [c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double),
                                          P(ctypes.c_int32), P(c_double), ctypes.c_char_p]
+    lib.qcx_write_gs.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, P(c_double), P(c_double)]
+    lib.qcx_format_res.argtypes = [c_int, c_double, c_int, c_int, c_int, c_int, c_int, c_int, P(ctypes.c_int32),
+                                   P(ctypes.c_int32), ctypes.c_char_p, c_int]
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
     _lib = lib
     return lib
@@ -228,6 +231,34 @@ def fragment_formula(Z, frag, mass):
         raise RuntimeError(_err(lib))
     k = int(n[0])
     return fm[:k], [buf.raw[80 * i:80 * (i + 1)].split(b"\0")[0].decode() for i in range(k)]
+
+
+def write_gs(path, nmax, xyz, vel):
+    """qcxms.gs of a ground-state sampling run (src/md.f90:150-153, 379-385):
+    xyz and vel [nrec][nat][3] (Bohr, atomic units), one record per loop top."""
+    lib = load_library()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    vel = np.ascontiguousarray(vel, dtype=np.float64)
+    if xyz.ndim == 2:
+        xyz, vel = xyz[None], vel[None]
+    nrec, nat = xyz.shape[0], xyz.shape[1]
+    if lib.qcx_write_gs(os.fsencode(path), int(nmax), nat, nrec, _dp(xyz), _dp(vel)) != 0:
+        raise RuntimeError("qcx_write_gs failed: " + _err(lib))
+
+
+def format_res(fragchrg3, mchrg, itrj, isec, ifrag, Z, counts, icoll=None):
+    """One qcxms.res line (src/write_fragments.f90:392-447); icoll given for
+    collision runs. Z, counts: the fragment's elements in order of atomic
+    number and their counts."""
+    lib = load_library()
+    z = np.ascontiguousarray(Z, dtype=np.int32)
+    c = np.ascontiguousarray(counts, dtype=np.int32)
+    buf = ctypes.create_string_buffer(256)
+    n = lib.qcx_format_res(int(icoll is not None), float(fragchrg3), int(mchrg), int(itrj),
+                           int(icoll or 0), int(isec), int(ifrag), len(z), _ip(z), _ip(c), buf, 256)
+    if n < 0:
+        raise RuntimeError("qcx_format_res failed: " + _err(lib))
+    return buf.value.decode()
 
 
 def boltz(units, temp, ip):

@@ -95,26 +95,56 @@ int symbol_to_z(const std::string& tok) {
   return -1;
 }
 
-// Fortran Dw.d edit descriptor (w = 22, d = 14): 0.<14 digits>D<sign><2 digits>,
-// right-justified; the mantissa digits are the value rounded to 14 significant
-// digits (the round-to-nearest of printf's %.13E).
-std::string fortran_d22_14(double x) {
+// Fortran Dw.d edit descriptor: 0.<d digits>D<sign><2 digits>, right-justified
+// in w characters; the mantissa digits are the value rounded to d significant
+// digits (the round-to-nearest of printf's %.(d-1)E). A three-digit exponent
+// drops the D (0.<digits><sign><3 digits>); a field too narrow is w asterisks.
+std::string fortran_d(double x, int w, int d) {
   char buf[64];
   std::string out;
   if (x == 0.0) {
-    out = "0.00000000000000D+00";
+    out = "0." + std::string((size_t)d, '0') + "D+00";
   } else {
-    std::snprintf(buf, sizeof(buf), "%.13E", std::fabs(x));
+    std::snprintf(buf, sizeof(buf), "%.*E", d - 1, std::fabs(x));
     std::string m(buf);
     const size_t e = m.find('E');
     const int ex = std::atoi(m.c_str() + e + 1) + 1;
     std::string digits = m.substr(0, 1) + m.substr(2, e - 2);
     char tail[16];
-    std::snprintf(tail, sizeof(tail), "D%c%02d", ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
+    const int ax = ex < 0 ? -ex : ex;
+    if (ax <= 99) std::snprintf(tail, sizeof(tail), "D%c%02d", ex < 0 ? '-' : '+', ax);
+    else std::snprintf(tail, sizeof(tail), "%c%03d", ex < 0 ? '-' : '+', ax);
     out = std::string(x < 0 ? "-" : "") + "0." + digits + tail;
   }
-  if (out.size() < 22) out = std::string(22 - out.size(), ' ') + out;
+  if ((int)out.size() > w) return std::string((size_t)w, '*');
+  if ((int)out.size() < w) out = std::string((size_t)w - out.size(), ' ') + out;
   return out;
+}
+
+std::string fortran_d22_14(double x) { return fortran_d(x, 22, 14); }
+
+// Fortran Iw: right-justified, w asterisks when the number does not fit
+std::string fortran_i(long long v, int w) {
+  char buf[32];
+  std::snprintf(buf, sizeof(buf), "%lld", v);
+  std::string s(buf);
+  if ((int)s.size() > w) return std::string((size_t)w, '*');
+  return std::string((size_t)w - s.size(), ' ') + s;
+}
+
+// Fortran Fw.d (gfortran prints the leading zero of |x| < 1 when it fits)
+std::string fortran_f(double x, int w, int d) {
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "%*.*f", w, d, x);
+  std::string s(buf);
+  if ((int)s.size() > w) {
+    // without the optional leading zero, if that makes it fit
+    size_t z = s.find("0.");
+    if (z != std::string::npos && (z == 0 || s[z - 1] == '-' || s[z - 1] == ' ') && (int)s.size() - 1 <= w)
+      s.erase(z, 1);
+    if ((int)s.size() > w) return std::string((size_t)w, '*');
+  }
+  return s;
 }
 
 }  // namespace
@@ -139,6 +169,67 @@ int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tad
   const bool ok = std::fclose(f) == 0;
   if (!ok) qcx::set_last_error(std::string("qcx_write_start: write error on ") + path);
   return ok ? 0 : -1;
+}
+
+int qcx_write_gs(const char* path, int nmax, int nat, int nrec, const double* xyz, const double* vel) {
+  if (!path || nat < 1 || nrec < 0 || (nrec > 0 && (!xyz || !vel))) {
+    qcx::set_last_error("qcx_write_gs: invalid arguments (nat >= 1, nrec >= 0, xyz and vel)");
+    return -1;
+  }
+  FILE* f = std::fopen(path, "w");
+  if (!f) {
+    qcx::set_last_error(std::string("qcx_write_gs: cannot write ") + path);
+    return -1;
+  }
+  // write(io_GS,*) nmax: list-directed, a blank and the integer in 11 columns
+  std::fprintf(f, " %11d\n", nmax);
+  for (long long r = 0; r < nrec; ++r)
+    for (int a = 0; a < nat; ++a) {
+      const double* x = xyz + (r * nat + a) * 3;
+      const double* v = vel + (r * nat + a) * 3;
+      std::string line;
+      for (int k = 0; k < 3; ++k) line += fortran_d(x[k], 16, 8);
+      for (int k = 0; k < 3; ++k) line += fortran_d(v[k], 16, 8);
+      std::fprintf(f, "%s\n", line.c_str());
+    }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) qcx::set_last_error(std::string("qcx_write_gs: write error on ") + path);
+  return ok ? 0 : -1;
+}
+
+int qcx_format_res(int cid, double fragchrg3, int mchrg, int itrj, int icoll, int isec, int ifrag, int nel,
+                   const int32_t* z, const int32_t* count, char* line, int len) {
+  if (!line || len < 1 || nel < 0 || nel > 20 || (nel > 0 && (!z || !count))) {
+    qcx::set_last_error("qcx_format_res: invalid arguments (0 <= nel <= 20, z and count, an output buffer)");
+    return -1;
+  }
+  // items in the order of the write statement; the edit descriptors
+  // F10.7, i3, 2i5, 2i2, 2x, i3, 2x, 20(i4, i3) take them in turn
+  std::vector<long long> items;
+  items.push_back(mchrg);
+  items.push_back(itrj);
+  if (cid) items.push_back(icoll);
+  items.push_back(isec);
+  items.push_back(ifrag);
+  items.push_back(nel);
+  for (int m = 0; m < nel; ++m) {
+    items.push_back(z[m]);
+    items.push_back(count[m]);
+  }
+  static const int kWidth[] = {3, 5, 5, 2, 2, 3};  // i3, 2i5, 2i2, 2x, i3
+  std::string out = fortran_f(fragchrg3, 10, 7);
+  for (size_t k = 0; k < items.size(); ++k) {
+    if (k == 5) out += "  ";                 // the 2x before i3
+    if (k == 6) out += "  ";                 // the 2x after it
+    const int w = k < 6 ? kWidth[k] : ((k - 6) % 2 == 0 ? 4 : 3);
+    out += fortran_i(items[k], w);
+  }
+  if ((int)out.size() + 1 > len) {
+    qcx::set_last_error("qcx_format_res: output buffer too small");
+    return -1;
+  }
+  std::memcpy(line, out.c_str(), out.size() + 1);
+  return (int)out.size();
 }
 
 int qcx_read_xyz(const char* path, int max_nat, int32_t* nat, int32_t* num, double* xyz) {

@@ -110,3 +110,57 @@ def test_gpu_driver_runs_ensemble_to_the_end(gpu):
         # trajectories that ended in fragments carry their IPs
         assert ("fragip_eV" in t) == (2 <= t["nfrag"] <= 10)
     assert any(t["nstep"] == 30 and t["mdok"] for t in res)
+
+
+# --- output files: qcxms.gs and qcxms.res lines ---------------------------------
+
+def _fortran_d(x, w, d):
+    """Fortran Dw.d restated with Python's decimal formatting (independent of the
+    library's printf-based one): 0.<d digits>D<sign><2 digits>, right-justified."""
+    if x == 0.0:
+        s = "0." + "0" * d + "D+00"
+    else:
+        m = "%.*e" % (d - 1, abs(x))
+        mant, ex = m.split("e")
+        e = int(ex) + 1
+        s = ("-" if x < 0 else "") + "0." + mant.replace(".", "") + ("D%+03d" % e if abs(e) <= 99 else "%+04d" % e)
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def test_gs_file_bytes(tmp_path):
+    """qcxms.gs: list-directed nmax, then (6d16.8) lines per atom and record
+    (src/md.f90:150-153, 379-385). Known answers written out by hand, then a
+    random record against the Python restatement of D16.8."""
+    p = tmp_path / "qcxms.gs"
+    xyz = np.array([[[1.5, -0.000123456789, 0.0]]])
+    vel = np.array([[[2.5e-4, -1.0, 123456.789]]])
+    qg.write_gs(str(p), 4000, xyz, vel)
+    lines = p.read_text().split("\n")
+    assert lines[0] == "        4000"
+    assert lines[1] == ("  0.15000000D+01 -0.12345679D-03  0.00000000D+00"
+                        "  0.25000000D-03 -0.10000000D+01  0.12345679D+06")
+    rng = np.random.default_rng(4)
+    xyz = rng.normal(scale=5.0, size=(3, 7, 3))
+    vel = rng.normal(scale=3e-4, size=(3, 7, 3))
+    qg.write_gs(str(p), 2, xyz, vel)
+    lines = p.read_text().split("\n")
+    assert lines[0] == "           2" and len(lines) == 1 + 21 + 1 and lines[-1] == ""
+    for r in range(3):
+        for a in range(7):
+            want = "".join(_fortran_d(v, 16, 8) for v in list(xyz[r, a]) + list(vel[r, a]))
+            assert lines[1 + 7 * r + a] == want
+
+
+def test_res_line_bytes():
+    """qcxms.res lines, format (F10.7,i3,2i5,2i2,2x,i3,2x,20(i4,i3))
+    (src/write_fragments.f90:392-447). Electron-impact records have no collision
+    number, so their items take the edit descriptors one position earlier."""
+    # EI: fragment 2 of trajectory 17 (isec 1), C2H4O1, assigned charge 0.75
+    line = qg.format_res(0.75, 1, 17, 1, 2, [1, 6, 8], [4, 2, 1])
+    assert line == " 0.7500000  1   17    1 2 3    1     4  6   2  8   1"
+    # CID: collision 3 of trajectory 123, fragment 1, C6H5 with charge 1
+    line = qg.format_res(1.0, 1, 123, 1, 1, [1, 6], [5, 6], icoll=3)
+    assert line == " 1.0000000  1  123    3 1 1    2     1  5   6  6"
+    # negative charges, a number too wide for its field
+    line = qg.format_res(-0.4999999, -1, 123456, 2, 10, [7], [1])
+    assert line == "-0.4999999 -1*****    210 1    7     1"
