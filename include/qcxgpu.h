@@ -356,6 +356,18 @@ int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tad
                     const double* velof);
 
 /*
+ * Self-check of the tensor-core product the SCC kernel uses (no counterpart in
+ * the reference): one CTA computes C[M][N] = op(A) op(B) on the tcgen05 tensor
+ * cores as split-TF32 (about 21 significant bits), reps times, from host
+ * matrices. op(A) = A [M][K] (ta = 0) or A^T with A [K][M] (ta = 1); op(B) =
+ * B [K][N] (tb = 0) or B^T with B [N][K] (tb = 1). M <= 128, N <= 256.
+ * *ms (may be NULL) gets the kernel time. Returns 0, -1 (invalid arguments or
+ * a CUDA error) or -2 (the completion wait ran out).
+ */
+int qcx_mma_selftest(int M, int N, int K, const float* A, int ta, const float* B, int tb, float* C, int reps,
+                     float* ms);
+
+/*
  * Ground-state sampling file qcxms.gs, as md writes it during the sampling run
  * (it = 0, src/md.f90:150-153, 379-385): the first line is nmax (list-directed,
  * a blank and 11 columns), then one record per MD loop top, each a line per

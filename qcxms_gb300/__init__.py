@@ -76,6 +76,8 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_egrad.argtypes = [ctypes.c_void_p]
     lib.qcx_batch_set_timing.argtypes = [ctypes.c_void_p, c_int]
     lib.qcx_batch_get_timing.argtypes = [ctypes.c_void_p, P(ctypes.c_float), c_int]
+    lib.qcx_mma_selftest.argtypes = [c_int, c_int, c_int, P(ctypes.c_float), c_int, P(ctypes.c_float), c_int,
+                                     P(ctypes.c_float), c_int, P(ctypes.c_float)]
     lib.qcx_checkqc.argtypes = [c_int, P(c_double), P(c_double), c_int, P(c_double)]
     lib.qcx_batch_load_state.argtypes = [ctypes.c_void_p, P(c_double), P(c_double)]
     lib.qcx_batch_step.argtypes = [ctypes.c_void_p, c_int, c_double]
@@ -271,6 +273,25 @@ def boltz(units, temp, ip):
     if rc != 0:
         raise RuntimeError("qcx_boltz: %s" % _err(lib))
     return out
+
+
+def mma_gemm(A, B, ta=False, tb=False, reps=1):
+    """The tensor-core (tcgen05, split-TF32) product of the SCC kernel on one
+    CTA: returns (C, kernel ms). A is [M][K] (or [K][M] with ta), B [K][N] (or
+    [N][K] with tb)."""
+    lib = load_library()
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    M = A.shape[1] if ta else A.shape[0]
+    K = A.shape[0] if ta else A.shape[1]
+    N = B.shape[0] if tb else B.shape[1]
+    C = np.zeros((M, N), dtype=np.float32)
+    ms = ctypes.c_float()
+    fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    rc = lib.qcx_mma_selftest(M, N, K, fp(A), int(ta), fp(B), int(tb), fp(C), int(reps), ctypes.byref(ms))
+    if rc != 0:
+        raise RuntimeError("qcx_mma_selftest returned %d: %s" % (rc, _err(lib)))
+    return C, ms.value
 
 
 def checkqc(energy, grad, qat, charge):

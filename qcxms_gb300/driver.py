@@ -13,31 +13,44 @@ rules) and, when the ion has fragmented, the fragment IPs of ``analyse``
 
 As in the reference, the IPs use the structure averaged over the last steps
 (``axyz``, ``src/md.f90:352-362, 695``) with the fragment numbers of the final
-structure. Differences from the reference: the electronic
-temperature is the one given (the reference's default, ``ieetemp = 0``, gives
-the constant 5000 + 20000 ax); the charge assignment of ``write_fragments``
-and the output files are not written.
+structure, and the electronic temperature follows ``setetemp`` after every step
+(``src/md.f90:443-446``): 5000 + 20000 ax (+ eimp ieetemp while heating). With
+``--etemp`` given, the start's evaluation runs at that temperature
+(``src/md.f90:167-171``); without it at ``setetemp(1, eimp)``.
 
-Usage: ``python -m qcxms_gb300.driver TMPQCXMS --etemp 17000 --max-steps 10000``
+Results: one JSON record per trajectory, and ``qcxms.res`` lines
+(``qcx_format_res``) for the fragments of trajectories that ended in 2-10
+fragments. Their charges come from the Boltzmann weights of the fragment IPs
+(``boltz``, ``src/utility.f90:469-498``) at the trajectory's mean temperature:
+the reference's own assignment (``src/write_fragments.f90:116-121``) reads
+``fragip(i,0)``, outside its array, so its numbers are not reproducible.
+
+Usage: ``python -m qcxms_gb300.driver TMPQCXMS --max-steps 10000 --res qcxms.res``
 """
 import argparse
 import json
 
 import numpy as np
 
-from . import Batch, constants, fragment_formula, fragment_ips, read_ensemble
+from . import Batch, boltz, constants, format_res, fragment_formula, fragment_ips, read_ensemble
 
 
-def run_ensemble(root, etemp, charge=1, nfragexit=2, more=250, max_steps=10000, tstep_fs=0.5, block=100,
-                 precision="mixed", ip_precision=0, ip_etemp=300.0):
-    """Run every trajectory of ``root`` to its end; returns one dict per trajectory."""
+def run_ensemble(root, etemp=-1.0, charge=1, nfragexit=2, more=250, max_steps=10000, tstep_fs=0.5, block=100,
+                 precision="mixed", ip_precision=0, ip_etemp=300.0, ax=0.0, ieetemp=0.0):
+    """Run every trajectory of ``root`` to its end; returns one dict per trajectory.
+    etemp > 0: the start's electronic temperature; otherwise setetemp's."""
     mols = read_ensemble(root, charge=charge)
     dt = tstep_fs * constants.FSTOAU
-    b = Batch(mols, etemp=etemp)
+    b = Batch(mols, etemp=etemp if etemp > 0 else 5000.0)
     b.set_precision(precision)
-    b.egrad()
     b.set_md_heating([m["eimp"] for m in mols], [m["tadd"] for m in mols], dt,
                      np.concatenate([m["velof"] for m in mols]))
+    if etemp > 0:
+        b.egrad()
+        b.set_md_etemp(ax, ieetemp)  # later evaluations follow setetemp
+    else:
+        b.set_md_etemp(ax, ieetemp)  # the start too
+        b.egrad()
     b.set_md_rules(nfragexit, more, max_steps)
     while True:
         active, _ = b.progress()
@@ -71,20 +84,70 @@ def run_ensemble(root, etemp, charge=1, nfragexit=2, more=250, max_steps=10000, 
         for k, (i, _) in enumerate(ends):
             out[i]["fragip_eV"] = ip[k][:, 0].tolist()
             out[i]["ipok"] = bool(ok[k])
+            tmean = float(st["tav"][i]) / max(1, int(st["nstep"][i]))
+            q = boltz(2, tmean, ip[k][:, :1])[:, 0] if ok[k] else np.zeros(len(out[i]["formula"]))
+            out[i]["fragchrg"] = q.tolist()
+            res = []
+            for j in range(out[i]["nfrag"]):
+                zs = [z for z in range(1, 19) if np.any((np.asarray(mols[i]["Z"]) == z) &
+                                                        (np.asarray(out[i]["frag"]) == j + 1))]
+                cnt = [int(np.sum((np.asarray(mols[i]["Z"]) == z) & (np.asarray(out[i]["frag"]) == j + 1)))
+                       for z in zs]
+                res.append(format_res(q[j], charge, out[i]["itrj"], 1, j + 1, zs, cnt))
+            out[i]["res_lines"] = res
     return out
+
+
+def gs_sampling(mols, nmax, path_fmt, etemp=298.15, tstep_fs=0.5, precision="fp64"):
+    """Ground-state sampling run of every molecule (md with it = 0: NVE, the
+    etemp of the ground-state runs, src/input.f90:142), writing path_fmt % i as
+    qcxms.gs: nmax, then the coordinates and velocities at each of the nmax
+    loop tops (the state before each step, src/md.f90:379-385). Returns the
+    number of records written per molecule (fewer when a run stops)."""
+    from . import write_gs
+    dt = tstep_fs * constants.FSTOAU
+    b = Batch(mols, etemp=etemp)
+    b.set_precision(precision)
+    b.egrad()
+    xs, vs = [], []
+    nrec = np.zeros(b.nmol, dtype=int)
+    for k in range(nmax):
+        r = b.get()
+        active, _ = b.progress()
+        xs.append(b.split(r["xyz"]))
+        vs.append(b.split(r["vel"]))
+        nrec += active > 0
+        if not active.any():
+            break
+        b.step(1, dt)
+    b.close()
+    for i in range(len(mols)):
+        n = int(nrec[i])
+        write_gs(path_fmt % i, nmax, np.array([xs[k][i] for k in range(n)]), np.array([vs[k][i] for k in range(n)]))
+    return nrec.tolist()
 
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("root", help="ensemble directory holding TMP.n/start.xyz and TMP.n/qcxms.start")
-    ap.add_argument("--etemp", type=float, required=True, help="electronic temperature (K)")
+    ap.add_argument("--etemp", type=float, default=-1.0,
+                    help="electronic temperature of the start (K); default: setetemp's, 5000 + 20000 ax")
+    ap.add_argument("--ax", type=float, default=0.0)
+    ap.add_argument("--ieetemp", type=float, default=0.0)
+    ap.add_argument("--res", default=None, help="write the qcxms.res lines here")
     ap.add_argument("--charge", type=int, default=1)
     ap.add_argument("--nfragexit", type=int, default=2)
     ap.add_argument("--max-steps", type=int, default=10000)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--out", default=None, help="write the results as JSON here")
     a = ap.parse_args()
-    res = run_ensemble(a.root, a.etemp, a.charge, a.nfragexit, max_steps=a.max_steps, precision=a.precision)
+    res = run_ensemble(a.root, a.etemp, a.charge, a.nfragexit, max_steps=a.max_steps, precision=a.precision,
+                       ax=a.ax, ieetemp=a.ieetemp)
+    if a.res:
+        with open(a.res, "w") as f:
+            for t in res:
+                for line in t.get("res_lines", []):
+                    f.write(line + "\n")
     for t in res:
         print("traj %5d  mdok %d  fragstate %d  steps %6d  fragments %d  %s  IPs %s" %
               (t["itrj"], t["mdok"], t["fragstate"], t["nstep"], t["nfrag"], " ".join(t.get("formula", [])),

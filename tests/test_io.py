@@ -107,8 +107,11 @@ def test_gpu_driver_runs_ensemble_to_the_end(gpu):
     assert [t["itrj"] for t in res] == [1, 2, 10]
     for t in res:
         assert 1 <= t["nstep"] <= 30 and len(t["frag"]) > 0
-        # trajectories that ended in fragments carry their IPs
+        # trajectories that ended in fragments carry their IPs and qcxms.res lines
         assert ("fragip_eV" in t) == (2 <= t["nfrag"] <= 10)
+        if "fragip_eV" in t:
+            assert len(t["res_lines"]) == t["nfrag"]
+            assert abs(sum(float(line[:10]) for line in t["res_lines"]) - 1.0) < 1e-6 or not t["ipok"]
     assert any(t["nstep"] == 30 and t["mdok"] for t in res)
 
 
@@ -164,3 +167,19 @@ def test_res_line_bytes():
     # negative charges, a number too wide for its field
     line = qg.format_res(-0.4999999, -1, 123456, 2, 10, [7], [1])
     assert line == "-0.4999999 -1*****    210 1    7     1"
+
+
+@pytest.mark.gpu
+def test_gpu_gs_sampling_writes_qcxms_gs(gpu, tmp_path):
+    """A ground-state sampling run writes qcxms.gs: nmax, then one record of
+    (6d16.8) lines per loop top; the first record is the start geometry."""
+    from qcxms_gb300 import driver, molgen
+    Z, xyz = molgen.c6h12o2()
+    vel = molgen.maxwell_boltzmann(Z, 300.0, 5)
+    mols = [{"Z": Z, "xyz": xyz, "vel": vel, "mass": molgen.masses(Z), "charge": 0}]
+    nrec = driver.gs_sampling(mols, 4, str(tmp_path / "gs.%d"))
+    assert nrec == [4]
+    lines = (tmp_path / "gs.0").read_text().split("\n")
+    assert lines[0] == "           4" and len(lines) == 1 + 4 * len(Z) + 1
+    first = lines[1].split()
+    assert abs(float(first[0].replace("D", "E")) - xyz[0][0]) < 1e-7 * max(1.0, abs(xyz[0][0]))
