@@ -360,7 +360,7 @@ int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tad
  * the reference): one CTA computes C[M][N] = op(A) op(B) on the tcgen05 tensor
  * cores as split-TF32 (about 21 significant bits), reps times, from host
  * matrices. op(A) = A [M][K] (ta = 0) or A^T with A [K][M] (ta = 1); op(B) =
- * B [K][N] (tb = 0) or B^T with B [N][K] (tb = 1). M <= 128, N <= 256.
+ * B [K][N] (tb = 0) or B^T with B [N][K] (tb = 1). M <= 512, N <= 256.
  * *ms (may be NULL) gets the kernel time. Returns 0, -1 (invalid arguments or
  * a CUDA error) or -2 (the completion wait ran out).
  */

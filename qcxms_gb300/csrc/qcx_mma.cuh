@@ -1,16 +1,16 @@
 // CTA-wide GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// C[M][N] = A[M][K] * B[K][N] for M <= 128, N <= 256, any K, FP32 in and out,
+// C[M][N] = A[M][K] * B[K][N] for N <= 256, any M and K (tiles of 128 rows), FP32 in and out,
 // computed as split-TF32: every operand is split into a TF32 head and an FP32
 // tail (x = hi + lo, lo exact), and the product accumulates hi*hi + hi*lo + lo*hi
 // (the lo*lo term is below FP32 rounding) in FP32 in tensor memory. The result
 // carries about 21 significant bits, which is what the FP32 SCC iterations need.
 //
-// Operands are staged chunk by chunk (32 values of K) into shared memory in the
+// Operands are staged chunk by chunk (16 values of K) into shared memory in the
 // canonical K-major layout without swizzle: core matrices of 8 rows x 16 bytes
 // (4 TF32 values), the next core matrix along K 128 bytes on (leading byte
-// offset), the next group of 8 rows 1024 bytes on (stride byte offset). One
-// elected thread issues tcgen05.mma.cta_group::1.kind::tf32 for the 4 K-steps
+// offset), the next group of 8 rows 512 bytes on (stride byte offset). One
+// elected thread issues tcgen05.mma.cta_group::1.kind::tf32 for the 2 K-steps
 // of 8 and the 3 split products, commits to an mbarrier, and every thread waits
 // on it with a bounded number of polls. The accumulator (128 lanes x N columns)
 // is read back with tcgen05.ld by the first four warps' lane quarters.
@@ -19,8 +19,8 @@
 
 namespace qcx {
 
-// staging bytes for one K chunk: A hi/lo (128 x 32) and B hi/lo (nmax x 32)
-constexpr int kMmaKc = 32;
+// staging bytes for one K chunk: A hi/lo (128 x 16) and B hi/lo (nmax x 16)
+constexpr int kMmaKc = 16;
 __host__ __device__ constexpr int mma_stage_bytes(int nmax) { return 2 * 128 * kMmaKc * 4 + 2 * nmax * kMmaKc * 4; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -114,7 +114,7 @@ __device__ __forceinline__ int mma_off(int r, int k) {
 // B(k,j) = tb ? B[j*ldb + k] : B[k*ldb + j]; C row-major (ldc), M <= 128,
 // N <= 256. All threads call it; blockDim.x must be a multiple of 128.
 template <typename TA, typename TB>
-__device__ void mma_gemm_tf32(MmaCtx& c, int M, int N, int K, const TA* A, int lda, bool ta, const TB* B, int ldb,
+__device__ void mma_gemm_tile(MmaCtx& c, int M, int N, int K, const TA* A, int lda, bool ta, const TB* B, int ldb,
                               bool tb, float* C, int ldc) {
   const int Np = (N + 15) & ~15;  // N multiple of 16 for M = 128
   float* a_hi = (float*)c.stage;
@@ -198,6 +198,17 @@ __device__ void mma_gemm_tf32(MmaCtx& c, int M, int N, int K, const TA* A, int l
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
+}
+
+// C = op(A) op(B) for any M: tiles of 128 rows of op(A) and C
+template <typename TA, typename TB>
+__device__ void mma_gemm_tf32(MmaCtx& c, int M, int N, int K, const TA* A, int lda, bool ta, const TB* B, int ldb,
+                              bool tb, float* C, int ldc) {
+  for (int m0 = 0; m0 < M; m0 += 128) {
+    const int mt = M - m0 < 128 ? M - m0 : 128;
+    const TA* Am = ta ? A + m0 : A + (long long)m0 * lda;
+    mma_gemm_tile(c, mt, N, K, Am, lda, ta, B, ldb, tb, C + (long long)m0 * ldc, ldc);
+  }
 }
 
 }  // namespace qcx

@@ -33,8 +33,8 @@ __global__ void __launch_bounds__(kMmaTestThreads) k_mma_selftest(int M, int N, 
 extern "C" int qcx_mma_selftest(int M, int N, int K, const float* A, int ta, const float* B, int tb, float* C,
                                 int reps, float* ms) {
   using namespace qcx;
-  if (M < 1 || M > 128 || N < 1 || N > 256 || K < 1 || !A || !B || !C || reps < 1) {
-    set_last_error("qcx_mma_selftest: 1 <= M <= 128, 1 <= N <= 256, K >= 1, reps >= 1");
+  if (M < 1 || M > 512 || N < 1 || N > 256 || K < 1 || !A || !B || !C || reps < 1) {
+    set_last_error("qcx_mma_selftest: 1 <= M <= 512, 1 <= N <= 256, K >= 1, reps >= 1");
     return -1;
   }
   float *dA = nullptr, *dB = nullptr, *dC = nullptr;

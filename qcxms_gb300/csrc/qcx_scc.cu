@@ -16,6 +16,7 @@
 
 #include "qcx_batch.cuh"
 #include "qcx_kernels.h"
+#include "qcx_mma.cuh"
 
 namespace qcx {
 
@@ -66,6 +67,11 @@ namespace qcx {
 #endif
 #ifndef QCX_HARD_ROUNDS
 #define QCX_HARD_ROUNDS 6
+#endif
+// FP32 products of the FP32 iterations on the tcgen05 tensor cores (split-TF32)
+// when the CTA has room to stage them; 0: CUDA cores only
+#ifndef QCX_SCC_MMA
+#define QCX_SCC_MMA 1
 #endif
 constexpr int kSccThreads = QCX_SCC_THREADS;
 constexpr int kWarps = kSccThreads / 32;
@@ -144,6 +150,21 @@ __device__ void cta_gemm(int M, int N, int K, const TA* A, int lda, bool ta, con
   }
 }
 
+// Products of the FP32 iterations: on the tensor cores (qcx_mma.cuh, split-TF32)
+// when the CTA holds a tcgen05 context, else on the CUDA cores. FP64 products
+// always take the CUDA cores.
+template <typename T>
+__device__ __forceinline__ void gemm_t(MmaCtx* mc, int M, int N, int K, const T* A, int lda, bool ta, const T* B,
+                                       int ldb, bool tb, T* C, int ldc) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (mc) {
+      mma_gemm_tf32(*mc, M, N, K, A, lda, ta, B, ldb, tb, C, ldc);
+      return;
+    }
+  }
+  cta_gemm<T, T, T, T>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc);
+}
+
 // ---------------------------------------------------------------------------
 // shared-memory layout
 // ---------------------------------------------------------------------------
@@ -195,7 +216,9 @@ size_t scc_smem_bytes(int max_nao, int precision) {
   (void)precision;
   int n = max_nao;
   int np = n + (n & 1);
-  size_t want = scc_fixed_bytes(n) + 2 * sizeof(double) * (size_t)np * np;
+  // both Jacobi matrices, then the staging buffer of the tensor-core products
+  size_t want = ((scc_fixed_bytes(n) + 2 * sizeof(double) * (size_t)np * np + 127) & ~(size_t)127) +
+                (size_t)mma_stage_bytes((n + 15) & ~15);
   return want < kSmemCap ? want : kSmemCap;
 }
 
@@ -1167,15 +1190,15 @@ __device__ int rotate_hard_pairs(T* JA, T* JV, const T* Km, int n, T khard, SccS
 template <typename T>
 __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, double* tmp, int n,
                        double kfail, double ktol, int max_pass, double ns_min, SccShared& sh,
-                       double mu = 0.0, double occ_gap = -1.0) {
+                       double mu = 0.0, double occ_gap = -1.0, MmaCtx* mc = nullptr) {
   const int np = n + (n & 1);
   int hard = 0;       // rounds of exact rotations so far
   bool fresh = true;  // JA holds B for the current rows of JV
   for (int pass = 0; pass < max_pass; ++pass) {
     if (pass > 0 && !fresh) {
-      cta_gemm<T, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
+      gemm_t<T>(mc, n, n, n, F, n, false, JV, np, true, Tm, n);
       __syncthreads();
-      cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, JA, np);
+      gemm_t<T>(mc, n, n, n, JV, np, false, Tm, n, false, JA, np);
       __syncthreads();
     }
     fresh = false;
@@ -1238,7 +1261,7 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
     for (int j = threadIdx.x; j < n; j += blockDim.x) JA[j * np + j] = lamv[j];
     if (kmax == 0.0) return true;
     // C^T <- C^T + K^T C^T
-    cta_gemm<T, T, T, T>(n, n, n, Tm, n, false, JV, np, false, Cm, n);
+    gemm_t<T>(mc, n, n, n, Tm, n, false, JV, np, false, Cm, n);
     __syncthreads();
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] += Cm[e];
     __syncthreads();
@@ -1255,9 +1278,9 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
     // predicted from the measured one (3/4 n E^2) is at FP32 rounding level.
     const int ns_steps = sizeof(T) == 4 ? 3 : 1;
     for (int st = 0; st < ns_steps; ++st) {
-      cta_gemm<T, T, T, T>(n, n, n, S, n, false, JV, np, true, Tm, n);
+      gemm_t<T>(mc, n, n, n, S, n, false, JV, np, true, Tm, n);
       __syncthreads();
-      cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, Cm, n);
+      gemm_t<T>(mc, n, n, n, JV, np, false, Tm, n, false, Cm, n);
       __syncthreads();
       T emax_t = T(0);
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -1269,7 +1292,7 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
       }
       double emax = ns_steps > 1 ? cta_max((double)emax_t, sh.red) : 0.0;
       __syncthreads();
-      cta_gemm<T, T, T, T>(n, n, n, Cm, n, false, JV, np, false, Tm, n);
+      gemm_t<T>(mc, n, n, n, Cm, n, false, JV, np, false, Tm, n);
       __syncthreads();
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = Tm[e];
       __syncthreads();
@@ -1279,9 +1302,9 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
     if (kmax < ktol) return true;
   }
   // passes exhausted: recompute B in the final basis for the caller's Jacobi
-  cta_gemm<T, T, T, T>(n, n, n, F, n, false, JV, np, true, Tm, n);
+  gemm_t<T>(mc, n, n, n, F, n, false, JV, np, true, Tm, n);
   __syncthreads();
-  cta_gemm<T, T, T, T>(n, n, n, JV, np, false, Tm, n, false, JA, np);
+  gemm_t<T>(mc, n, n, n, JV, np, false, Tm, n, false, JA, np);
   __syncthreads();
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int i = e / n, j = e % n;
@@ -1640,6 +1663,28 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   float* JV32 = a32_shared ? (float*)Ag : (float*)JA + (long long)np * np;
   float* T32 = (float*)T;
   float* X32 = (float*)Wm;
+  // Tensor-core context of the FP32 iterations (mixed mode): the staging buffer
+  // of the operands goes after this molecule's part of shared memory when it
+  // fits there, else (both FP64 Jacobi matrices in shared memory) into the
+  // FP64 coefficient matrix, which the FP32 iterations leave unused.
+  __shared__ uint32_t mma_tmem_slot;
+  __shared__ __align__(8) uint64_t mma_bar;
+  MmaCtx mctx;
+  MmaCtx* mc = nullptr;
+  if (MIXED && QCX_SCC_MMA) {
+    const size_t jac_used = mode == 0 ? 2 * sizeof(double) * (size_t)np * np
+                                      : mode == 1 ? sizeof(double) * (size_t)np * np
+                                                  : (a32_shared ? sizeof(float) * (size_t)np * np : 0);
+    const size_t need = (size_t)mma_stage_bytes((n + 15) & ~15);
+    const size_t tail = (scc_fixed_bytes(n) + jac_used + 127) & ~(size_t)127;
+    char* stage = nullptr;
+    if (tail + need <= (size_t)bt.smem_bytes) stage = smem_raw + tail;
+    else if (mode == 0 && sizeof(double) * (size_t)np * np >= need) stage = (char*)JV;
+    if (stage) {
+      mma_setup(mctx, &mma_tmem_slot, &mma_bar, stage);
+      mc = &mctx;
+    }
+  }
 
   // --- per-AO maps -------------------------------------------------------
   const int* sh_atom = bt.sh_atom + md.sh_off;
@@ -1720,6 +1765,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       bt.iters[mol] = 0;
       if (bt.have_prev) bt.have_prev[mol] = 0;
     }
+    if (mc) mma_teardown(mctx);
     return;
   }
   // X = L^-T: row j of X = column j of L^-1, one forward substitution per thread
@@ -1898,9 +1944,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         __syncthreads();
         float* C32 = (float*)C;
         for (int st = 0; st < 2; ++st) {
-          cta_gemm<float, float, float, float>(n, n, n, S32, n, false, JV32, np, true, T32, n);
+          gemm_t<float>(mc, n, n, n, S32, n, false, JV32, np, true, T32, n);
           __syncthreads();
-          cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, T32, n, false, C32, n);
+          gemm_t<float>(mc, n, n, n, JV32, np, false, T32, n, false, C32, n);
           __syncthreads();
           float em = 0.f;
           for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -1911,7 +1957,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
           }
           const double emax = cta_max((double)em, sh.red);
           if (st == 0 && !(emax < 0.25)) break;  // too far from the new metric: start from scratch
-          cta_gemm<float, float, float, float>(n, n, n, C32, n, false, JV32, np, false, T32, n);
+          gemm_t<float>(mc, n, n, n, C32, n, false, JV32, np, false, T32, n);
           __syncthreads();
           for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV32[(e / n) * np + (e % n)] = T32[e];
           __syncthreads();
@@ -1919,9 +1965,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         }
       }
       if (!have32 && !seeded) {
-        cta_gemm<float, float, float, float>(n, n, n, (const float*)F, n, false, X32, n, false, T32, n);
+        gemm_t<float>(mc, n, n, n, (const float*)F, n, false, X32, n, false, T32, n);
         __syncthreads();
-        cta_gemm<float, float, float, float>(n, n, n, X32, n, true, T32, n, false, JA32, np);
+        gemm_t<float>(mc, n, n, n, X32, n, true, T32, n, false, JA32, np);
         __syncthreads();
       } else {
         // B = V F V^T with V^T copied out first (the FP64 X slot is free in
@@ -1932,9 +1978,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
           Vt32[e] = JV32[j * np + k];
         }
         __syncthreads();
-        cta_gemm<float, float, float, float>(n, n, n, (const float*)F, n, false, Vt32, n, false, T32, n);
+        gemm_t<float>(mc, n, n, n, (const float*)F, n, false, Vt32, n, false, T32, n);
         __syncthreads();
-        cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, T32, n, false, JA32, np);
+        gemm_t<float>(mc, n, n, n, JV32, np, false, T32, n, false, JA32, np);
         __syncthreads();
       }
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -1953,7 +1999,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       if (backoff32 > 0) --backoff32;
       bool ok32 = try32 &&
                   refine<float>(JA32, JV32, (const float*)F, S32, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, QCX_REFINE32_KTOL,
-                                QCX_REFINE32_PASSES, 1e-3, sh, efermi, 25.0 * md.kT);
+                                QCX_REFINE32_PASSES, 1e-3, sh, efermi, 25.0 * md.kT, mc);
       PHASE_MARK(16);
       if (try32 && !ok32) backoff32 = QCX_REFINE32_BACKOFF;
       // the first (cold) solve only seeds the FP32 iterations: it stops at a
@@ -1968,7 +2014,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       if (!have32) {
         if (!seeded) {
           // eigenvectors of X^T F X -> C^T = V X^T
-          cta_gemm<float, float, float, float>(n, n, n, JV32, np, false, X32, n, true, T32, n);
+          gemm_t<float>(mc, n, n, n, JV32, np, false, X32, n, true, T32, n);
           __syncthreads();
           for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV32[(e / n) * np + (e % n)] = T32[e];
           __syncthreads();
@@ -2185,7 +2231,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         Vo32[e] = v;
       }
       __syncthreads();
-      cta_gemm<float, float, float, float>(n, n, nocc, G32, n, true, Vo32, n, false, P32, n);
+      gemm_t<float>(mc, n, n, nocc, G32, n, true, Vo32, n, false, P32, n);
     } else if (MIXED && have32) {
       dd_density(dm, n, nocc, sh.perm, focc, Pm, sh);
     } else {
@@ -2350,11 +2396,13 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     int st = 0;
     if (!converged) st |= kSccNotConverged;
     if (eig_fail) st |= kEigenNotConverged;
+    if (mc && !mctx.ok) st |= kEigenNotConverged | kNonFinite;  // a tensor-core wait ran out
     if (!isfinite(eel)) st |= kNonFinite;
     bt.status[mol] = st;
     if (bt.have_prev) bt.have_prev[mol] = (st == 0 ? 1 : 0) | (basis_saved ? 2 : 0);
     bt.iters[mol] = it;
   }
+  if (mc) mma_teardown(mctx);
 }
 
 #ifdef QCX_SCC_PHASE_TIMING

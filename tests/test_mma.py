@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("M,N,K,ta,tb", [(8, 16, 8, 0, 0), (37, 41, 53, 0, 0), (128, 128, 128, 0, 1),
                                          (122, 122, 122, 1, 0), (100, 250, 77, 1, 1), (1, 1, 1, 0, 0),
-                                         (64, 160, 300, 0, 0)])
+                                         (64, 160, 300, 0, 0), (160, 160, 160, 0, 0), (250, 96, 40, 1, 0)])
 def test_mma_gemm_matches_fp64(gpu, M, N, K, ta, tb):
     import qcxms_gb300 as qg
     rng = np.random.default_rng(M * 1000 + N + K)
