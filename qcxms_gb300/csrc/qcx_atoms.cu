@@ -213,8 +213,10 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
       const double* dgwa = bt.dw4 + (long long)(off + a) * kMaxRef;
       double dwa[kMaxRef];
       for (int i = 0; i < kMaxRef; ++i) dwa[i] = dgwa[i] * zqa[i];
-      dEdR += -d4_c6(P, za, wqa, zb, wqb) * dgd;
-      dcda += -gd * d4_c6(P, za, dwa, zb, wqb);
+      double c6ab, dc6a;
+      d4_c6_pair(P, za, wqa, dwa, zb, wqb, c6ab, dc6a);
+      dEdR += -c6ab * dgd;
+      dcda += -gd * dc6a;
       // repulsion
       {
         double al = sqrt(P.rep_alpha[za] * P.rep_alpha[zb]);

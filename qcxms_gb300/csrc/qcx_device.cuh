@@ -198,6 +198,19 @@ __device__ inline double d4_c6(const Params& p, int za, const double* wa, int zb
   }
   return s;
 }
+// both sums_ij wa_i wb_j C6_ij and da_i wb_j C6_ij with one pass over the table
+__device__ inline void d4_c6_pair(const Params& p, int za, const double* wa, const double* da, int zb,
+                                  const double* wb, double& c6, double& dc6) {
+  double s = 0.0, ds = 0.0;
+  for (int i = 0; i < p.d4_refn[za]; ++i) {
+    double t = 0.0;
+    for (int j = 0; j < p.d4_refn[zb]; ++j) t += wb[j] * p.d4_c6r[za][zb][i][j];
+    s += wa[i] * t;
+    ds += da[i] * t;
+  }
+  c6 = s;
+  dc6 = ds;
+}
 __device__ inline float d4_c6(const Params& p, int za, const float* wa, int zb, const float* wb) {
   float s = 0.0f;
   for (int i = 0; i < p.d4_refn[za]; ++i) {

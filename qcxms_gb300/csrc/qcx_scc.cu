@@ -334,8 +334,8 @@ __device__ void potentials(const MolView& mv, const double* x, double* en, doubl
     // dispersion: E_ab = -g_ab sum_ij wq_ai wq_bj C6_ij; the a-side charge derivative
     const double gd = gdm[a * nat + b];
     const int za = mv.Z[a], zb = mv.Z[b];
-    const double c6 = d4_c6(P, za, wq + kMaxRef * a, zb, wq + kMaxRef * b);
-    const double dc6 = d4_c6(P, za, dwq + kMaxRef * a, zb, wq + kMaxRef * b);
+    double c6, dc6;
+    d4_c6_pair(P, za, wq + kMaxRef * a, dwq + kMaxRef * a, zb, wq + kMaxRef * b, c6, dc6);
     e[2] += 0.5 * (f3 * (qat[a] * mbr - qat[b] * mar) + f5 * (qat[a] * rtb + qat[b] * rta + mab * r2 - 3.0 * mar * mbr));
     e[4] += -0.5 * gd * c6;
     atomicAdd(&vat[a], f3 * mbr + f5 * rtb - gd * dc6);
