@@ -33,6 +33,9 @@ extern "C" {
  * outside [1e-8, 20], or a cation with max(qat) below 1e-5 in magnitude; the
  * last two set the energy to 0, as the reference does */
 #define QCX_STATUS_CHECKQC 16
+/* the SCC stopped at the per-launch budget of qcx_batch_set_scc_budget; the
+ * next qcx_batch_step or qcx_batch_egrad continues it (not a failure) */
+#define QCX_STATUS_SCC_PENDING 32
 
 /* Library version (major*10000 + minor*100 + patch). */
 int qcx_version(void);
@@ -84,7 +87,7 @@ qcx_batch* qcx_batch_create(int nmol, const int32_t* nat, const int32_t* num, co
                             const double* etemp);
 void qcx_batch_destroy(qcx_batch* b);
 
-/* SCC controls (defaults: 100, 1e-7 Eh, 1e-6, 0.25). max_iter <= 100. */
+/* SCC controls (defaults: 250, 1e-7 Eh, 1e-6, 0.25). max_iter <= 250. */
 int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, double mixing);
 
 /* Arithmetic of the SCC loop: 0 = FP64 throughout (default); 1 = mixed.
@@ -112,8 +115,25 @@ int qcx_batch_set_precision(qcx_batch* b, int precision);
 #define QCX_GUESS_PREVIOUS 1
 int qcx_batch_set_guess(qcx_batch* b, int guess);
 
+/* SCC iteration budget of one MD step (0, the default: none). QCxMS runs its
+ * trajectories as independent processes (bin/pqcxms), each at its own pace;
+ * a batch that steps all trajectories together waits in every step for the
+ * slowest SCC. With a budget b, the SCC of a molecule of n AOs stops after
+ * ceil(b (nmax / n)^2) iterations of one qcx_batch_step (nmax: the batch's
+ * largest molecule; mixed precision stops only between FP32 iterations) and
+ * the next step continues it at the same coordinates: that trajectory does
+ * not move and counts no step until its SCC has converged (status
+ * QCX_STATUS_SCC_PENDING meanwhile), so trajectories advance at their own
+ * pace, as the reference's processes do, and each trajectory's sequence of
+ * steps is the one without a budget up to the SCC tolerances. The iteration
+ * limit (qcx_batch_set_scc) counts every iteration of an SCC.
+ * qcx_batch_egrad ignores the budget and completes every SCC, a suspended one
+ * included. Returns 0 or -1. */
+int qcx_batch_set_scc_budget(qcx_batch* b, int iters);
+
 /* Copy host state in. Any pointer may be NULL to keep the current value.
- * xyz, vel: [natom][3]; mass: [natom] (atomic units). */
+ * xyz, vel: [natom][3]; mass: [natom] (atomic units). New coordinates start
+ * every trajectory afresh: stopped ones run again, suspended SCCs are dropped. */
 int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, const double* mass);
 
 /* Copy coordinates and/or velocities ([natom][3], NULL keeps the current
@@ -390,6 +410,49 @@ int qcx_write_gs(const char* path, int nmax, int nat, int nrec, const double* xy
  */
 int qcx_format_res(int cid, double fragchrg3, int mchrg, int itrj, int icoll, int isec, int ifrag, int nel,
                    const int32_t* z, const int32_t* count, char* line, int len);
+
+/*
+ * MO spectrum path: get_xtb_egrad(..., spec_calc=.true.) (src/tblite.f90:
+ * 153-166) hands the converged orbitals to write_qmo (src/mo_energ.f90:7-80).
+ *
+ * qcx_batch_set_keep_mo(b, 1) makes the FP64 SCC (qcx_batch_set_precision(b,
+ * 0)) keep its last orbitals on the device; after qcx_batch_egrad,
+ * qcx_batch_mo_populations returns for molecule mol the orbital energies
+ * emo[nao] (Eh, ascending), the occupations focc[nao] (0..2), the Mulliken
+ * populations qmo[nao][nat] of every orbital on every atom as write_qmo forms
+ * them (sum over the atom's AOs j and all AOs l of C(j,k) C(l,k) S(j,l), plus
+ * 1e-10, each orbital's row divided by its sum over the atoms) and ihomo =
+ * max(homo, 1), homo = floor(nel / 2), the aufbau count of one spin channel
+ * of the spin-restricted wavefunction. Any output pointer may be NULL.
+ * Returns nao, or -1 (no keep_mo, mixed precision or a CUDA error).
+ */
+int qcx_batch_set_keep_mo(qcx_batch* b, int on);
+int qcx_batch_mo_populations(qcx_batch* b, int mol, double* emo, double* focc, double* qmo, int32_t* ihomo);
+
+/*
+ * get_xtb_egrad(spec_calc=.true.) for one structure, as getspec calls it
+ * through eqm (src/mo_spec.f90:74): the FP64 single point (no checkqc), its
+ * energy, nao, ihomo and the quantities of qcx_batch_mo_populations. emo and
+ * focc hold max_nao values, qmo max_nao * nat. Returns 0, 5 (method not
+ * implemented) or -1 (failed calculation, or more than max_nao orbitals:
+ * *nao is set then).
+ */
+int qcx_mo_spectrum(int method, int nat, const int32_t* num, const double* xyz, int charge, int multiplicity,
+                    double etemp, double* energy, int32_t* nao, int32_t* ihomo, double* emo, double* focc,
+                    double* qmo, int max_nao);
+
+/*
+ * The two files of write_qmo (src/mo_energ.f90:26-79); either path may be
+ * NULL. mspec_path (qcxms.Mspec.tbxtb): nao and ihomo list-directed, then per
+ * orbital an empty line, (i3,1x,f10.3) the orbital number and emo in eV,
+ * (1x,f6.2) focc and (10(1x,f6.2)) the populations in percent. tmp_path
+ * (tmp.mspec, read back by readpopmo, src/mo_energ.f90:82-107): nao, ihomo,
+ * then per orbital emo in eV, focc and the nat populations, one list-directed
+ * item per line in gfortran's layout (17 significant digits). emo in Eh as
+ * qcx_batch_mo_populations returns it. Returns 0 or -1.
+ */
+int qcx_write_qmo(const char* tmp_path, const char* mspec_path, int nat, int nao, int ihomo, const double* emo,
+                  const double* focc, const double* qmo);
 
 /*
  * Allocation-free variant of qcx_egrad for callers that cannot call

@@ -130,6 +130,21 @@ def scc(Z, xyz, charge=0, kT=300.0 * 3.166808578545117e-06, opts=None):
     return P, qsh, dp, qp, eps, focc, info.as_dict()
 
 
+def mo_spectrum(Z, xyz, charge=0, kT=300.0 * 3.166808578545117e-06, opts=None):
+    """write_qmo's quantities (src/mo_energ.f90:7-80) of the converged SCC:
+    returns (rc, emo [nao] in Eh, focc [nao], qmo [nao][nat], ihomo, info)."""
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    n, nat = nao(Z), len(Z)
+    emo = np.zeros(n); focc = np.zeros(n); qmo = np.zeros((n, nat))
+    ih = ctypes.c_int()
+    info = Info()
+    o = opts if opts is not None else default_opts()
+    rc = lib().qcxo_mo_spectrum(nat, _p(Z, ctypes.c_int), _p(xyz), ctypes.c_double(charge), ctypes.c_double(kT),
+                                ctypes.byref(o), _p(emo), _p(focc), _p(qmo), ctypes.byref(ih), ctypes.byref(info))
+    return rc, emo, focc, qmo, ih.value, info.as_dict()
+
+
 def syev(A):
     A = np.array(A, dtype=np.float64, order="C")
     n = A.shape[0]

@@ -1099,6 +1099,7 @@ typedef struct {
   mol_t m;
   double *cn, *cnd, *S, *H0, *Dm, *Qm, *X;
   double *P, *W, *eps, *focc, *x_out, *vsh, *vdp, *vqp;
+  double* C; /* MO coefficients of the last iteration, C[i*n + k]: AO i, orbital k by energy */
   es_t es;
   es_energy_t esen;
   double e_band, e_ts, e_elec, efermi;
@@ -1109,6 +1110,7 @@ typedef struct {
 static void scc_free(scc_t* c) {
   free(c->cn); free(c->cnd); free(c->S); free(c->H0); free(c->Dm); free(c->Qm); free(c->X);
   free(c->P); free(c->W); free(c->eps); free(c->focc); free(c->x_out); free(c->vsh); free(c->vdp); free(c->vqp);
+  free(c->C);
   es_free(&c->es);
   mol_free(&c->m);
 }
@@ -1245,7 +1247,8 @@ static int run_scc(int nat, const int* Z, const double* xyz, double charge, doub
   }
   c->iterations = it > o->max_iter ? o->max_iter : it;
   broyden_free(&br);
-  free(x); free(F); free(T); free(A); free(V); free(C);
+  free(x); free(F); free(T); free(A); free(V);
+  c->C = C;
   return 0;
 }
 
@@ -1271,6 +1274,57 @@ int qcxo_scc(int nat, const int* Z, const double* xyz, double charge, double kT,
   }
   scc_free(&c);
   return 0;
+}
+
+/* MO populations of the spectrum path: get_xtb_egrad(spec_calc=.true.)
+ * (src/tblite.f90:153-166) hands the overlap, the AO-to-atom map, the
+ * coefficients, orbital energies and occupations of the converged SCC to
+ * write_qmo (src/mo_energ.f90:7-80), which forms per orbital k and atom a
+ *   qmo(k,a) = sum_{j on a} sum_l C(j,k) C(l,k) S(j,l) + 1e-10
+ * (j ascending, l ascending, each term (C(j,k) C(l,k)) S(j,l)) and divides
+ * every orbital's row by its sum over the atoms (atoms ascending).
+ * ihomo = max(homo, 1) with tblite's homo of a spin-restricted wavefunction:
+ * the aufbau count floor(nel / 2) of one spin channel (uhf = 0).
+ * emo[nao] (Eh, ascending), focc[nao], qmo[nao][nat]. Returns 0, -1 (invalid
+ * input or Cholesky failure) or 1 (SCC not converged; outputs still set). */
+int qcxo_mo_spectrum(int nat, const int* Z, const double* xyz, double charge, double kT, const qcxo_opts* opts,
+                     double* emo, double* focc, double* qmo, int* ihomo, qcxo_info* info) {
+  qcxo_opts o;
+  if (opts) o = *opts; else qcxo_default_opts(&o);
+  scc_t c;
+  int rc = run_scc(nat, Z, xyz, charge, kT, &o, &c);
+  if (rc) { scc_free(&c); return -1; }
+  const int n = c.m.nao;
+  int* aoat = malloc(sizeof(int) * n);
+  for (int s = 0; s < c.m.nsh; ++s)
+    for (int i = 0; i < c.m.sh_nao[s]; ++i) aoat[c.m.sh_ao0[s] + i] = c.m.sh_atom[s];
+  for (int a = 0; a < nat; ++a)
+    for (int k = 0; k < n; ++k) {
+      double sum = 0.0;
+      for (int j = 0; j < n; ++j) {
+        if (aoat[j] != a) continue;
+        for (int l = 0; l < n; ++l) sum = sum + (c.C[j * n + k] * c.C[l * n + k]) * c.S[j * n + l];
+      }
+      qmo[(size_t)k * nat + a] = sum + 1e-10;
+    }
+  for (int k = 0; k < n; ++k) {
+    double sum = 0.0;
+    for (int a = 0; a < nat; ++a) sum = sum + qmo[(size_t)k * nat + a];
+    for (int a = 0; a < nat; ++a) qmo[(size_t)k * nat + a] = qmo[(size_t)k * nat + a] / sum;
+  }
+  memcpy(emo, c.eps, sizeof(double) * n);
+  memcpy(focc, c.focc, sizeof(double) * n);
+  int homo = (int)floor(0.5 * c.nel);
+  *ihomo = homo > 1 ? homo : 1;
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->iterations = c.iterations; info->converged = c.converged; info->nao = n; info->nsh = c.m.nsh;
+    info->nel = c.nel; info->e_total = c.e_elec;
+  }
+  int conv = c.converged;
+  free(aoat);
+  scc_free(&c);
+  return conv ? 0 : 1;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -61,6 +61,11 @@ int qcxo_scc(int nat, const int* Z, const double* xyz, double charge, double kT,
 /* Symmetric eigensolver used by the oracle (Householder + implicit QL).
  * A [n][n] is destroyed; V [n][n] holds eigenvectors as columns. */
 int qcxo_syev(int n, double* A, double* w, double* V);
+/* MO energies, occupations and normalised Mulliken populations per atom of
+ * the converged SCC, as write_qmo forms them (src/mo_energ.f90:7-80); qmo is
+ * [nao][nat]. Returns 0, 1 (SCC not converged) or -1. */
+int qcxo_mo_spectrum(int nat, const int* Z, const double* xyz, double charge, double kT, const qcxo_opts* opts,
+                     double* emo, double* focc, double* qmo, int* ihomo, qcxo_info* info);
 
 /* D4 data checks: C6 of reference pair (za, i; zb, j) built from QCxMS's
  * reference polarisabilities (src/dftd4.f90:531-595, 665), -1 outside the

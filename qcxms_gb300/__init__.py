@@ -40,6 +40,7 @@ STATUS_NON_FINITE = 2
 STATUS_CHOLESKY_FAILED = 4
 STATUS_EIGEN_NOT_CONVERGED = 8
 STATUS_CHECKQC = 16
+STATUS_SCC_PENDING = 32
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _lib = None
@@ -117,6 +118,15 @@ def load_library(build_if_missing=True):
     lib.qcx_format_res.argtypes = [c_int, c_double, c_int, c_int, c_int, c_int, c_int, c_int, P(ctypes.c_int32),
                                    P(ctypes.c_int32), ctypes.c_char_p, c_int]
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
+    lib.qcx_batch_set_keep_mo.argtypes = [ctypes.c_void_p, c_int]
+    lib.qcx_batch_set_scc_budget.argtypes = [ctypes.c_void_p, c_int]
+    lib.qcx_batch_mo_populations.argtypes = [ctypes.c_void_p, c_int, P(c_double), P(c_double), P(c_double),
+                                             P(ctypes.c_int32)]
+    lib.qcx_mo_spectrum.argtypes = [c_int, c_int, P(ctypes.c_int32), P(c_double), c_int, c_int, c_double,
+                                    P(c_double), P(ctypes.c_int32), P(ctypes.c_int32), P(c_double), P(c_double),
+                                    P(c_double), c_int]
+    lib.qcx_write_qmo.argtypes = [ctypes.c_char_p, ctypes.c_char_p, c_int, c_int, c_int, P(c_double), P(c_double),
+                                  P(c_double)]
     _lib = lib
     return lib
 
@@ -263,6 +273,41 @@ def format_res(fragchrg3, mchrg, itrj, isec, ifrag, Z, counts, icoll=None):
     return buf.value.decode()
 
 
+def mo_spectrum(num, xyz, charge=0, multiplicity=1, method=None, etemp=300.0, max_nao=None):
+    """get_xtb_egrad(spec_calc=.true.) for one structure (src/tblite.f90:153-166):
+    returns (energy, emo [nao] in Eh, focc [nao], qmo [nao][nat], ihomo) with
+    write_qmo's populations (src/mo_energ.f90:7-80)."""
+    lib = load_library()
+    num = np.ascontiguousarray(num, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    nat = len(num)
+    mx = int(max_nao or 9 * nat)
+    e = np.zeros(1)
+    n = np.zeros(1, dtype=np.int32)
+    ih = np.zeros(1, dtype=np.int32)
+    emo, focc, qmo = np.zeros(mx), np.zeros(mx), np.zeros(mx * nat)
+    rc = lib.qcx_mo_spectrum(gfn2_xtb if method is None else int(method), nat, _ip(num), _dp(xyz), int(charge),
+                             int(multiplicity), float(etemp), _dp(e), _ip(n), _ip(ih), _dp(emo), _dp(focc), _dp(qmo),
+                             mx)
+    if rc != 0:
+        raise RuntimeError("qcx_mo_spectrum returned %d: %s" % (rc, _err(lib)))
+    k = int(n[0])
+    return float(e[0]), emo[:k].copy(), focc[:k].copy(), qmo[:k * nat].reshape(k, nat).copy(), int(ih[0])
+
+
+def write_qmo(tmp_path, mspec_path, emo, focc, qmo, ihomo):
+    """write_qmo's two files (src/mo_energ.f90:26-79): tmp.mspec (list-directed,
+    read back by readpopmo) and qcxms.Mspec.tbxtb; either path may be None."""
+    lib = load_library()
+    emo = np.ascontiguousarray(emo, dtype=np.float64)
+    focc = np.ascontiguousarray(focc, dtype=np.float64)
+    qmo = np.ascontiguousarray(qmo, dtype=np.float64)
+    enc = lambda p: None if p is None else os.fsencode(p)
+    if lib.qcx_write_qmo(enc(tmp_path), enc(mspec_path), qmo.shape[1], qmo.shape[0], int(ihomo), _dp(emo), _dp(focc),
+                         _dp(qmo)) != 0:
+        raise RuntimeError("qcx_write_qmo failed: " + _err(lib))
+
+
 def boltz(units, temp, ip):
     """Boltzmann weights of an ``(nfrag, mchrg)`` IP array, ``boltz`` of
     ``src/utility.f90:469-498`` (units 1: kcal/mol, 2: eV)."""
@@ -335,7 +380,7 @@ class Batch:
         if rc != 0:
             raise RuntimeError("%s failed: %s" % (what, _err(self._lib)))
 
-    def set_scc(self, max_iter=100, econv=1e-7, pconv=1e-6, mixing=0.25):
+    def set_scc(self, max_iter=250, econv=1e-7, pconv=1e-6, mixing=0.25):
         self._check(self._lib.qcx_batch_set_scc(self._h, int(max_iter), float(econv), float(pconv), float(mixing)),
                     "set_scc")
 
@@ -433,6 +478,29 @@ class Batch:
         vf = None if velof is None else np.ascontiguousarray(velof, dtype=np.float64)
         self._check(self._lib.qcx_batch_set_md_heating(self._h, _dp(eimp), _dp(tadd), _dp(vf), float(tstep)),
                     "set_md_heating")
+
+    def set_scc_budget(self, iters):
+        """SCC iterations per step for the batch's largest molecule (0: none);
+        a molecule whose SCC needs more continues it in the next step without
+        moving (status STATUS_SCC_PENDING)."""
+        self._check(self._lib.qcx_batch_set_scc_budget(self._h, int(iters)), "set_scc_budget")
+
+    def set_keep_mo(self, on=True):
+        """Keep the orbitals of the FP64 SCC for mo_populations (set before egrad)."""
+        self._check(self._lib.qcx_batch_set_keep_mo(self._h, int(bool(on))), "set_keep_mo")
+
+    def mo_populations(self, i):
+        """(emo [nao] in Eh, focc [nao], qmo [nao][nat], ihomo) of molecule i
+        after egrad with set_keep_mo (FP64 precision)."""
+        nat = int(self.nat[i])
+        from .basis import nao_of
+        n = nao_of(self.Z[self.offsets[i]:self.offsets[i] + nat])
+        emo, focc, qmo = np.zeros(n), np.zeros(n), np.zeros((n, nat))
+        ih = np.zeros(1, dtype=np.int32)
+        rc = self._lib.qcx_batch_mo_populations(self._h, int(i), _dp(emo), _dp(focc), _dp(qmo), _ip(ih))
+        if rc < 0:
+            raise RuntimeError("mo_populations failed: " + _err(self._lib))
+        return emo, focc, qmo, int(ih[0])
 
     def set_md_etemp(self, ax=0.0, ieetemp=0.0):
         """Per-step electronic temperature of EI runs (setetemp after every step).

@@ -13,7 +13,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libqcxgpu.so")
 SOURCES = ["qcx_api.cu", "qcx_integrals.cu", "qcx_scc.cu", "qcx_atoms.cu", "qcx_noalloc.cu", "qcx_fragip.cu",
-           "qcx_mdrules.cu", "qcx_io.cu", "qcx_cidrules.cu", "qcx_mmatest.cu"]
+           "qcx_mdrules.cu", "qcx_io.cu", "qcx_cidrules.cu", "qcx_mmatest.cu",
+           "qcx_mospec.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + CSRC, "-I" + os.path.join(HERE, "..", "include")]

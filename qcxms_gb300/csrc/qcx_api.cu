@@ -6,6 +6,7 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -111,6 +112,7 @@ struct qcx_batch {
   MdState* d_md = nullptr;
   double* d_md_heat = nullptr;  // [nmol][3] eimp, fadd, nadd (qcx_batch_set_md_heating)
   double* d_velof = nullptr;    // [natom] velocity scaling weights of the heating
+  SccCarry* d_carry = nullptr;  // [nmol] state of suspended SCCs (qcx_batch_set_scc_budget)
   double* d_avxyz = nullptr;    // [natom][3] coordinate sums of the averaged structure
   bool md_heat = false;
   std::vector<double> h_eimp;   // eimp of every trajectory (qcx_batch_set_md_heating)
@@ -172,9 +174,12 @@ int mark(qcx_batch* b, bool marks, int k, cudaStream_t st) {
 
 // Enqueues one energy + gradient evaluation; returns the number of kernels
 // launched, or -1 on an error in the stream bookkeeping. marks: record the
-// per-group timing marks (only while capturing the step graph).
-int enqueue_egrad(qcx_batch* b, bool marks = false) {
-  const DevBatch& d = b->dev;
+// per-group timing marks (only while capturing the step graph). budget: the
+// SCCs may stop at the per-launch budget (the step graph); without it every
+// SCC, a suspended one included, runs to its end (qcx_batch_egrad).
+int enqueue_egrad(qcx_batch* b, bool marks = false, bool budget = false) {
+  DevBatch d = b->dev;
+  if (!budget) d.scc_budget = 0;
   int n = 0;
   launch_cn(d, b->stream);
   launch_zero_grad(d, b->stream);
@@ -195,6 +200,7 @@ int enqueue_egrad(qcx_batch* b, bool marks = false) {
     cudaStream_t st = b->g_stream[g];
     if (g > 0 && cudaStreamWaitEvent(st, b->g_fork, 0) != cudaSuccess) return -1;
     DevBatch gd = group_dev(b, g);
+    if (!budget) gd.scc_budget = 0;
     if (mark(b, marks, 1 + 4 * g, st)) return -1;
     n += launch_integrals(gd, st);  // the group's shell pairs only
     if (mark(b, marks, 2 + 4 * g, st)) return -1;
@@ -231,6 +237,7 @@ void free_batch(qcx_batch* b) {
   if (b->d_avxyz) cudaFree(b->d_avxyz);
   if (b->d_cid) cudaFree(b->d_cid);
   if (b->d_velof) cudaFree(b->d_velof);
+  if (b->d_carry) cudaFree(b->d_carry);
   for (size_t g = 1; g < b->g_stream.size(); ++g)
     if (b->g_stream[g]) cudaStreamDestroy(b->g_stream[g]);
   for (cudaEvent_t e : b->g_join)
@@ -754,7 +761,8 @@ int qcx_batch_set_state(qcx_batch* b, const double* xyz, const double* vel, cons
       drop_graph(b);
     }
     CK(cudaMemcpyAsync(b->d_xyz, xyz, n3, cudaMemcpyHostToDevice, b->stream));
-    // new coordinates start every trajectory afresh
+    // new coordinates start every trajectory afresh (and end suspended SCCs)
+    CK(cudaMemsetAsync(b->d_status, 0, sizeof(int) * b->nmol, b->stream));
     std::vector<int> on(b->nmol, 1);
     CK(cudaMemcpyAsync(b->d_active, on.data(), sizeof(int) * b->nmol, cudaMemcpyHostToDevice, b->stream));
     CK(cudaStreamSynchronize(b->stream));
@@ -796,7 +804,7 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
     const bool marks = b->timing;
     int n = mark(b, marks, 0, b->stream);
     launch_leapfrog(b->dev, tstep, b->stream);
-    if (n >= 0) n = enqueue_egrad(b, marks);
+    if (n >= 0) n = enqueue_egrad(b, marks, true);
     if (n >= 0 && b->md_on) {
       // fragment_structure(nuc, iat, xyz, 3.0, 1, 0, list) of src/md.f90:450, then the rules
       launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream);
@@ -1020,6 +1028,114 @@ int qcx_egrad(int method, int nat, const int32_t* num, const double* xyz, int ch
     return -1;
   }
   return 0;
+}
+
+int qcx_batch_set_scc_budget(qcx_batch* b, int iters) {
+  if (!b || iters < 0) {
+    set_error("qcx_batch_set_scc_budget: iters must be >= 0");
+    return -1;
+  }
+  if (iters > 0 && !b->d_carry) {
+    CK(cudaMalloc((void**)&b->d_carry, sizeof(SccCarry) * b->nmol));
+    CK(cudaMemset(b->d_carry, 0, sizeof(SccCarry) * b->nmol));
+    b->dev.carry = b->d_carry;
+  }
+  if (iters != b->dev.scc_budget) drop_graph(b);
+  b->dev.scc_budget = iters;
+  b->dev.budget_nao = b->max_nao;
+  return 0;
+}
+
+int qcx_batch_set_keep_mo(qcx_batch* b, int on) {
+  if (!b || (on != 0 && on != 1)) {
+    set_error("qcx_batch_set_keep_mo: on must be 0 or 1");
+    return -1;
+  }
+  if (b->dev.keep_mo != on) drop_graph(b);
+  b->dev.keep_mo = on;
+  return 0;
+}
+
+int qcx_batch_mo_populations(qcx_batch* b, int mol, double* emo, double* focc, double* qmo, int32_t* ihomo) {
+  if (!b || mol < 0 || mol >= b->nmol) {
+    set_error("qcx_batch_mo_populations: invalid batch or molecule index");
+    return -1;
+  }
+  if (!b->dev.keep_mo || b->precision != 0) {
+    set_error("qcx_batch_mo_populations: needs qcx_batch_set_keep_mo(b, 1) and FP64 precision before qcx_batch_egrad");
+    return -1;
+  }
+  const MolDesc& md = b->mol[mol];
+  const VecLayout vl = VecLayout::make(md.nat, md.nsh, md.nao, md.len, md.nmem);
+  const double* vec = b->d_vecs + md.vec_off;
+  if (emo) CK(cudaMemcpyAsync(emo, vec + vl.eps, sizeof(double) * md.nao, cudaMemcpyDeviceToHost, b->stream));
+  if (focc) CK(cudaMemcpyAsync(focc, vec + vl.focc, sizeof(double) * md.nao, cudaMemcpyDeviceToHost, b->stream));
+  if (qmo) {
+    double* d = nullptr;
+    const size_t bytes = sizeof(double) * (size_t)md.nao * md.nat;
+    CK(cudaMallocAsync((void**)&d, bytes, b->stream));
+    qcx::launch_mo_pops(b->dev, mol, md.nao, d, b->stream);
+    if (check_launch()) {
+      cudaFreeAsync(d, b->stream);
+      return -1;
+    }
+    cudaError_t e = cudaMemcpyAsync(qmo, d, bytes, cudaMemcpyDeviceToHost, b->stream);
+    cudaFreeAsync(d, b->stream);
+    if (e != cudaSuccess) {
+      set_error(std::string("qcx_batch_mo_populations: ") + cudaGetErrorString(e));
+      return -1;
+    }
+  }
+  // ihomo = max(homo, 1) (src/tblite.f90:161): the aufbau count of one spin
+  // channel of the spin-restricted wavefunction, floor(nel / 2)
+  if (ihomo) {
+    const int homo = (int)std::floor(0.5 * md.nel);
+    *ihomo = homo > 1 ? homo : 1;
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  return md.nao;
+}
+
+int qcx_mo_spectrum(int method, int nat, const int32_t* num, const double* xyz, int charge, int multiplicity,
+                    double etemp, double* energy, int32_t* nao, int32_t* ihomo, double* emo, double* focc,
+                    double* qmo, int max_nao) {
+  (void)multiplicity;
+  if (method != QCX_METHOD_GFN2) {
+    set_error("only the GFN2-xTB Hamiltonian is implemented");
+    return 5;
+  }
+  if (nat < 1 || !num || !xyz || !energy || !nao || !ihomo || !emo || !focc || !qmo) {
+    set_error("qcx_mo_spectrum: invalid arguments");
+    return -1;
+  }
+  int32_t n1 = nat;
+  double ch = charge, et = etemp;
+  qcx_batch* b = qcx_batch_create(1, &n1, num, &ch, &et);
+  if (!b) return -1;
+  int32_t na = 0, nt = 0;
+  qcx_batch_get_sizes(b, &na, &nt);
+  *nao = na;
+  if (na > max_nao) {
+    set_error("qcx_mo_spectrum: the structure has more atomic orbitals than max_nao");
+    free_batch(b);
+    return -1;
+  }
+  // the spectrum call of eqm has no checkqc (src/mo_spec.f90:74, src/iniqm.f90:393-421)
+  qcx::batch_set_checkqc(b, 0);
+  int32_t st = 0;
+  int rc = qcx_batch_set_keep_mo(b, 1);
+  if (!rc) rc = qcx_batch_set_state(b, xyz, nullptr, nullptr);
+  if (!rc) rc = qcx_batch_egrad(b);
+  if (!rc) rc = qcx_batch_get(b, nullptr, nullptr, nullptr, energy, nullptr, nullptr, &st, nullptr);
+  if (!rc && st != 0) {
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), "qcx_mo_spectrum: calculation failed, status bits 0x%x", st);
+    set_error(buf);
+    rc = -1;
+  }
+  if (!rc && qcx_batch_mo_populations(b, 0, emo, focc, qmo, ihomo) < 0) rc = -1;
+  free_batch(b);
+  return rc;
 }
 
 }  // extern "C"

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kAtomThreads) k_grad_atoms(DevBatch bt) {
   extern __shared__ __align__(16) double sm[];
   const int mol = bt.order ? bt.order[blockIdx.x] : blockIdx.x;
   const MolDesc md = bt.mol[mol];
-  if (!bt.active[mol]) return;
+  if (!bt.active[mol] || scc_pending(bt, mol)) return;  // no result yet: nothing to add
   if (bt.status[mol] & kCholeskyFailed) {
     if (threadIdx.x == 0) bt.active[mol] = 0;
     return;
@@ -403,7 +403,8 @@ __global__ void k_leapfrog(DevBatch bt, double tstep) {
   __shared__ double red[32];
   const int mol = blockIdx.x;
   const MolDesc md = bt.mol[mol];
-  if (!bt.active[mol]) return;
+  // a trajectory whose SCC is pending has moved already and waits for its gradient
+  if (!bt.active[mol] || scc_pending(bt, mol)) return;
   double ke = 0.0;
   for (int i = threadIdx.x; i < 3 * md.nat; i += blockDim.x) {
     long long e = 3LL * md.atom_off + i;

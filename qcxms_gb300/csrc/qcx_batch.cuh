@@ -39,9 +39,24 @@ enum Status : int {
   kEigenNotConverged = 8,
   // checkqc (src/iniqm.f90:684-715) rejected the result
   kCheckqcFailed = 16,
+  // the SCC used up its iteration budget of one launch (qcx_batch_set_scc_budget)
+  // before converging: the next launch resumes it at the same geometry, and
+  // until then the trajectory neither moves nor counts a step
+  kSccPending = 32,
 };
 // evaluations that end a trajectory whatever checkqc says
 constexpr int kFailedEval = kSccNotConverged | kNonFinite | kCholeskyFailed;
+
+// SCC state kept between the launches of a suspended SCC (kSccPending); the
+// moment vector and the Broyden history stay in the molecule's vector block
+struct SccCarry {
+  int it;         // iterations done
+  int bro_it;     // Broyden updates since the mixer's last restart
+  int phase32;    // mixed mode: still in the FP32 iterations
+  int stall32, backoff32, n64, eig_fail;
+  int basis;      // mixed mode: the FP32 eigenvectors were saved (B32 region of the kD32 slots)
+  double best32, eprev, efermi, pad_;
+};
 
 struct MolDesc {
   int nat, nsh, nao, len;      // len = nsh + 9 nat (mixed moment vector)
@@ -143,6 +158,13 @@ struct DevBatch {
   int* have_prev;    // [nmol] 1 when the moment vector of a converged SCC at an earlier geometry is kept
   int guess;         // SCC start: 0 = zero moments (a fresh wavefunction every call), 1 = the kept moments
   int checkqc;       // 1: apply checkqc after every evaluation, as egrad does (src/iniqm.f90:650)
+  int keep_mo;       // 1: the FP64 SCC leaves its last orbitals, by energy, as the rows of the kC slot
+  // per-launch SCC budget: 0 = every SCC runs to convergence (or max_iter) in
+  // one launch; b > 0 = a molecule of budget_nao AOs stops after b iterations,
+  // a molecule of n AOs after ceil(b (budget_nao / n)^2), and resumes in the
+  // next launch (kSccPending)
+  int scc_budget, budget_nao;
+  SccCarry* carry;   // [nmol] (allocated with the first nonzero budget)
   const int* order;  // [nmol] molecules by decreasing size: CTA b of a per-molecule kernel takes order[b]
   int max_nao;
   int smem_bytes;  // dynamic shared memory granted to the SCC kernel
@@ -157,6 +179,10 @@ struct DevBatch {
 __host__ __device__ inline long long slot_size(int nao) {
   long long np = nao + (nao & 1);
   return np * np;
+}
+
+__host__ __device__ inline bool scc_pending(const DevBatch& b, int mol) {
+  return (b.status[mol] & kSccPending) != 0;
 }
 
 __host__ __device__ inline double* mat_ptr(const DevBatch& b, const MolDesc& m, int slot) {

@@ -89,7 +89,7 @@ __global__ void k_cid_rules(DevBatch bt, CidState* st, const int* nfrag, CidRule
   const int mol = blockIdx.x * blockDim.x + threadIdx.x;
   if (mol >= bt.nmol) return;
   CidState s = st[mol];
-  if (s.done) return;
+  if (s.done || scc_pending(bt, mol)) return;  // a pending SCC: the step has not happened yet
   const MolDesc md = bt.mol[mol];
   const int nuc = md.nat - 1;
   s.nstep += 1;

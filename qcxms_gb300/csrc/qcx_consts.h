@@ -13,8 +13,10 @@
  * their contribution is below exp(-40) ~ 4e-18 of a normalised integral. */
 #define QCX_PRIM_SCREEN 40.0
 
-/* SCC defaults */
-#define QCX_SCC_MAXITER 100
+/* SCC defaults. The iteration limit is the one of the xtb programs (250, the
+ * default of tblite's calculator), which QCxMS's call keeps (src/tblite.f90:
+ * 136 passes no limit); a molecule that needs more fails its energy call. */
+#define QCX_SCC_MAXITER 250
 #define QCX_SCC_ECONV 1.0e-7
 #define QCX_SCC_PCONV 1.0e-6
 #define QCX_BROYDEN_ALPHA 0.25

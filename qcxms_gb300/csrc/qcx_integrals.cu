@@ -325,7 +325,7 @@ __global__ void k_grad_pairs(DevBatch bt) {
   ShellPair sp = bt.pairs[idx];
   int A = bt.sh_atom[sp.s], B = bt.sh_atom[sp.t];
   if (A == B) return;
-  if (!bt.active[bt.atom_mol[A]]) return;
+  if (!bt.active[bt.atom_mol[A]] || scc_pending(bt, bt.atom_mol[A])) return;
   const MolDesc md = bt.mol[bt.atom_mol[A]];
   pair_gradient<LA, LB>(bt, md, sp.s, sp.t, A, B);
 }

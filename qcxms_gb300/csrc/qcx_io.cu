@@ -147,9 +147,103 @@ std::string fortran_f(double x, int w, int d) {
   return s;
 }
 
+// gfortran's list-directed output of one REAL(8) item: a blank, then the item
+// in 25 columns with 17 significant digits, 1PG25.17E3 style: F editing with
+// 16 - e decimals and five trailing blanks for 0.1 <= |x| < 1e17 (e = the
+// decimal exponent after rounding), else E editing with one digit before the
+// point and a three-digit exponent. List-directed layout is processor
+// dependent; this is the layout of gfortran, which the reference builds with.
+std::string fortran_list_real(double x) {
+  char buf[64];
+  std::string body;
+  if (x == 0.0) {
+    body = std::string(std::signbit(x) ? "-" : "") + "0.0000000000000000     ";
+  } else {
+    std::snprintf(buf, sizeof(buf), "%.16e", x);
+    std::string m(buf);
+    const size_t p = m.find('e');
+    const int ex = std::atoi(m.c_str() + p + 1);
+    if (ex >= -1 && ex < 17) {
+      std::snprintf(buf, sizeof(buf), "%.*f", 16 - ex, x);
+      body = buf;
+      if (16 - ex == 0) body += ".";
+      body += "     ";
+    } else {
+      char tail[16];
+      std::snprintf(tail, sizeof(tail), "E%c%03d", ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
+      body = m.substr(0, p) + tail;
+    }
+  }
+  if (body.size() < 25) body = std::string(25 - body.size(), ' ') + body;
+  return " " + body;
+}
+
+// list-directed INTEGER item of gfortran: a blank and 11 columns
+std::string fortran_list_int(long long v) {
+  char buf[32];
+  std::snprintf(buf, sizeof(buf), " %11lld", v);
+  return buf;
+}
+
 }  // namespace
 
 extern "C" {
+
+int qcx_write_qmo(const char* tmp_path, const char* mspec_path, int nat, int nao, int ihomo, const double* emo,
+                  const double* focc, const double* qmo) {
+  if (nat < 1 || nao < 1 || !emo || !focc || !qmo) {
+    qcx::set_last_error("qcx_write_qmo: invalid arguments (nat >= 1, nao >= 1, emo, focc and qmo)");
+    return -1;
+  }
+  const double autoev = 27.21138505;  // src/xtb_mctc_convert.f90:27
+  if (mspec_path) {
+    // qcxms.Mspec.tbxtb: write(*) nao, ihomo; per orbital an empty record,
+    // (i3,1x,f10.3) k and emo*autoev, (1x,f6.2) focc, (10(1x,f6.2)) the
+    // populations in percent, ten to a line
+    FILE* f = std::fopen(mspec_path, "w");
+    if (!f) {
+      qcx::set_last_error(std::string("qcx_write_qmo: cannot write ") + mspec_path);
+      return -1;
+    }
+    std::fprintf(f, "%s%s\n", fortran_list_int(nao).c_str(), fortran_list_int(ihomo).c_str());
+    for (int k = 0; k < nao; ++k) {
+      std::fprintf(f, "\n%s %s\n %s\n", fortran_i(k + 1, 3).c_str(), fortran_f(emo[k] * autoev, 10, 3).c_str(),
+                   fortran_f(focc[k], 6, 2).c_str());
+      std::string line;
+      for (int a = 0; a < nat; ++a) {
+        line += " " + fortran_f(qmo[(size_t)k * nat + a] * 100.0, 6, 2);
+        if (a % 10 == 9 || a == nat - 1) {
+          std::fprintf(f, "%s\n", line.c_str());
+          line.clear();
+        }
+      }
+    }
+    if (std::fclose(f) != 0) {
+      qcx::set_last_error(std::string("qcx_write_qmo: write error on ") + mspec_path);
+      return -1;
+    }
+  }
+  if (tmp_path) {
+    // tmp.mspec, list-directed throughout: nao, ihomo; per orbital emo*autoev,
+    // focc and the nat populations, one item to a record
+    FILE* f = std::fopen(tmp_path, "w");
+    if (!f) {
+      qcx::set_last_error(std::string("qcx_write_qmo: cannot write ") + tmp_path);
+      return -1;
+    }
+    std::fprintf(f, "%s%s\n", fortran_list_int(nao).c_str(), fortran_list_int(ihomo).c_str());
+    for (int k = 0; k < nao; ++k) {
+      std::fprintf(f, "%s\n%s\n", fortran_list_real(emo[k] * autoev).c_str(), fortran_list_real(focc[k]).c_str());
+      for (int a = 0; a < nat; ++a) std::fprintf(f, "%s\n", fortran_list_real(qmo[(size_t)k * nat + a]).c_str());
+    }
+    if (std::fclose(f) != 0) {
+      qcx::set_last_error(std::string("qcx_write_qmo: write error on ") + tmp_path);
+      return -1;
+    }
+  }
+  return 0;
+}
+
 
 int qcx_write_start(const char* path, int itrj, int nat, double eimp, double tadd, const double* vel,
                     const double* velof) {

@@ -23,6 +23,10 @@ void launch_zero_grad(const DevBatch& bt, cudaStream_t st);
 // accepted, 1 |E| < 1e-8, 2 gradient norm, 3 charges; *e set to 0 for 2 and 3
 void launch_checkqc(int nat, const double* grad, const double* qat, double charge, double* e, int* code,
                     cudaStream_t st);
+// normalised Mulliken populations of every orbital of molecule mol on every
+// atom (qmo [nao][nat], write_qmo, src/mo_energ.f90:7-80), from the orbitals a
+// keep_mo SCC left in the kC slot
+void launch_mo_pops(const DevBatch& bt, int mol, int nao, double* qmo, cudaStream_t st);
 // fragment numbers of every molecule's atoms (frag[natom]) and fragment counts (nfrag[nmol])
 // skip_last = 1: the last atom of every molecule is left out (fragment 0)
 void launch_fragments(const DevBatch& bt, int max_nat, const double* rad, double rcut, int at1, int at2, int* frag,

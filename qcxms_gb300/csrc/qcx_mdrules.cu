@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(32 * kRulesWarps) k_md_rules(DevBatch bt, MdSt
   if (mol >= bt.nmol) return;
   double* terms = md_terms + (size_t)warp * r.max_nat;
   MdState s = st[mol];
-  if (s.done) return;
+  if (s.done || scc_pending(bt, mol)) return;  // a pending SCC: the step has not happened yet
   const MolDesc md = bt.mol[mol];
   s.ttime = __dadd_rn(s.ttime, __ddiv_rn(r.tstep, QCX_FSTOAU));
   s.kdump += 1;  // src/md.f90:400

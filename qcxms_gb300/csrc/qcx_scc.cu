@@ -1619,6 +1619,10 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   // largest molecules first, so that the longest CTAs start in the first wave
   const int mol = bt.order ? bt.order[blockIdx.x] : blockIdx.x;
   if (!bt.active[mol]) return;
+  // an SCC suspended at the previous launch's budget continues from its state
+  const bool resume = bt.carry != nullptr && scc_pending(bt, mol);
+  SccCarry cr{};
+  if (resume) cr = bt.carry[mol];
   MolView mv;
   mv.bt = &bt;
   mv.md = bt.mol[mol];
@@ -1817,27 +1821,41 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   // bit 1 of have_prev: the first-iteration FP32 eigenvectors of the previous SCC
   // of this molecule are kept (after the three FP32 dipole matrices in the kD32 slots)
   float* B32 = D32 + 3 * nn;
-  const bool basis_kept = MIXED && bt.have_prev != nullptr && (bt.have_prev[mol] & 2) != 0;
+  // a resumed SCC seeds its first FP32 eigensolve with the eigenvectors it had
+  // at the suspension (same geometry), and keeps its moment vector
+  const bool basis_kept =
+      MIXED && (resume ? cr.basis != 0 : (bt.have_prev != nullptr && (bt.have_prev[mol] & 2) != 0));
   bool basis_saved = false;
-  for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = warm_guess ? xout[i] : 0.0;
+  if (!resume)
+    for (int i = threadIdx.x; i < len; i += blockDim.x) xin[i] = warm_guess ? xout[i] : 0.0;
   __syncthreads();
 
   double en[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  double eprev = 0.0, eel = 0.0, ets = 0.0, eband = 0.0, efermi = 0.0;
-  int it, converged = 0, eig_fail = 0;
-  bool fp32_phase = MIXED != 0 && bt.max_iter > 8 && n >= bt.mixed_min_nao;
+  double eprev = resume ? cr.eprev : 0.0, eel = 0.0, ets = 0.0, eband = 0.0, efermi = resume ? cr.efermi : 0.0;
+  int it, converged = 0, eig_fail = resume ? cr.eig_fail : 0;
+  bool fp32_phase = resume ? cr.phase32 != 0 : (MIXED != 0 && bt.max_iter > 8 && n >= bt.mixed_min_nao);
   bool have64 = false;  // JV holds an orthonormal FP64 basis from a previous iteration
   bool have32 = false;  // JV32 holds FP32 eigenvectors from a previous iteration
-  int bro_it = 0;       // Broyden updates since the last (re)start of the mixer
-  double best32 = 1e300;  // best residual seen in the FP32 phase
-  int stall32 = 0;
-  int backoff32 = 0;    // FP32 iterations left before the next refinement attempt
-  int n64 = 0;          // FP64 iterations done
+  int bro_it = resume ? cr.bro_it : 0;  // Broyden updates since the last (re)start of the mixer
+  double best32 = resume ? cr.best32 : 1e300;  // best residual seen in the FP32 phase
+  int stall32 = resume ? cr.stall32 : 0;
+  int backoff32 = resume ? cr.backoff32 : 0;  // FP32 iterations left before the next refinement attempt
+  int n64 = resume ? cr.n64 : 0;              // FP64 iterations done
+  // iteration budget of this launch (0: none); suspension only between FP32
+  // iterations in mixed mode, so that the double-float finishing iterations
+  // always run in one launch
+  const int it0 = resume ? cr.it + 1 : 1;
+  int budget = 0;
+  if (bt.scc_budget > 0 && bt.carry != nullptr) {
+    const double r = (double)bt.budget_nao / (double)n;
+    budget = (int)ceil((double)bt.scc_budget * r * r);
+  }
+  bool suspended = false;
   PHASE_BEGIN();
 #ifdef QCX_SCC_PHASE_TIMING
   long long _t_start = clock64();
 #endif
-  for (it = 1; it <= bt.max_iter; ++it) {
+  for (it = it0; it <= bt.max_iter; ++it) {
     PHASE_MARK(15);
     // FP32 iterations take their potentials in FP32 straight into shared memory
     const bool pot32 = fp32_phase && potentials32(mv, xin, (float*)sh.mom, n);
@@ -2352,8 +2370,40 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     broyden(mv, xin, xout, bro_it, bt.mix_alpha, sh);
     ++bro_it;
     PHASE_MARK(12);
+    if (budget > 0 && it - it0 + 1 >= budget && (!MIXED || fp32_phase)) {
+      suspended = true;
+      break;
+    }
   }
   if (it > bt.max_iter) it = bt.max_iter;
+  if (suspended && !(mc && !mctx.ok)) {
+    // keep the state for the next launch: the mixer's input moments (xin) and
+    // history are in the vector block already; the FP32 eigenvectors go to
+    // the B32 region (the FP64 path restarts its eigensolve cold)
+    const bool keep_basis = MIXED && have32;
+    if (keep_basis)
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) B32[e] = JV32[(e / n) * np + (e % n)];
+    if (threadIdx.x == 0) {
+      SccCarry c{};
+      c.it = it;
+      c.bro_it = bro_it;
+      c.phase32 = fp32_phase ? 1 : 0;
+      c.stall32 = stall32;
+      c.backoff32 = backoff32;
+      c.n64 = n64;
+      c.eig_fail = eig_fail;
+      c.basis = keep_basis ? 1 : 0;
+      c.best32 = best32;
+      c.eprev = eprev;
+      c.efermi = efermi;
+      bt.carry[mol] = c;
+      bt.status[mol] = kSccPending;
+      bt.iters[mol] = it;
+      if (bt.have_prev) bt.have_prev[mol] = basis_saved ? 2 : 0;
+    }
+    if (mc) mma_teardown(mctx);
+    return;
+  }
 #ifdef QCX_SCC_PHASE_TIMING
   if (threadIdx.x == 0 && mol < 4096) g_mol_cycles[mol] = (unsigned long long)(clock64() - _t_start);
 #endif
@@ -2377,6 +2427,14 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       }
       Wm[(long long)i * n + j] = w;
       Wm[(long long)j * n + i] = w;
+    }
+  }
+  // the orbitals of the last iteration for the MO populations of the spectrum
+  // path: row k of the C slot = AO coefficients of the k-th orbital by energy
+  if (!MIXED && bt.keep_mo) {
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+      const int k = (int)(e / n), i = (int)(e - (long long)k * n);
+      C[e] = JV[(long long)sh.perm[k] * np + i];
     }
   }
   // outputs

@@ -68,7 +68,7 @@ def test_cid_first_evaluation_matches_oracle(gpu, oracle_lib):
     g = b.split(r["grad"])
     for i, m in enumerate(mols):
         rc, e, gref, q, info = oracle_lib.egrad(m["Z"], m["xyz"], 1, kT=KT,
-                                                opts=oracle_lib.default_opts(econv=1e-10, pconv=1e-8))
+                                                opts=oracle_lib.default_opts(econv=1e-10, pconv=1e-8, max_iter=100))
         # both sides agree on whether the SCC converges (one of these systems does not)
         assert (r["status"][i] == 0) == (rc == 0)
         if rc != 0:
