@@ -357,49 +357,67 @@ def run_gpu(args):
             torch.distributed.barrier()
             torch.cuda.synchronize()
 
+    paced = args.stepping == "paced"
+
+    def one_step():
+        if paced:
+            b.step_paced(1, dt)
+        else:
+            b.step(1, dt)
+
     # ---- device-resident timing: graph replay, L2 flushed between steps ----
-    # Timing marks inside the step graph give the SCC phase of every timed step:
-    # from the first group's SCC start to the last group's SCC end.
-    b.set_timing(True)
+    # Whole-batch steps: timing marks inside the step graph give the SCC phase of
+    # every timed step (first group's SCC start to last group's SCC end). Paced
+    # steps: the groups' SCC launches overlap one another and the other kernels,
+    # so the SCC rate is taken over the whole timed region.
+    b.set_timing(not paced)
     for _ in range(args.warmup):
-        b.step(1, dt)
+        one_step()
     barrier()
     _, steps0 = b.progress()
     total_ms = 0.0
     launches = 0
     scc_flops_sum = scc_ms_sum = 0.0
     scc_iters_all = []
+    scc_launches = []
     phase = {"step": [], "scc_span": [], "scc_sum": [], "integrals_sum": [], "gradient_sum": []}
     with ClockSampler(local) as clk:
         barrier()
         for _ in range(args.steps):
-            act_before, _ = b.progress()
-            st_before, it_before = b.status_iters()
+            _, st_before_steps = b.progress()
+            isum0 = b.iterations()
             l2_flush.zero_()
             torch.cuda.synchronize()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
-            b.step(1, dt)
+            one_step()
             e.record(stream)
             e.synchronize()
-            total_ms += s.elapsed_time(e)
+            step_ms = s.elapsed_time(e)
+            total_ms += step_ms
             launches += b.kernel_launches()
-            tm = b.timing()
             st, it = b.status_iters()
-            ran = act_before > 0
-            # iterations of this launch: a resumed SCC had done it_before already
-            resumed = (st_before & qg.STATUS_SCC_PENDING) != 0
-            it_launch = it - np.where(resumed, it_before, 0)
-            scc_flops_sum += scc_flops(nao[ran], it_launch[ran].astype(np.float64))
-            scc_ms_sum += tm["scc_span"]
-            done_now = ran & ((st & qg.STATUS_SCC_PENDING) == 0)
-            scc_iters_all.append(it[done_now])
-            mk = tm["marks"]
-            phase["step"].append(tm["step"])
-            phase["scc_span"].append(tm["scc_span"])
-            phase["scc_sum"].append(tm["scc_sum"])
-            phase["integrals_sum"].append(float(np.sum(mk[:, 1] - mk[:, 0])))
-            phase["gradient_sum"].append(float(np.sum(mk[:, 3] - mk[:, 2])))
+            _, st_after_steps = b.progress()
+            # SCC work of this step from the device's iteration counters: 11 n^3 per
+            # iteration, 2 n^3 per completed evaluation (all launches of the step)
+            dit = (b.iterations() - isum0).astype(np.float64)
+            nev = (st_after_steps - st_before_steps).astype(np.float64)
+            n3 = nao.astype(np.float64) ** 3
+            scc_flops_sum += float(np.sum(dit * 11.0 * n3 + nev * 2.0 * n3))
+            scc_iters_all.append(it[(nev > 0) & ((st & qg.STATUS_SCC_PENDING) == 0)])
+            scc_launches.append(float(nev.sum() + np.sum((st & qg.STATUS_SCC_PENDING) != 0)))
+            if paced:
+                scc_ms_sum += step_ms
+                phase["step"].append(step_ms)
+            else:
+                tm = b.timing()
+                scc_ms_sum += tm["scc_span"]
+                mk = tm["marks"]
+                phase["step"].append(tm["step"])
+                phase["scc_span"].append(tm["scc_span"])
+                phase["scc_sum"].append(tm["scc_sum"])
+                phase["integrals_sum"].append(float(np.sum(mk[:, 1] - mk[:, 0])))
+                phase["gradient_sum"].append(float(np.sum(mk[:, 3] - mk[:, 2])))
         barrier()
     act_end, steps1 = b.progress()
     done = float(np.sum(steps1 - steps0))
@@ -417,14 +435,14 @@ def run_gpu(args):
     hv = torch.from_numpy(r["vel"]).pin_memory()
     he = torch.zeros(b.nmol, dtype=torch.float64).pin_memory()
     e2e_steps = max(3, min(args.steps, 10))
-    b.step(1, dt)  # capture the graph without timing marks outside the timed region
+    one_step()  # capture the graph without timing marks outside the timed region
     b.sync()
     _, s0 = b.progress()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         b.load_state_ptr(hx.data_ptr(), hv.data_ptr())
-        b.step(1, dt)
+        one_step()
         b.get_ptr(hx.data_ptr(), hv.data_ptr(), he.data_ptr())
     barrier()
     e2e_s = time.perf_counter() - t0
@@ -453,7 +471,20 @@ def run_gpu(args):
             v, calls, el, cdone, wall = cpu_sample(sample, 12.0, ncpu)
             cpu = {"value": v, "unit": "trajectory-steps/s", "cores": ncpu, "kind": "port",
                    "sample": cpu_sample_desc(sample, NTRAJ, calls, 10, el, cdone, wall)}
-        med = {k: round(statistics.median(v), 3) for k, v in phase.items()}
+        med = {k: round(statistics.median(v), 3) for k, v in phase.items() if v}
+        if paced:
+            _, gsteps, gms = b.group_info()
+            execution = ("size-bucketed: 8 molecule groups by size, each stepping from its own CUDA graph on its own "
+                         "stream; per step of the largest molecules' group the groups took %s steps"
+                         % gsteps.tolist())
+            unit = ("all k_scc launches of the timed region (the groups' launches overlap one another and the "
+                    "integral and gradient kernels); time = the timed region; FLOPs from the device's per-molecule "
+                    "iteration counters")
+        else:
+            execution = "one CUDA graph per MD step, 8 molecule groups on separate streams"
+            unit = ("the SCC phase of one timed step: one k_scc launch per molecule group (8, concurrent); time = "
+                    "first group's SCC start to last group's SCC end, from event marks inside the step graph; "
+                    "FLOPs from the device's per-molecule iteration counters")
         line = {
             "metric": METRIC, "value": value, "unit": "trajectory-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -467,7 +498,7 @@ def run_gpu(args):
                                       "FP64 integrals, potentials of the finishing iterations, Fermi level, Broyden, "
                                       "energies and gradient") if mixed else "FP64 throughout",
                        "md_rules_on_device": bool(args.md_rules),
-                       "execution": "one CUDA graph per MD step, 8 molecule groups on separate streams",
+                       "execution": execution,
                        "l2": "flushed between timed steps (256 MiB write)",
                        "mean_nao": float(np.mean(nao)),
                        "mean_scc_iters": float(np.mean(iters_cat)) if len(iters_cat) else 0.0,
@@ -478,15 +509,14 @@ def run_gpu(args):
             "gpu_launches": launches,
             "roofline": {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak,
-                         "traffic": SCC_DRAM_BYTES_PER_MOLECULE * float(np.mean([len(x) for x in scc_iters_all])),
+                         "traffic": SCC_DRAM_BYTES_PER_MOLECULE * float(np.mean(scc_launches)),
                          "kernel": "k_scc",
-                         "launch_unit": "the SCC phase of one timed step: one k_scc launch per molecule group (8, "
-                                        "concurrent); time = first group's SCC start to last group's SCC end, from "
-                                        "event marks inside the step graph; FLOPs over the molecules that ran",
+                         "launch_unit": unit,
                          "peak_source": "measured in this run: cuBLAS %s GEMM 4096^3 on CUDA cores "
                                         "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)"
                                         % ("FP32" if mixed else "FP64"),
-                         "flops_convention": "algorithmic, per molecule: iters*(9n^3+2n^3)+2n^3",
+                         "flops_convention": "algorithmic, per molecule: 11 n^3 per SCC iteration (9 n^3 eigensolve, "
+                                             "2 n^3 density) + 2 n^3 per completed evaluation (W)",
                          "tensor": {"peak": tpk, "unit": "TFLOP/s", "frac": achieved / tpk, "peak_source": tsrc,
                                     "note": "the same achieved FLOPs against the dense bf16 tensor peak: the "
                                             "kernel's FP32 products run on the tensor cores (split-TF32), its "
@@ -578,6 +608,9 @@ def main():
     ap.add_argument("--md-rules", action="store_true",
                     help="run the MD heating, bookkeeping and exit rules on the device in the timed steps "
                          "(the end-to-end leg sets new coordinates, which switches them off)")
+    ap.add_argument("--stepping", default="paced", choices=["paced", "graph"],
+                    help="paced: every molecule group steps from its own graph, small molecules several times per "
+                         "step of the largest (default); graph: one graph per step for the whole batch")
     ap.add_argument("--scc-budget", type=int, default=SCC_BUDGET,
                     help="SCC iterations per step for the largest molecule (0: none); slower SCCs continue in the "
                          "next step while their trajectory waits, as independent trajectory processes would")

@@ -131,6 +131,26 @@ int qcx_batch_set_guess(qcx_batch* b, int guess);
  * included. Returns 0 or -1. */
 int qcx_batch_set_scc_budget(qcx_batch* b, int iters);
 
+/* Size-bucketed stepping. The batch's molecules form qcx_batch_group_info
+ * groups by size (group 0 the largest). qcx_batch_step_groups advances group g
+ * by nsteps[g] MD steps (each as qcx_batch_step does it: leapfrog, energy +
+ * gradient, the device loop rules when on), every group from its own captured
+ * graph on its own stream, concurrently with the others; the batch stream
+ * continues after all of them. Trajectories never interact (bin/pqcxms runs
+ * each as its own process), so groups of small molecules can take several
+ * steps while the largest molecules take one. qcx_batch_step_paced gives group
+ * 0 nsteps steps and every other group as many as fit into the same time, from
+ * the per-step times the previous paced call measured (the first call gives
+ * every group nsteps). Both return 0 or -1. */
+int qcx_batch_step_groups(qcx_batch* b, const int32_t* nsteps, double tstep);
+int qcx_batch_step_paced(qcx_batch* b, int nsteps, double tstep);
+/* Number of groups; group_of_mol [nmol], the step counts of the last grouped
+ * call nsteps_last [ngroup] and the measured per-step times ms_per_step
+ * [ngroup] (0: not measured yet) when not NULL. */
+int qcx_batch_group_info(qcx_batch* b, int32_t* group_of_mol, int32_t* nsteps_last, double* ms_per_step);
+/* SCC iterations run so far per molecule (all launches), iter_sum [nmol]. */
+int qcx_batch_get_iterations(qcx_batch* b, int64_t* iter_sum);
+
 /* Copy host state in. Any pointer may be NULL to keep the current value.
  * xyz, vel: [natom][3]; mass: [natom] (atomic units). New coordinates start
  * every trajectory afresh: stopped ones run again, suspended SCCs are dropped. */

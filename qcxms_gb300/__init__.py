@@ -120,6 +120,10 @@ def load_library(build_if_missing=True):
     lib.qcx_boltz.argtypes = [c_int, c_int, c_int, c_double, P(c_double), P(c_double)]
     lib.qcx_batch_set_keep_mo.argtypes = [ctypes.c_void_p, c_int]
     lib.qcx_batch_set_scc_budget.argtypes = [ctypes.c_void_p, c_int]
+    lib.qcx_batch_step_groups.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), c_double]
+    lib.qcx_batch_step_paced.argtypes = [ctypes.c_void_p, c_int, c_double]
+    lib.qcx_batch_group_info.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double)]
+    lib.qcx_batch_get_iterations.argtypes = [ctypes.c_void_p, P(ctypes.c_int64)]
     lib.qcx_batch_mo_populations.argtypes = [ctypes.c_void_p, c_int, P(c_double), P(c_double), P(c_double),
                                              P(ctypes.c_int32)]
     lib.qcx_mo_spectrum.argtypes = [c_int, c_int, P(ctypes.c_int32), P(c_double), c_int, c_int, c_double,
@@ -415,6 +419,34 @@ class Batch:
 
     def step(self, nsteps, tstep=0.5 * constants.FSTOAU):
         self._check(self._lib.qcx_batch_step(self._h, int(nsteps), float(tstep)), "step")
+
+    def step_groups(self, nsteps, tstep=0.5 * constants.FSTOAU):
+        """Group g (by size, 0 = largest) takes nsteps[g] MD steps, every group
+        from its own graph on its own stream, concurrently."""
+        n = np.ascontiguousarray(nsteps, dtype=np.int32)
+        self._check(self._lib.qcx_batch_step_groups(self._h, _ip(n), float(tstep)), "step_groups")
+
+    def step_paced(self, nsteps=1, tstep=0.5 * constants.FSTOAU):
+        """The largest molecules' group takes nsteps steps, every other group as
+        many as fit into the same time (measured at the previous paced call)."""
+        self._check(self._lib.qcx_batch_step_paced(self._h, int(nsteps), float(tstep)), "step_paced")
+
+    def group_info(self):
+        """(group of every molecule, step counts of the last grouped call, measured ms per step)."""
+        g = np.zeros(self.nmol, dtype=np.int32)
+        n = np.zeros(64, dtype=np.int32)
+        t = np.zeros(64)
+        ng = self._lib.qcx_batch_group_info(self._h, _ip(g), _ip(n), _dp(t))
+        if ng < 0:
+            raise RuntimeError("group_info failed: " + _err(self._lib))
+        return g, n[:ng].copy(), t[:ng].copy()
+
+    def iterations(self):
+        """SCC iterations run so far per molecule (all launches)."""
+        it = np.zeros(self.nmol, dtype=np.int64)
+        self._check(self._lib.qcx_batch_get_iterations(self._h, it.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))),
+                    "iterations")
+        return it
 
     def sync(self):
         self._check(self._lib.qcx_batch_sync(self._h), "sync")

@@ -113,6 +113,21 @@ struct qcx_batch {
   double* d_md_heat = nullptr;  // [nmol][3] eimp, fadd, nadd (qcx_batch_set_md_heating)
   double* d_velof = nullptr;    // [natom] velocity scaling weights of the heating
   SccCarry* d_carry = nullptr;  // [nmol] state of suspended SCCs (qcx_batch_set_scc_budget)
+  long long* d_iter_sum = nullptr;  // [nmol] SCC iterations run
+  // Size-bucketed stepping (qcx_batch_step_groups / _paced): one step graph per
+  // molecule group, replayed on the group's own stream as often as the group's
+  // step count asks; the group's atoms for its atom-level kernels.
+  int* d_gatoms = nullptr;
+  std::vector<int> g_atom_start, g_atom_count;
+  std::vector<cudaGraph_t> gg_graph;
+  std::vector<cudaGraphExec_t> gg_exec;
+  double gg_tstep = 0.0;
+  std::vector<int> gg_kernels;           // kernels in each group's step graph
+  std::vector<cudaEvent_t> gg_end;       // per group: end of its steps in the last paced call
+  cudaEvent_t gg_start = nullptr;
+  std::vector<int> gg_n;                 // steps of each group in the last paced call
+  std::vector<double> gg_ms_per_step;    // measured per-step time of each group (0: unknown)
+  bool gg_pending_times = false;         // the last paced call's events are not read yet
   double* d_avxyz = nullptr;    // [natom][3] coordinate sums of the averaged structure
   bool md_heat = false;
   std::vector<double> h_eimp;   // eimp of every trajectory (qcx_batch_set_md_heating)
@@ -139,6 +154,7 @@ struct qcx_batch {
   // of groups that converge early overlap the SCC of the slowest molecules.
   int ngroup = 1;
   std::vector<int> g_start, g_count;      // range of each group in the size order
+  std::vector<int> g_smem;                // SCC shared memory of each group (its largest molecule's)
   std::vector<int> g_pair_start;          // first pair of each group in d_gpairs
   std::vector<std::array<int, 10>> g_pair_off;  // class offsets inside the group
   ShellPair* d_gpairs = nullptr;          // shell pairs ordered by group, then class
@@ -162,6 +178,11 @@ DevBatch group_dev(const qcx_batch* b, int g) {
   d.pairs = b->d_gpairs + b->g_pair_start[g];
   for (int c = 0; c < 10; ++c) d.pair_off[c] = b->g_pair_off[g][c];
   d.npair = d.pair_off[9];
+  d.atom_list = b->d_gatoms + b->g_atom_start[g];
+  d.natom_list = b->g_atom_count[g];
+  // shared memory for the group's largest molecule only: groups of small
+  // molecules leave room for more CTAs per SM
+  d.smem_bytes = b->g_smem[g];
   return d;
 }
 
@@ -238,6 +259,15 @@ void free_batch(qcx_batch* b) {
   if (b->d_cid) cudaFree(b->d_cid);
   if (b->d_velof) cudaFree(b->d_velof);
   if (b->d_carry) cudaFree(b->d_carry);
+  if (b->d_iter_sum) cudaFree(b->d_iter_sum);
+  if (b->d_gatoms) cudaFree(b->d_gatoms);
+  for (cudaGraphExec_t e : b->gg_exec)
+    if (e) cudaGraphExecDestroy(e);
+  for (cudaGraph_t g : b->gg_graph)
+    if (g) cudaGraphDestroy(g);
+  for (cudaEvent_t e : b->gg_end)
+    if (e) cudaEventDestroy(e);
+  if (b->gg_start) cudaEventDestroy(b->gg_start);
   for (size_t g = 1; g < b->g_stream.size(); ++g)
     if (b->g_stream[g]) cudaStreamDestroy(b->g_stream[g]);
   for (cudaEvent_t e : b->g_join)
@@ -255,6 +285,14 @@ static void drop_graph(qcx_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   b->graph_exec = nullptr;
   b->graph = nullptr;
+  for (cudaGraphExec_t& e : b->gg_exec) {
+    if (e) cudaGraphExecDestroy(e);
+    e = nullptr;
+  }
+  for (cudaGraph_t& g : b->gg_graph) {
+    if (g) cudaGraphDestroy(g);
+    g = nullptr;
+  }
 }
 
 int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, const double* charge,
@@ -337,7 +375,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
       dalloc(&b->d_energy, (size_t)nmol * kNumEnergy) || dalloc(&b->d_ekin, nmol) || dalloc(&b->d_status, nmol) ||
       dalloc(&b->d_iters, nmol) || dalloc(&b->d_active, nmol) || dalloc(&b->d_steps, nmol) ||
       dalloc(&b->d_order, nmol) || dalloc(&b->d_have_prev, nmol) || dalloc(&b->d_frag, na) ||
-      dalloc(&b->d_nfrag, nmol) || dalloc(&b->d_frad, kMaxZ + 1))
+      dalloc(&b->d_nfrag, nmol) || dalloc(&b->d_frad, kMaxZ + 1) || dalloc(&b->d_iter_sum, nmol))
     return -1;
   {
     // launch order of the per-molecule kernels: decreasing nao^3 (work of the SCC)
@@ -357,6 +395,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
       const int k0 = (int)((long long)g * nmol / G), k1 = (int)((long long)(g + 1) * nmol / G);
       b->g_start.push_back(k0);
       b->g_count.push_back(k1 - k0);
+      b->g_smem.push_back((int)scc_smem_bytes(b->mol[order[k0]].nao, 0));
       b->g_pair_start.push_back((int)gp.size());
       std::array<int, 10> off{};
       for (int c = 0; c < 9; ++c) {
@@ -371,6 +410,26 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
       off[9] = (int)gp.size() - b->g_pair_start[g];
       b->g_pair_off.push_back(off);
     }
+    // every group's atoms, for the atom-level kernels of its own step graph
+    std::vector<int> gatoms;
+    for (int g = 0; g < G; ++g) {
+      b->g_atom_start.push_back((int)gatoms.size());
+      for (int k = b->g_start[g]; k < b->g_start[g] + b->g_count[g]; ++k) {
+        const MolDesc& md = b->mol[order[k]];
+        for (int a = 0; a < md.nat; ++a) gatoms.push_back(md.atom_off + a);
+      }
+      b->g_atom_count.push_back((int)gatoms.size() - b->g_atom_start[g]);
+    }
+    if (dalloc(&b->d_gatoms, gatoms.size())) return -1;
+    CK(cudaMemcpy(b->d_gatoms, gatoms.data(), sizeof(int) * gatoms.size(), cudaMemcpyHostToDevice));
+    b->gg_graph.assign(G, nullptr);
+    b->gg_exec.assign(G, nullptr);
+    b->gg_end.assign(G, nullptr);
+    b->gg_n.assign(G, 0);
+    b->gg_kernels.assign(G, 0);
+    b->gg_ms_per_step.assign(G, 0.0);
+    for (int g = 0; g < G; ++g) CK(cudaEventCreate(&b->gg_end[g]));
+    CK(cudaEventCreate(&b->gg_start));
     if (dalloc(&b->d_gpairs, gp.size())) return -1;
     CK(cudaMemcpy(b->d_gpairs, gp.data(), sizeof(ShellPair) * gp.size(), cudaMemcpyHostToDevice));
     b->g_stream.assign(G, nullptr);
@@ -398,6 +457,7 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   CK(cudaMemset(b->d_energy, 0, sizeof(double) * nmol * kNumEnergy));
   CK(cudaMemset(b->d_ekin, 0, sizeof(double) * nmol));
   CK(cudaMemset(b->d_steps, 0, sizeof(long long) * nmol));
+  CK(cudaMemset(b->d_iter_sum, 0, sizeof(long long) * nmol));
   CK(cudaMemset(b->d_have_prev, 0, sizeof(int) * nmol));
   {
     // radii of the fragment test: src/covalent_radii.f90:89 (Rad, Angstrom) times
@@ -459,6 +519,9 @@ int build_batch(qcx_batch* b, int nmol, const int32_t* nat, const int32_t* num, 
   d.ekin = b->d_ekin;
   d.active = b->d_active;
   d.steps_done = b->d_steps;
+  d.iter_sum = b->d_iter_sum;
+  d.atom_list = nullptr;
+  d.natom_list = 0;
   d.have_prev = b->d_have_prev;
   d.guess = 0;
   d.checkqc = 1;
@@ -722,12 +785,7 @@ int qcx_batch_set_guess(qcx_batch* b, int guess) {
     set_error("qcx_batch_set_guess: guess must be 0 (zero moments) or 1 (previous converged moments)");
     return -1;
   }
-  if (guess != b->dev.guess && b->graph_exec) {
-    cudaGraphExecDestroy(b->graph_exec);
-    cudaGraphDestroy(b->graph);
-    b->graph_exec = nullptr;
-    b->graph = nullptr;
-  }
+  if (guess != b->dev.guess) drop_graph(b);
   b->dev.guess = guess;
   return 0;
 }
@@ -736,12 +794,7 @@ int qcx_batch_set_precision(qcx_batch* b, int precision) {
     set_error("qcx_batch_set_precision: precision must be 0 (FP64) or 1 (mixed)");
     return -1;
   }
-  if (precision != b->precision && b->graph_exec) {
-    cudaGraphExecDestroy(b->graph_exec);
-    cudaGraphDestroy(b->graph);
-    b->graph_exec = nullptr;
-    b->graph = nullptr;
-  }
+  if (precision != b->precision) drop_graph(b);
   b->precision = precision;
   return 0;
 }
@@ -838,6 +891,154 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
   for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(b->graph_exec, b->stream));
   b->launches = (long long)nsteps * b->step_launches;
   return check_launch();
+}
+
+}  // extern "C"
+
+namespace {
+// Captures the step graph of molecule group g on the group's stream: leapfrog,
+// coordination numbers, integrals, SCC and gradient of the group's molecules,
+// then the device loop rules when they are on. Returns its kernel count or -1.
+int capture_group(qcx_batch* b, int g, double tstep) {
+  cudaStream_t st = b->g_stream[g];
+  const DevBatch gd = group_dev(b, g);
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int n = 3;
+  launch_leapfrog(gd, tstep, st);
+  launch_cn(gd, st);
+  launch_zero_grad(gd, st);
+  n += launch_integrals(gd, st);
+  launch_scc(gd, b->precision, st);
+  n += 2 + launch_grad_pairs(gd, st);
+  launch_grad_atoms(gd, st);
+  if (b->md_on) {
+    launch_fragments(gd, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, st);
+    MdRules r = b->md_rules;
+    r.tstep = tstep;
+    r.max_nat = b->max_nat;
+    launch_md_rules(gd, b->d_md, b->d_frag, b->d_nfrag, b->md_heat ? b->d_velof : nullptr, b->d_avxyz, r, st);
+    n += 2;
+  }
+  if (b->cid_on) {
+    launch_fragments(gd, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, st, 1);
+    CidRules r = b->cid_rules;
+    r.tstep = tstep;
+    launch_cid_rules(gd, b->d_cid, b->d_nfrag, r, st);
+    n += 2;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    set_error(std::string("group step graph capture failed: ") + cudaGetErrorString(ce));
+    return -1;
+  }
+  b->gg_graph[g] = graph;
+  CK(cudaGraphInstantiate(&b->gg_exec[g], graph, 0));
+  return n;
+}
+}  // namespace
+
+extern "C" {
+
+int qcx_batch_step_groups(qcx_batch* b, const int32_t* nsteps, double tstep) {
+  if (!b || !nsteps) {
+    set_error("qcx_batch_step_groups: invalid arguments");
+    return -1;
+  }
+  const int G = b->ngroup;
+  for (int g = 0; g < G; ++g)
+    if (nsteps[g] < 0) {
+      set_error("qcx_batch_step_groups: negative step count");
+      return -1;
+    }
+  if (b->gg_tstep != tstep || !b->gg_exec[0]) {
+    for (int g = 0; g < G; ++g) {
+      if (b->gg_exec[g]) cudaGraphExecDestroy(b->gg_exec[g]);
+      if (b->gg_graph[g]) cudaGraphDestroy(b->gg_graph[g]);
+      b->gg_exec[g] = nullptr;
+      b->gg_graph[g] = nullptr;
+    }
+    for (int g = 0; g < G; ++g) {
+      const int n = capture_group(b, g, tstep);
+      if (n < 0) return -1;
+      b->gg_kernels[g] = n;
+    }
+    b->gg_tstep = tstep;
+  }
+  // every group starts after the work queued so far on the batch stream and
+  // the batch stream continues after every group's last step
+  CK(cudaEventRecord(b->gg_start, b->stream));
+  long long launches = 0;
+  for (int g = 0; g < G; ++g) {
+    cudaStream_t st = b->g_stream[g];
+    if (g > 0) CK(cudaStreamWaitEvent(st, b->gg_start, 0));
+    for (int s = 0; s < nsteps[g]; ++s) CK(cudaGraphLaunch(b->gg_exec[g], st));
+    CK(cudaEventRecord(b->gg_end[g], st));
+    b->gg_n[g] = nsteps[g];
+    launches += (long long)nsteps[g] * b->gg_kernels[g];
+  }
+  for (int g = 1; g < G; ++g) CK(cudaStreamWaitEvent(b->stream, b->gg_end[g], 0));
+  b->gg_pending_times = true;
+  b->launches = launches;
+  return check_launch();
+}
+
+int qcx_batch_step_paced(qcx_batch* b, int nsteps, double tstep) {
+  if (!b || nsteps < 0) {
+    set_error("qcx_batch_step_paced: invalid arguments");
+    return -1;
+  }
+  const int G = b->ngroup;
+  // per-step time of every group from the previous call (when its work is done)
+  if (b->gg_pending_times) {
+    bool done = true;
+    for (int g = 0; g < G; ++g) done = done && cudaEventQuery(b->gg_end[g]) == cudaSuccess;
+    if (done) {
+      for (int g = 0; g < G; ++g) {
+        float ms = 0.f;
+        if (b->gg_n[g] > 0 && cudaEventElapsedTime(&ms, b->gg_start, b->gg_end[g]) == cudaSuccess) {
+          const double per = ms / b->gg_n[g];
+          double& t = b->gg_ms_per_step[g];
+          t = t > 0.0 ? 0.5 * (t + per) : per;
+        }
+      }
+      b->gg_pending_times = false;
+    }
+    cudaGetLastError();  // a query of unfinished work is not an error
+  }
+  // group 0 (the largest molecules) takes nsteps steps; every other group as
+  // many as fit into the same time, at least one
+  std::vector<int32_t> n(G, nsteps);
+  const double T = b->gg_ms_per_step[0] * nsteps;
+  for (int g = 1; g < G; ++g) {
+    const double t = b->gg_ms_per_step[g];
+    if (nsteps > 0 && T > 0.0 && t > 0.0) {
+      const double k = std::floor(T / t);
+      n[g] = (int32_t)std::max(1.0, std::min(k, 64.0 * nsteps));
+    }
+  }
+  return qcx_batch_step_groups(b, n.data(), tstep);
+}
+
+int qcx_batch_group_info(qcx_batch* b, int32_t* group_of_mol, int32_t* nsteps_last, double* ms_per_step) {
+  if (!b) return -1;
+  std::vector<int> order(b->nmol);
+  CK(cudaMemcpy(order.data(), b->d_order, sizeof(int) * b->nmol, cudaMemcpyDeviceToHost));
+  for (int g = 0; g < b->ngroup; ++g) {
+    for (int k = b->g_start[g]; k < b->g_start[g] + b->g_count[g]; ++k)
+      if (group_of_mol) group_of_mol[order[k]] = g;
+    if (nsteps_last) nsteps_last[g] = b->gg_n[g];
+    if (ms_per_step) ms_per_step[g] = b->gg_ms_per_step[g];
+  }
+  return b->ngroup;
+}
+
+int qcx_batch_get_iterations(qcx_batch* b, int64_t* iter_sum) {
+  if (!b || !iter_sum) return -1;
+  CK(cudaMemcpyAsync(iter_sum, b->d_iter_sum, sizeof(long long) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return 0;
 }
 
 int qcx_batch_get(qcx_batch* b, double* xyz, double* vel, double* grad, double* energy, double* qat, double* ekin,

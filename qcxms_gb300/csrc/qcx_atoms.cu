@@ -8,9 +8,16 @@ namespace qcx {
 // ---------------------------------------------------------------------------
 // coordination numbers, multipole radii and dispersion reference weights
 // ---------------------------------------------------------------------------
+// thread t of an atom-level kernel: atom t of the batch, or of the group's list
+__device__ inline int atom_of_thread(const DevBatch& bt, int t) {
+  if (bt.atom_list) return t < bt.natom_list ? bt.atom_list[t] : -1;
+  return t < bt.natom ? t : -1;
+}
+inline int atom_threads(const DevBatch& bt) { return bt.atom_list ? bt.natom_list : bt.natom; }
+
 __global__ void k_cn(DevBatch bt) {
-  int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= bt.natom) return;
+  const int a = atom_of_thread(bt, blockIdx.x * blockDim.x + threadIdx.x);
+  if (a < 0) return;
   if (!bt.active[bt.atom_mol[a]]) return;
   const Params& P = *bt.prm;
   const MolDesc md = bt.mol[bt.atom_mol[a]];
@@ -39,12 +46,12 @@ __global__ void k_cn(DevBatch bt) {
 
 void launch_cn(const DevBatch& bt, cudaStream_t st) {
   int threads = 128;
-  k_cn<<<(bt.natom + threads - 1) / threads, threads, 0, st>>>(bt);
+  k_cn<<<(atom_threads(bt) + threads - 1) / threads, threads, 0, st>>>(bt);
 }
 
 __global__ void k_zero_grad(DevBatch bt) {
-  int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= bt.natom) return;
+  const int a = atom_of_thread(bt, blockIdx.x * blockDim.x + threadIdx.x);
+  if (a < 0) return;
   if (!bt.active[bt.atom_mol[a]]) return;
   bt.grad[3 * a] = 0.0;
   bt.grad[3 * a + 1] = 0.0;
@@ -55,7 +62,7 @@ __global__ void k_zero_grad(DevBatch bt) {
 
 void launch_zero_grad(const DevBatch& bt, cudaStream_t st) {
   int threads = 128;
-  k_zero_grad<<<(bt.natom + threads - 1) / threads, threads, 0, st>>>(bt);
+  k_zero_grad<<<(atom_threads(bt) + threads - 1) / threads, threads, 0, st>>>(bt);
 }
 
 // ---------------------------------------------------------------------------
@@ -401,7 +408,7 @@ void launch_grad_atoms(const DevBatch& bt, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 __global__ void k_leapfrog(DevBatch bt, double tstep) {
   __shared__ double red[32];
-  const int mol = blockIdx.x;
+  const int mol = bt.order ? bt.order[blockIdx.x] : blockIdx.x;
   const MolDesc md = bt.mol[mol];
   // a trajectory whose SCC is pending has moved already and waits for its gradient
   if (!bt.active[mol] || scc_pending(bt, mol)) return;
@@ -452,7 +459,7 @@ constexpr int kFragThreads = 256;
 __global__ void __launch_bounds__(kFragThreads) k_fragments(DevBatch bt, const double* rad, double rcut, int at1,
                                                             int at2, int* frag, int* nfrag, int skip_last) {
   extern __shared__ int fsm[];
-  const int mol = blockIdx.x;
+  const int mol = bt.order ? bt.order[blockIdx.x] : blockIdx.x;
   const MolDesc md = bt.mol[mol];
   // skip_last: the last atom (a collision gas atom) is not part of the ion; it gets fragment 0
   const int nat = md.nat - (skip_last && md.nat > 1 ? 1 : 0), off = md.atom_off;

@@ -165,6 +165,10 @@ struct DevBatch {
   // next launch (kSccPending)
   int scc_budget, budget_nao;
   SccCarry* carry;   // [nmol] (allocated with the first nonzero budget)
+  long long* iter_sum;  // [nmol] SCC iterations run so far (all launches)
+  // atom-level kernels of one molecule group: the group's atoms (nullptr: all natom atoms)
+  const int* atom_list;
+  int natom_list;
   const int* order;  // [nmol] molecules by decreasing size: CTA b of a per-molecule kernel takes order[b]
   int max_nao;
   int smem_bytes;  // dynamic shared memory granted to the SCC kernel

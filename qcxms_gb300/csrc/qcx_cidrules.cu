@@ -86,8 +86,9 @@ __global__ void k_cid_begin(DevBatch bt, CidState* st, CidRules r) {
 }
 
 __global__ void k_cid_rules(DevBatch bt, CidState* st, const int* nfrag, CidRules r) {
-  const int mol = blockIdx.x * blockDim.x + threadIdx.x;
-  if (mol >= bt.nmol) return;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= bt.nmol) return;
+  const int mol = bt.order ? bt.order[idx] : idx;
   CidState s = st[mol];
   if (s.done || scc_pending(bt, mol)) return;  // a pending SCC: the step has not happened yet
   const MolDesc md = bt.mol[mol];

@@ -174,8 +174,9 @@ __global__ void __launch_bounds__(32 * kRulesWarps) k_md_rules(DevBatch bt, MdSt
                                                                double* avxyz, MdRules r) {
   extern __shared__ double md_terms[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int mol = blockIdx.x * kRulesWarps + warp;
-  if (mol >= bt.nmol) return;
+  const int idx = blockIdx.x * kRulesWarps + warp;
+  if (idx >= bt.nmol) return;
+  const int mol = bt.order ? bt.order[idx] : idx;
   double* terms = md_terms + (size_t)warp * r.max_nat;
   MdState s = st[mol];
   if (s.done || scc_pending(bt, mol)) return;  // a pending SCC: the step has not happened yet

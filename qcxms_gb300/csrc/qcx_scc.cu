@@ -2399,6 +2399,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       bt.carry[mol] = c;
       bt.status[mol] = kSccPending;
       bt.iters[mol] = it;
+      if (bt.iter_sum) bt.iter_sum[mol] += it - it0 + 1;
       if (bt.have_prev) bt.have_prev[mol] = basis_saved ? 2 : 0;
     }
     if (mc) mma_teardown(mctx);
@@ -2459,6 +2460,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     bt.status[mol] = st;
     if (bt.have_prev) bt.have_prev[mol] = (st == 0 ? 1 : 0) | (basis_saved ? 2 : 0);
     bt.iters[mol] = it;
+    if (bt.iter_sum) bt.iter_sum[mol] += it - it0 + 1;
   }
   if (mc) mma_teardown(mctx);
 }
