@@ -369,6 +369,15 @@ int qcx_boltz(int units, int nfrag, int mchrg, double temp, const double* ip, do
  * covered: the averaged structures and the output files.
  */
 int qcx_batch_set_cid_rules(qcx_batch* b, double tinit, int ntot);
+/* The averaged structure of every collision trajectory, as the collision loop
+ * hands it to the fragment IPs (src/cid.f90:1095-1101): after the ion fell
+ * into more fragments, the average over the steps counted while the fragments
+ * kept their atom counts (at most cnt_steps = 50, src/cid.f90:802-909); else
+ * the coordinate sum of the current window of dumpavg = 50 loop tops divided
+ * by its length. axyz [natom][3], the gas atom's rows 0. For trajectories still
+ * running: the value if the run ended now. Returns 0 or -1. */
+int qcx_batch_get_cid_avg_xyz(qcx_batch* b, double* axyz);
+
 /* State of the collision rules per trajectory (any pointer may be NULL). */
 int qcx_batch_get_cid_state(qcx_batch* b, int32_t* nstep, int32_t* nfrag, int32_t* collided, int32_t* fragmented,
                             int32_t* total_steps, int32_t* done, int32_t* failed, double* avg_temp,

@@ -441,19 +441,78 @@ def cid_rules_begin(xyz, mass, ntot):
     g = xyz[nuc]
     d0 = _norm3(g[0] - cm[0], g[1] - cm[1], g[2] - cm[2])
     s["lowest"] = s["highest"] = d0
+    # averaged structures: avxyz = avxyz2 = 0 (src/cid.f90:244-245), xyzavg_dump = 0
+    # (:715), check_fragmented = 1 (:265), count_average .false. (:147); save_natf
+    # has no initial value in the reference (0 here)
+    s["avxyz"] = np.zeros((nuc, 3))
+    s["avxyz2"] = np.zeros((nuc, 3))
+    s["store"] = np.zeros((nuc, 3))
+    s["xyzavg_dump"], s["cnt"], s["count_average"], s["check_fragmented"] = 0, 0, 0, 1
+    s["save_natf"] = [0] * 10
     return s
 
 
-def cid_rules_step(s, failed, xyz, vel, mass, nfrag, tstep, tinit):
-    """One step of the collision loop after leapfrog + egrad (src/cid.f90:739-1036)."""
+def _cid_average(s, xyz, nfrag, frag):
+    """src/cid.f90:802-909: the averaged structures after the fragment count."""
+    nuc = s["avxyz"].shape[0]
+    x = np.asarray(xyz, dtype=np.float64)[:nuc]
+    s["avxyz"] = s["avxyz"] + x
+    if nfrag > s["check_fragmented"]:
+        s["count_average"] = 1
+        s["check_fragmented"] = nfrag
+    if nfrag < s["check_fragmented"] and s["count_average"]:
+        s["cnt"] = 0
+        s["avxyz2"] = np.zeros((nuc, 3))
+        s["store"] = np.zeros((nuc, 3))
+        s["count_average"] = 0
+        s["check_fragmented"] = 1
+    if s["count_average"]:
+        s["cnt"] += 1
+        s["avxyz2"] = s["avxyz2"] + x
+        s["store"] = s["avxyz2"] / s["cnt"]
+        # avg_frag_struc (src/analyse.f90:452-502): atoms per fragment
+        natf = [0] * 10
+        for lab in list(frag)[:nuc]:
+            if 1 <= lab <= 10:
+                natf[lab - 1] += 1
+        for k in range(min(nfrag, 10)):
+            if s["cnt"] == 1:
+                s["save_natf"][k] = natf[k]
+            if natf[k] != s["save_natf"][k]:
+                s["cnt"] = 0
+                s["store"] = np.zeros((nuc, 3))
+                s["avxyz2"] = np.zeros((nuc, 3))
+                break
+        if s["cnt"] == 50:
+            s["store"] = s["avxyz2"] / s["cnt"]
+            s["avxyz2"] = np.zeros((nuc, 3))
+            s["cnt"] = 0
+            s["count_average"] = 0
+
+
+def cid_avg_xyz(s):
+    """The averaged structure the collision loop returns (src/cid.f90:1095-1101)."""
+    if s["check_fragmented"] > 1:
+        return s["store"].copy()
+    return s["avxyz"] / s["xyzavg_dump"]
+
+
+def cid_rules_step(s, failed, xyz, vel, mass, nfrag, tstep, tinit, frag=None):
+    """One step of the collision loop after leapfrog + egrad (src/cid.f90:739-1036).
+    frag: the ion's fragment numbers (for the averaged structures; every atom in
+    fragment 1 when not given)."""
     if s["done"]:
         return s
     autofs = 1.0 / FSTOAU
     mstoau = 1.0 / 2.18769126364e6
     nuc = len(mass) - 1
     s["nstep"] += 1
+    if s["xyzavg_dump"] == 50:  # src/cid.f90:743-746
+        s["xyzavg_dump"] = 0
+        s["avxyz"] = np.zeros((nuc, 3))
     s["ttime"] = s["ttime"] + tstep * autofs
     s["distance_dump"] += 1
+    s["xyzavg_dump"] += 1
     if failed:
         s["done"], s["failed"] = 1, 1
         return s
@@ -479,6 +538,7 @@ def cid_rules_step(s, failed, xyz, vel, mass, nfrag, tstep, tinit):
     mgas = mass[nuc]
     s["ecom"] = ((mgas / (mgas + s["summass"])) * e_velo) * AUTOEV
     s["nfrag"] = nfrag
+    _cid_average(s, xyz, nfrag, frag if frag is not None else [1] * nuc)
     if s["distance_dump"] == 10:
         s["distance_dump"] = 0
         g = xyz[nuc]

@@ -102,6 +102,7 @@ def load_library(build_if_missing=True):
                                      P(ctypes.c_int32)]
     lib.qcx_batch_get_md_avg_xyz.argtypes = [ctypes.c_void_p, P(c_double)]
     lib.qcx_batch_set_cid_rules.argtypes = [ctypes.c_void_p, c_double, c_int]
+    lib.qcx_batch_get_cid_avg_xyz.argtypes = [ctypes.c_void_p, P(c_double)]
     lib.qcx_batch_get_cid_state.argtypes = [ctypes.c_void_p] + [P(ctypes.c_int32)] * 7 + [P(c_double)] * 2
     lib.qcx_batch_set_md_heating.argtypes = [ctypes.c_void_p, P(c_double), P(c_double), P(c_double), c_double]
     lib.qcx_batch_set_md_etemp.argtypes = [ctypes.c_void_p, c_double, c_double]
@@ -548,6 +549,12 @@ class Batch:
         """Stop rules of the collision MD (src/cid.f90:739-1052) on the device;
         every molecule is the ion followed by one gas atom. Call after egrad()."""
         self._check(self._lib.qcx_batch_set_cid_rules(self._h, float(tinit), int(ntot)), "set_cid_rules")
+
+    def cid_avg_xyz(self):
+        """The collision loop's averaged structures [natom][3] (src/cid.f90:1095-1101)."""
+        a = np.zeros((self.natom, 3))
+        self._check(self._lib.qcx_batch_get_cid_avg_xyz(self._h, _dp(a)), "cid_avg_xyz")
+        return a
 
     def cid_state(self):
         n = self.nmol

@@ -137,6 +137,7 @@ struct qcx_batch {
   bool md_on = false;
   // collision MD stop rules on the device (qcx_batch_set_cid_rules)
   CidState* d_cid = nullptr;
+  double* d_cav = nullptr;  // [natom][9] the collision loop's averaged-structure sums
   bool cid_on = false;
   CidRules cid_rules{};
   MdRules md_rules{};
@@ -257,6 +258,7 @@ void free_batch(qcx_batch* b) {
   if (b->d_etemp0) cudaFree(b->d_etemp0);
   if (b->d_avxyz) cudaFree(b->d_avxyz);
   if (b->d_cid) cudaFree(b->d_cid);
+  if (b->d_cav) cudaFree(b->d_cav);
   if (b->d_velof) cudaFree(b->d_velof);
   if (b->d_carry) cudaFree(b->d_carry);
   if (b->d_iter_sum) cudaFree(b->d_iter_sum);
@@ -657,14 +659,41 @@ int qcx_batch_set_cid_rules(qcx_batch* b, double tinit, int ntot) {
     return -1;
   }
   if (!b->d_cid && dalloc(&b->d_cid, b->nmol)) return -1;
+  if (!b->d_cav && dalloc(&b->d_cav, 9 * (size_t)b->natom)) return -1;
   b->cid_rules.tinit = tinit;
   b->cid_rules.ntot = ntot;
-  launch_cid_begin(b->dev, b->d_cid, b->cid_rules, b->stream);
+  launch_cid_begin(b->dev, b->d_cid, b->d_cav, b->cid_rules, b->stream);
   if (check_launch()) return -1;
   CK(cudaStreamSynchronize(b->stream));
   drop_graph(b);
   b->cid_on = true;
   b->md_on = false;
+  return 0;
+}
+
+int qcx_batch_get_cid_avg_xyz(qcx_batch* b, double* axyz) {
+  if (!b || !b->d_cid || !axyz) {
+    set_error("qcx_batch_get_cid_avg_xyz: no collision rules set");
+    return -1;
+  }
+  std::vector<CidState> st(b->nmol);
+  std::vector<double> av(9 * (size_t)b->natom);
+  CK(cudaMemcpyAsync(st.data(), b->d_cid, sizeof(CidState) * b->nmol, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaMemcpyAsync(av.data(), b->d_cav, sizeof(double) * av.size(), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  // src/cid.f90:1095-1101: the fragments' average when the ion fell apart,
+  // else the current window's sum over its steps
+  for (int m = 0; m < b->nmol; ++m) {
+    const MolDesc& md = b->mol[m];
+    for (int i = 0; i < md.nat; ++i)
+      for (int d = 0; d < 3; ++d) {
+        const size_t a = (size_t)(md.atom_off + i);
+        double v = 0.0;
+        if (i < md.nat - 1)
+          v = st[m].check_fragmented > 1 ? av[9 * a + 6 + d] : av[9 * a + d] / (double)st[m].xyzavg_dump;
+        axyz[3 * a + d] = v;
+      }
+  }
   return 0;
 }
 
@@ -873,7 +902,7 @@ int qcx_batch_step(qcx_batch* b, int nsteps, double tstep) {
       launch_fragments(b->dev, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, b->stream, 1);
       CidRules r = b->cid_rules;
       r.tstep = tstep;
-      launch_cid_rules(b->dev, b->d_cid, b->d_nfrag, r, b->stream);
+      launch_cid_rules(b->dev, b->d_cid, b->d_frag, b->d_nfrag, b->d_cav, r, b->stream);
       n += 2;
     }
     if (n >= 0 && mark(b, marks, 1 + 4 * b->ngroup, b->stream)) n = -1;
@@ -923,7 +952,7 @@ int capture_group(qcx_batch* b, int g, double tstep) {
     launch_fragments(gd, b->max_nat, b->d_frad, 3.0, 1, 0, b->d_frag, b->d_nfrag, st, 1);
     CidRules r = b->cid_rules;
     r.tstep = tstep;
-    launch_cid_rules(gd, b->d_cid, b->d_nfrag, r, st);
+    launch_cid_rules(gd, b->d_cid, b->d_frag, b->d_nfrag, b->d_cav, r, st);
     n += 2;
   }
   cudaGraph_t graph = nullptr;

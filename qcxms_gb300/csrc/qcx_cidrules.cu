@@ -12,9 +12,10 @@
 // 800 * (2 tstep in fs) steps later (src/cid.f90:955-985); after a
 // fragmentation that follows the collision the end moves to add_steps after
 // it (src/cid.f90:988-1001, add_steps from the ion size, src/cid.f90:276-278);
-// and stops at that step (src/cid.f90:1030-1036). One thread per trajectory,
-// the reference's operation order with explicit roundings. Not covered: the
-// averaged structures and the output files.
+// and stops at that step (src/cid.f90:1030-1036). It also keeps the averaged
+// structures that the fragment IPs take (src/cid.f90:743-746, 802-909, the
+// result at 1095-1101). One thread per trajectory, the reference's operation
+// order with explicit roundings. Not covered: the output files.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -62,12 +63,17 @@ __device__ bool failed_eval(const DevBatch& bt, int mol) {
 
 }  // namespace
 
-__global__ void k_cid_begin(DevBatch bt, CidState* st, CidRules r) {
+__global__ void k_cid_begin(DevBatch bt, CidState* st, double* cav, CidRules r) {
   const int mol = blockIdx.x * blockDim.x + threadIdx.x;
   if (mol >= bt.nmol) return;
   const MolDesc md = bt.mol[mol];
   CidState s = {};
   s.total_steps = r.ntot;
+  // avxyz = avxyz2 = 0 (src/cid.f90:244-245), check_fragmented = 1 (:265);
+  // count_average starts .false. (its initialiser, :147); save_natf has no
+  // initial value in the reference and starts at 0 here
+  s.check_fragmented = 1;
+  for (long long e = 9LL * md.atom_off; e < 9LL * (md.atom_off + md.nat); ++e) cav[e] = 0.0;
   const int nuc = md.nat - 1;
   for (int i = 0; i < nuc; ++i) s.summass = __dadd_rn(s.summass, bt.mass[md.atom_off + i]);
   double cm[3];
@@ -85,7 +91,7 @@ __global__ void k_cid_begin(DevBatch bt, CidState* st, CidRules r) {
   st[mol] = s;
 }
 
-__global__ void k_cid_rules(DevBatch bt, CidState* st, const int* nfrag, CidRules r) {
+__global__ void k_cid_rules(DevBatch bt, CidState* st, const int* frag, const int* nfrag, double* cav, CidRules r) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= bt.nmol) return;
   const int mol = bt.order ? bt.order[idx] : idx;
@@ -94,8 +100,16 @@ __global__ void k_cid_rules(DevBatch bt, CidState* st, const int* nfrag, CidRule
   const MolDesc md = bt.mol[mol];
   const int nuc = md.nat - 1;
   s.nstep += 1;
+  double* av = cav + 9LL * md.atom_off;  // per ion atom: avxyz, avxyz2, store_avxyz
+  // a new window of the averaged structure every dumpavg = 50 loop tops (src/cid.f90:743-746)
+  if (s.xyzavg_dump == 50) {
+    s.xyzavg_dump = 0;
+    for (int i = 0; i < nuc; ++i)
+      for (int d = 0; d < 3; ++d) av[9 * i + d] = 0.0;
+  }
   s.ttime = __dadd_rn(s.ttime, __dmul_rn(r.tstep, kAutoFs));
   s.distance_dump += 1;
+  s.xyzavg_dump += 1;
   if (failed_eval(bt, mol)) {
     s.done = 1;
     s.failed = 1;
@@ -129,6 +143,61 @@ __global__ void k_cid_rules(DevBatch bt, CidState* st, const int* nfrag, CidRule
   const double mgas = bt.mass[md.atom_off + nuc];
   s.ecom = __dmul_rn(__dmul_rn(__ddiv_rn(mgas, __dadd_rn(mgas, s.summass)), e_velo), kAutoEV);
   s.nfrag = nfrag[mol];
+  // averaged structures (src/cid.f90:802-909): avxyz sums every step of the
+  // window; after the ion has fallen into more fragments, avxyz2 sums up to
+  // cnt_steps = 50 steps as long as the fragments keep their atom counts
+  {
+    const int nf = s.nfrag;
+    const double* x = bt.xyz + 3LL * md.atom_off;
+    for (int i = 0; i < nuc; ++i)
+      for (int d = 0; d < 3; ++d) av[9 * i + d] = __dadd_rn(av[9 * i + d], x[3 * i + d]);
+    if (nf > s.check_fragmented) {
+      s.count_average = 1;
+      s.check_fragmented = nf;
+    }
+    if (nf < s.check_fragmented && s.count_average) {
+      s.cnt = 0;
+      for (int i = 0; i < nuc; ++i)
+        for (int d = 3; d < 9; ++d) av[9 * i + d] = 0.0;
+      s.count_average = 0;
+      s.check_fragmented = 1;
+    }
+    if (s.count_average) {
+      s.cnt += 1;
+      for (int i = 0; i < nuc; ++i)
+        for (int d = 0; d < 3; ++d) {
+          av[9 * i + 3 + d] = __dadd_rn(av[9 * i + 3 + d], x[3 * i + d]);
+          av[9 * i + 6 + d] = __ddiv_rn(av[9 * i + 3 + d], (double)s.cnt);
+        }
+      // avg_frag_struc (src/analyse.f90:452-502): the atom count of every
+      // fragment (its arrays hold 10 fragments)
+      int natf[10];
+      for (int k = 0; k < 10; ++k) natf[k] = 0;
+      const int* lab = frag + md.atom_off;
+      for (int i = 0; i < nuc; ++i)
+        if (lab[i] >= 1 && lab[i] <= 10) natf[lab[i] - 1] += 1;
+      const int nchk = nf < 10 ? nf : 10;
+      for (int k = 0; k < nchk; ++k) {
+        if (s.cnt == 1) s.save_natf[k] = natf[k];
+        if (natf[k] != s.save_natf[k]) {
+          // a fragment changed: the count starts again (src/cid.f90:860-866)
+          s.cnt = 0;
+          for (int i = 0; i < nuc; ++i)
+            for (int d = 3; d < 9; ++d) av[9 * i + d] = 0.0;
+          break;
+        }
+      }
+      if (s.cnt == 50) {
+        for (int i = 0; i < nuc; ++i)
+          for (int d = 0; d < 3; ++d) {
+            av[9 * i + 6 + d] = __ddiv_rn(av[9 * i + 3 + d], (double)s.cnt);
+            av[9 * i + 3 + d] = 0.0;
+          }
+        s.cnt = 0;
+        s.count_average = 0;
+      }
+    }
+  }
   if (s.distance_dump == 10) {
     s.distance_dump = 0;
     const double dist = gas_distance(bt, md, cm);
@@ -152,12 +221,13 @@ __global__ void k_cid_rules(DevBatch bt, CidState* st, const int* nfrag, CidRule
   st[mol] = s;
 }
 
-void launch_cid_begin(const DevBatch& bt, CidState* st, const CidRules& r, cudaStream_t stream) {
-  k_cid_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, r);
+void launch_cid_begin(const DevBatch& bt, CidState* st, double* cav, const CidRules& r, cudaStream_t stream) {
+  k_cid_begin<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, cav, r);
 }
 
-void launch_cid_rules(const DevBatch& bt, CidState* st, const int* nfrag, const CidRules& r, cudaStream_t stream) {
-  k_cid_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, nfrag, r);
+void launch_cid_rules(const DevBatch& bt, CidState* st, const int* frag, const int* nfrag, double* cav,
+                      const CidRules& r, cudaStream_t stream) {
+  k_cid_rules<<<(bt.nmol + 127) / 128, 128, 0, stream>>>(bt, st, frag, nfrag, cav, r);
 }
 
 }  // namespace qcx

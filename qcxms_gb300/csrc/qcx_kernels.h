@@ -72,13 +72,20 @@ struct CidState {
   int nstep, m, step_counter, collided, fragmented, total_steps, nfrag, done, failed, distance_dump;
   double ttime, tav, avgT, lowest, highest, new_temp, ecom, summass;
   double old_cm[3];
+  // averaged structures (src/cid.f90:743-746, 802-909): the window counter of
+  // avxyz, the count of avxyz2, whether the fragments' structure is averaged,
+  // the fragment count that started it and the fragments' atom counts then
+  int xyzavg_dump, cnt, count_average, check_fragmented;
+  int save_natf[10];
 };
 struct CidRules {
   double tinit, tstep;
   int ntot;
 };
-void launch_cid_begin(const DevBatch& bt, CidState* st, const CidRules& r, cudaStream_t stream);
-void launch_cid_rules(const DevBatch& bt, CidState* st, const int* nfrag, const CidRules& r, cudaStream_t stream);
+// cav [natom][9]: per ion atom avxyz (3), avxyz2 (3) and store_avxyz (3)
+void launch_cid_begin(const DevBatch& bt, CidState* st, double* cav, const CidRules& r, cudaStream_t stream);
+void launch_cid_rules(const DevBatch& bt, CidState* st, const int* frag, const int* nfrag, double* cav,
+                      const CidRules& r, cudaStream_t stream);
 
 // sets the text qcx_last_error() returns
 void set_last_error(const std::string& s);

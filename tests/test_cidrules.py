@@ -83,6 +83,62 @@ def test_gas_atom_mass_is_the_reference_literal(oracle_lib):
         assert abs(s["ecom"] - (m_ar / (m_ar + summass)) * e_velo * constants.AUTOEV) < 1e-12 * s["ecom"]
 
 
+def test_oracle_averaged_structures_known_answers(oracle_lib):
+    """src/cid.f90:743-746, 802-909, 1095-1101 on a constructed run: a 4-atom ion
+    (gas atom approaching, so no collision) whose coordinates are known per step.
+    Steps 1-60 one fragment: the window restarts after 50 loop tops, the result
+    is the mean of steps 51-60. Steps 61-80 two fragments (2 + 2 atoms): the
+    fragments' mean over 61-80. At step 81 a fragment changes its atom count
+    (1 + 3): the count restarts, steps 82-131 fill it to cnt_steps = 50 and the
+    average freezes; later steps (and the ion going back to one fragment)
+    leave it."""
+    o = oracle_lib
+    mass = [1.0, 1.0, 1.0, 1.0, 40.0]
+    vel = [[0.0] * 3] * 5
+    rng = np.random.default_rng(3)
+    base = rng.normal(size=(4, 3))
+
+    def xyz(k):
+        x = np.vstack([base + 0.01 * k * np.arange(1, 13).reshape(4, 3), [[60.0 - 0.01 * k, 0.0, 0.0]]])
+        return x
+
+    def labels(k):
+        if k <= 60:
+            return [1, 1, 1, 1], 1
+        if k <= 80:
+            return [1, 1, 2, 2], 2
+        if k <= 140:
+            return [1, 2, 2, 2], 2
+        return [1, 1, 1, 1], 1
+
+    s = o.cid_rules_begin(xyz(0), mass, 100000)
+    for k in range(1, 61):
+        lab, nf = labels(k)
+        o.cid_rules_step(s, False, xyz(k), vel, mass, nf, DT, 300.0, frag=lab)
+    want = sum(xyz(k)[:4] for k in range(51, 61)) / 10
+    assert np.allclose(o.cid_avg_xyz(s), want, rtol=0, atol=1e-12)
+    assert s["xyzavg_dump"] == 10 and s["check_fragmented"] == 1
+    for k in range(61, 81):
+        lab, nf = labels(k)
+        o.cid_rules_step(s, False, xyz(k), vel, mass, nf, DT, 300.0, frag=lab)
+    assert s["count_average"] == 1 and s["cnt"] == 20
+    assert np.allclose(o.cid_avg_xyz(s), sum(xyz(k)[:4] for k in range(61, 81)) / 20, rtol=0, atol=1e-12)
+    lab, nf = labels(81)
+    o.cid_rules_step(s, False, xyz(81), vel, mass, nf, DT, 300.0, frag=lab)
+    assert s["cnt"] == 0 and np.all(o.cid_avg_xyz(s) == 0.0)
+    for k in range(82, 132):
+        lab, nf = labels(k)
+        o.cid_rules_step(s, False, xyz(k), vel, mass, nf, DT, 300.0, frag=lab)
+    frozen = sum(xyz(k)[:4] for k in range(82, 132)) / 50
+    assert s["count_average"] == 0 and s["cnt"] == 0
+    assert np.allclose(o.cid_avg_xyz(s), frozen, rtol=0, atol=1e-12)
+    for k in range(132, 160):
+        lab, nf = labels(k)
+        o.cid_rules_step(s, False, xyz(k), vel, mass, nf, DT, 300.0, frag=lab)
+    assert s["check_fragmented"] == 2 and np.allclose(o.cid_avg_xyz(s), frozen, rtol=0, atol=1e-12)
+    assert not s["done"] and not s["collided"]
+
+
 @pytest.mark.gpu
 def test_gpu_cid_rules_match_oracle(gpu, oracle_lib):
     o = oracle_lib
@@ -110,9 +166,15 @@ def test_gpu_cid_rules_match_oracle(gpu, oracle_lib):
         r = b.get()
         for i, m in enumerate(mols):
             sl = slice(off[i], off[i + 1])
-            nf = o.fragments(m["Z"][:-1], r["xyz"][sl][:-1])[1]
+            lab, nf = o.fragments(m["Z"][:-1], r["xyz"][sl][:-1])
             o.cid_rules_step(ref[i], bool(r["status"][i] & fail), r["xyz"][sl], r["vel"][sl], list(m["mass"]), nf,
-                             DT, tinit)
+                             DT, tinit, frag=list(lab))
+        if step % 20 == 19:
+            ax = b.cid_avg_xyz()
+            for i in range(len(mols)):
+                sl = slice(off[i], off[i + 1] - 1)
+                want = o.cid_avg_xyz(ref[i])
+                assert np.array_equal(ax[sl], want), (step, i)
     # the set exercises the collision detection (how many collide within 160
     # steps depends on the trajectories' SCC paths; the CPU oracle's own runs
     # of the same set collide 5 times)
