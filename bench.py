@@ -56,6 +56,8 @@ NTRAJ, NMIN, NMAX = 256, 5, 40
 # iterations gave the highest completed-step rate of 10-120 (and of a flat or
 # linear scaling with n).
 SCC_BUDGET = 20
+# candidates of the budget autotuner of paced runs (0: no budget)
+AUTOTUNE_BUDGETS = (0, 10, 20, 40)
 DT_FS = 0.5
 ETEMP = 300.0
 
@@ -371,6 +373,11 @@ def run_gpu(args):
     # steps: the groups' SCC launches overlap one another and the other kernels,
     # so the SCC rate is taken over the whole timed region.
     b.set_timing(not paced)
+    tune = None
+    if paced and not args.no_autotune:
+        # untimed: pick the per-step SCC budget on this batch (real MD steps)
+        best, rates = b.autotune_budget(AUTOTUNE_BUDGETS, calls=2, tstep=dt)
+        tune = {"candidates": {str(k): round(v, 1) for k, v in rates.items()}, "chosen": best}
     for _ in range(args.warmup):
         one_step()
     barrier()
@@ -493,7 +500,8 @@ def run_gpu(args):
                        "atoms": [NMIN, NMAX] if args.workload == "batch" else [10, 81],
                        "etemp_K": ETEMP, "precision": args.precision, "scc_guess": args.guess,
                        "scc_iteration_limit": 250,
-                       "scc_budget_per_step": args.scc_budget,
+                       "scc_budget_per_step": tune["chosen"] if tune else args.scc_budget,
+                       "scc_budget_autotune": tune,
                        "arithmetic": ("FP32 SCC iterations, then double-float (hi+lo FP32) finishing iterations; "
                                       "FP64 integrals, potentials of the finishing iterations, Fermi level, Broyden, "
                                       "energies and gradient") if mixed else "FP64 throughout",
@@ -611,6 +619,8 @@ def main():
     ap.add_argument("--stepping", default="paced", choices=["paced", "graph"],
                     help="paced: every molecule group steps from its own graph, small molecules several times per "
                          "step of the largest (default); graph: one graph per step for the whole batch")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="paced runs: keep --scc-budget instead of picking the budget by measurement")
     ap.add_argument("--scc-budget", type=int, default=SCC_BUDGET,
                     help="SCC iterations per step for the largest molecule (0: none); slower SCCs continue in the "
                          "next step while their trajectory waits, as independent trajectory processes would")

@@ -144,6 +144,13 @@ int qcx_batch_set_scc_budget(qcx_batch* b, int iters);
  * every group nsteps). Both return 0 or -1. */
 int qcx_batch_step_groups(qcx_batch* b, const int32_t* nsteps, double tstep);
 int qcx_batch_step_paced(qcx_batch* b, int nsteps, double tstep);
+/* Autotuner of the per-step SCC budget for paced stepping: for every candidate
+ * budget cand[c] (0: none) one untimed paced step and then `calls` timed ones
+ * on the batch's own trajectories (real MD steps: the run continues), rates[c]
+ * (may be NULL) = completed trajectory-steps per second; the batch keeps the
+ * fastest budget, which the call returns (or -1). */
+int qcx_batch_autotune_budget(qcx_batch* b, double tstep, const int32_t* cand, int ncand, int calls,
+                              double* rates);
 /* Number of groups; group_of_mol [nmol], the step counts of the last grouped
  * call nsteps_last [ngroup] and the measured per-step times ms_per_step
  * [ngroup] (0: not measured yet) when not NULL. */

@@ -1050,6 +1050,61 @@ int qcx_batch_step_paced(qcx_batch* b, int nsteps, double tstep) {
   return qcx_batch_step_groups(b, n.data(), tstep);
 }
 
+int qcx_batch_autotune_budget(qcx_batch* b, double tstep, const int32_t* cand, int ncand, int calls,
+                              double* rates) {
+  if (!b || !cand || ncand < 1 || calls < 1) {
+    set_error("qcx_batch_autotune_budget: invalid arguments");
+    return -1;
+  }
+  for (int c = 0; c < ncand; ++c)
+    if (cand[c] < 0) {
+      set_error("qcx_batch_autotune_budget: negative budget");
+      return -1;
+    }
+  // Completed trajectory-steps per second of paced steps under every candidate
+  // budget, measured on the batch's own trajectories (the steps are real MD
+  // steps: every candidate continues the run where the previous one left it).
+  // One untimed call per candidate lets the pacing settle to it.
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  std::vector<long long> s0(b->nmol), s1(b->nmol);
+  int best = -1;
+  double best_rate = -1.0;
+  int rc = 0;
+  for (int c = 0; c < ncand && rc == 0; ++c) {
+    rc = qcx_batch_set_scc_budget(b, cand[c]);
+    if (!rc) rc = qcx_batch_step_paced(b, 1, tstep);
+    if (!rc && cudaMemcpyAsync(s0.data(), b->d_steps, sizeof(long long) * b->nmol, cudaMemcpyDeviceToHost,
+                               b->stream) != cudaSuccess) rc = -1;
+    if (!rc && cudaEventRecord(e0, b->stream) != cudaSuccess) rc = -1;
+    for (int k = 0; k < calls && !rc; ++k) rc = qcx_batch_step_paced(b, 1, tstep);
+    if (!rc && cudaEventRecord(e1, b->stream) != cudaSuccess) rc = -1;
+    if (!rc && cudaMemcpyAsync(s1.data(), b->d_steps, sizeof(long long) * b->nmol, cudaMemcpyDeviceToHost,
+                               b->stream) != cudaSuccess) rc = -1;
+    if (!rc && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = -1;
+    float ms = 0.f;
+    if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = -1;
+    if (rc) break;
+    long long done = 0;
+    for (int m = 0; m < b->nmol; ++m) done += s1[m] - s0[m];
+    const double rate = ms > 0.f ? 1e3 * (double)done / ms : 0.0;
+    if (rates) rates[c] = rate;
+    if (rate > best_rate) {
+      best_rate = rate;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) {
+    set_error("qcx_batch_autotune_budget: a timed step failed");
+    return -1;
+  }
+  if (qcx_batch_set_scc_budget(b, cand[best])) return -1;
+  return cand[best];
+}
+
 int qcx_batch_group_info(qcx_batch* b, int32_t* group_of_mol, int32_t* nsteps_last, double* ms_per_step) {
   if (!b) return -1;
   std::vector<int> order(b->nmol);

@@ -112,3 +112,19 @@ def test_md_rules_in_groups(gpu):
     d = offsets(b)
     assert len(ref) > 0 and len(d) > 0 and np.all(d == ref[0])
     b.close()
+
+
+def test_budget_autotuner(gpu):
+    """The autotuner measures every candidate on the batch's own paced steps,
+    keeps the fastest and leaves the batch stepping with it."""
+    mols = molgen.batch_workload(24, 6, 30, seed0=900)
+    b = qg.Batch(mols)
+    b.egrad()
+    _, s0 = b.progress()
+    best, rates = b.autotune_budget((0, 8, 30), calls=2, tstep=DT)
+    assert best in (0, 8, 30) and set(rates) == {0, 8, 30}
+    assert all(v > 0 for v in rates.values()) and rates[best] == max(rates.values())
+    _, s1 = b.progress()
+    assert np.sum(s1 - s0) > 0  # the measured steps advanced the trajectories
+    b.step_paced(1, DT)
+    b.close()
