@@ -54,7 +54,8 @@ struct MmaCtx {
   int ok;           // 0 after a wait ran out: the caller must not trust the results
 };
 
-// Tensor-memory columns of the accumulator (a power of two >= 32; N <= 256)
+// Tensor-memory columns of the accumulator (a power of two >= 32): the largest
+// N a caller may pass (rounded up to 16), and the MMA's own limit for M = 128
 constexpr int kMmaTmemCols = 256;
 
 // Warp 0 allocates the accumulator; the address goes through shared memory.

@@ -151,13 +151,13 @@ __device__ void cta_gemm(int M, int N, int K, const TA* A, int lda, bool ta, con
 }
 
 // Products of the FP32 iterations: on the tensor cores (qcx_mma.cuh, split-TF32)
-// when the CTA holds a tcgen05 context, else on the CUDA cores. FP64 products
-// always take the CUDA cores.
+// when the CTA holds a tcgen05 context and N fits the accumulator, else on the
+// CUDA cores. FP64 products always take the CUDA cores.
 template <typename T>
 __device__ __forceinline__ void gemm_t(MmaCtx* mc, int M, int N, int K, const T* A, int lda, bool ta, const T* B,
                                        int ldb, bool tb, T* C, int ldc) {
   if constexpr (std::is_same<T, float>::value) {
-    if (mc) {
+    if (mc && ((N + 15) & ~15) <= kMmaTmemCols) {
       mma_gemm_tf32(*mc, M, N, K, A, lda, ta, B, ldb, tb, C, ldc);
       return;
     }
@@ -1670,12 +1670,14 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   // Tensor-core context of the FP32 iterations (mixed mode): the staging buffer
   // of the operands goes after this molecule's part of shared memory when it
   // fits there, else (both FP64 Jacobi matrices in shared memory) into the
-  // FP64 coefficient matrix, which the FP32 iterations leave unused.
+  // FP64 coefficient matrix, which the FP32 iterations leave unused. The
+  // products have N = n columns: one MMA takes N <= 256 and the accumulator
+  // holds kMmaTmemCols columns, so larger molecules keep the CUDA-core path.
   __shared__ uint32_t mma_tmem_slot;
   __shared__ __align__(8) uint64_t mma_bar;
   MmaCtx mctx;
   MmaCtx* mc = nullptr;
-  if (MIXED && QCX_SCC_MMA) {
+  if (MIXED && QCX_SCC_MMA && ((n + 15) & ~15) <= kMmaTmemCols) {
     const size_t jac_used = mode == 0 ? 2 * sizeof(double) * (size_t)np * np
                                       : mode == 1 ? sizeof(double) * (size_t)np * np
                                                   : (a32_shared ? sizeof(float) * (size_t)np * np : 0);
@@ -2345,9 +2347,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       double de = fabs(eel - eprev);
       eprev = eel;
       if (fp32_phase) {
-        // hand over to FP64 once the FP32 iterations reach their noise floor;
-        // the FP64 iterations restart the Broyden mixer from the current point
-        // (or once the FP32 residual has stopped improving below 1e-3)
+        // hand over to FP64 once the FP32 iterations reach their noise floor
+        // (or once the FP32 residual has stopped improving below 1e-3); the
+        // mixer keeps its history across the hand-over
         if (res < 0.9 * best32) {
           best32 = res;
           stall32 = 0;

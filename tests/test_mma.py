@@ -38,3 +38,29 @@ def test_mma_gemm_repeated_calls_reuse_the_accumulator(gpu):
     C, ms = qg.mma_gemm(A, B, reps=5)
     ref = A.astype(np.float64) @ B.astype(np.float64)
     assert np.abs(C - ref).max() < 1e-4 and ms > 0.0
+
+
+@pytest.mark.gpu
+def test_mixed_scc_above_the_accumulator_width(gpu, oracle_lib):
+    """Molecules with more than 256 AOs (CID ions of ~80 atoms with S) run the
+    FP32 products on the CUDA cores: one MMA takes N <= 256 and the tensor-memory
+    accumulator has 256 columns. Energies against the FP64 oracle."""
+    import qcxms_gb300 as qg
+    from qcxms_gb300 import constants, molgen
+    from qcxms_gb300.basis import nao_of
+    big = [m for m in molgen.cid_workload(96, 76, 80, seed0=5) if nao_of(m["Z"]) > 256][:3]
+    assert big, "no molecule above 256 AOs in the sample"
+    b = qg.Batch(big)
+    b.set_precision("mixed")
+    b.egrad()
+    r = b.get()
+    kT = 300.0 * constants.KB_AU
+    ok = 0
+    for i, m in enumerate(big):
+        rc, e, g, q, info = oracle_lib.egrad(m["Z"], m["xyz"], m["charge"], kT=kT)
+        if rc != 0 or r["status"][i] != 0:
+            continue
+        ok += 1
+        assert abs(r["energy"][i] - e) < 1e-6
+    assert ok >= 1
+    b.close()
