@@ -51,15 +51,24 @@ __device__ inline double sph_coef(int i, int c) {
   }
 }
 
-// 1D overlap table S1[k][i][j] for i <= IMAX, j <= LB
+// 1D overlap table S1[k][i][j] for i <= IMAX, j <= LB. Every integral is a
+// product of one entry per direction and each direction's recursion is linear
+// in its start value, so the Gaussian factor exp(-mu r^2) of all three
+// directions is carried by the x table alone: one exponential per primitive
+// pair instead of three (FP64 exponentials dominate these kernels).
 template <int IMAX, int LB>
 __device__ inline void os_table(double a, double b, const double d[3], double S1[3][IMAX + 1][LB + 1]) {
-  double p = a + b, o2p = 0.5 / p, mu = a * b / p;
-  double sp = sqrt(QCX_PI / p);
+  // one FP64 division per primitive pair (a division is a multi-instruction
+  // sequence at the FP64 rate)
+  const double ip = 1.0 / (a + b), o2p = 0.5 * ip, mu = a * b * ip;
+  const double sp = sqrt(QCX_PI * ip);
+  const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  const double s0 = sp * exp(-mu * r2);
+  const double bp = b * ip, ap = a * ip;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    double xpa = -b * d[k] / p, xpb = a * d[k] / p;
-    S1[k][0][0] = sp * exp(-mu * d[k] * d[k]);
+    double xpa = -bp * d[k], xpb = ap * d[k];
+    S1[k][0][0] = k == 0 ? s0 : sp;
 #pragma unroll
     for (int i = 0; i < IMAX; ++i) S1[k][i + 1][0] = xpa * S1[k][i][0] + (i > 0 ? i * o2p * S1[k][i - 1][0] : 0.0);
 #pragma unroll

@@ -20,8 +20,13 @@
 
 namespace qcx {
 
+// warm FP32 Jacobi sweeps (at most) when the first-order refinement cannot
+// update the eigenvectors: a single sweep left errors of order 1e-2 in the
+// density of molecules with near-degenerate orbitals at the Fermi level, which
+// stalled the FP32 phase (measured: 43 iterations per evaluation with one
+// sweep, 38 with two or three, and fewer stopped trajectories)
 #ifndef QCX_JAC32_WARM_SWEEPS
-#define QCX_JAC32_WARM_SWEEPS 1
+#define QCX_JAC32_WARM_SWEEPS 2
 #endif
 #ifndef QCX_JAC32_COLD_TOL
 #define QCX_JAC32_COLD_TOL 2e-6
@@ -67,6 +72,21 @@ namespace qcx {
 #endif
 #ifndef QCX_HARD_ROUNDS
 #define QCX_HARD_ROUNDS 6
+#endif
+// Newton-Schulz steps (at most) after a first-order refinement step in FP64
+// and in double-float
+#ifndef QCX_NS64_STEPS
+#define QCX_NS64_STEPS 4
+#endif
+// a stalled FP32 phase hands over to the finishing iterations once its
+// residual is below this
+#ifndef QCX_STALL_HANDOVER
+#define QCX_STALL_HANDOVER 1e-3
+#endif
+// an FP32 phase that has not reached the hand-over residual after this many
+// iterations hands over anyway (a hard SCC continues in the accurate arithmetic)
+#ifndef QCX_FP32_MAXIT
+#define QCX_FP32_MAXIT 1000
 #endif
 // FP32 products of the FP32 iterations on the tcgen05 tensor cores (split-TF32)
 // when the CTA has room to stage them; 0: CUDA cores only
@@ -1272,11 +1292,15 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
       if (kmax < ktol) return true;
       continue;
     }
-    // FP64: one step (later passes and iterations remove what is left). FP32:
-    // the exact rotations let first-order steps of up to kfail through, whose
-    // O(K^2) defect one step does not remove, so steps repeat until the defect
-    // predicted from the measured one (3/4 n E^2) is at FP32 rounding level.
-    const int ns_steps = sizeof(T) == 4 ? 3 : 1;
+    // A first-order step of size K leaves an S-orthonormality defect of order
+    // K^2 and one Newton-Schulz step squares it: after a step with K ~ 0.1 one
+    // step still leaves ~1e-4. The Jacobi fallback and the next passes treat
+    // B = V F V^T as a standard eigenproblem, so a defect left here becomes an
+    // eigenvalue error of the same order (measured: 3e-4 Eh, which stalled the
+    // SCC). Steps therefore repeat until the defect predicted from the
+    // measured one (3/4 n E^2) is below the precision's floor.
+    const int ns_steps = sizeof(T) == 4 ? 3 : QCX_NS64_STEPS;
+    const double ns_floor = sizeof(T) == 4 ? 1e-9 : 1e-13;
     for (int st = 0; st < ns_steps; ++st) {
       gemm_t<T>(mc, n, n, n, S, n, false, JV, np, true, Tm, n);
       __syncthreads();
@@ -1290,13 +1314,13 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
         emax_t = ad > emax_t ? ad : emax_t;
         Cm[e] = (i == j ? T(1) : T(0)) - T(0.5) * d;
       }
-      double emax = ns_steps > 1 ? cta_max((double)emax_t, sh.red) : 0.0;
+      double emax = cta_max((double)emax_t, sh.red);
       __syncthreads();
       gemm_t<T>(mc, n, n, n, Cm, n, false, JV, np, false, Tm, n);
       __syncthreads();
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = Tm[e];
       __syncthreads();
-      if (0.75 * n * emax * emax < 1e-9) break;
+      if (0.75 * n * emax * emax < ns_floor) break;
     }
     // the remaining off-diagonal is of order kmax^2: stop once that is below ktol^2
     if (kmax < ktol) return true;
@@ -1473,7 +1497,8 @@ __device__ void dd_rotate_fock(const DDMats& d, int n, int np) {
 // Newton-Schulz steps V <- (3I - V S V^T)/2 V: the overlap V S V^T in
 // double-float, the (small) correction -(V S V^T - I)/2 V in FP32. Returns the
 // largest |V S V^T - I| seen before the last step.
-__device__ double dd_orthonormalize(const DDMats& d, int n, int np, int steps, SccShared& sh) {
+__device__ double dd_orthonormalize(const DDMats& d, int n, int np, int steps, SccShared& sh,
+                                   double floor = 1e-26) {
   double emax = 0.0;
   for (int st = 0; st < steps; ++st) {
     cta_gemm_dd(n, n, n, d.S, n, false, d.Vt, n, false, d.T, nullptr, n);
@@ -1493,7 +1518,7 @@ __device__ double dd_orthonormalize(const DDMats& d, int n, int np, int steps, S
     __syncthreads();
     dd_add_rows(d, n, np);
     // the defect left is about 3/4 n emax^2
-    if (0.75 * n * emax * emax < 1e-26) break;
+    if (0.75 * n * emax * emax < floor) break;
   }
   return emax;
 }
@@ -1546,7 +1571,9 @@ __device__ bool refine_dd(const DDMats& d, int n, double* lam, double kfail, dou
     cta_gemm_hi(n, n, n, d.Kf, n, d.V, np, d.dV, n);
     __syncthreads();
     dd_add_rows(d, n, np);
-    if (kmax >= ns_min) dd_orthonormalize(d, n, np, 1, sh);
+    // as in refine(): remove the O(K^2) defect completely, the fallback Jacobi
+    // and the next passes need an S-orthonormal basis
+    if (kmax >= ns_min) dd_orthonormalize(d, n, np, QCX_NS64_STEPS, sh, 1e-13);
     if (kmax < ktol) return true;
   }
   dd_rotate_fock(d, n, np);
@@ -1611,6 +1638,13 @@ __device__ unsigned long long g_counts[8];  // refine64 ok, jacobi64 fallbacks
 #else
 #define PHASE_BEGIN()
 #define PHASE_MARK(i)
+#endif
+// Optional per-iteration trace of molecule 0 (diagnostic builds only: -DQCX_SCC_TRACE):
+// residual, energy change, electronic energy, FP32 phase, Fermi level, highest occupied + 1
+#ifdef QCX_SCC_TRACE
+__device__ double g_trace[QCX_SCC_MAXITER + 1][6];
+// orbital energies, occupations, input and output moment vectors (first 128 entries)
+__device__ double g_trace_vec[QCX_SCC_MAXITER + 1][4][128];
 #endif
 
 template <int MIXED>
@@ -2345,6 +2379,23 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       double res = sqrt(acc[1] / len);
       eel = eband + en[0] + en[1] + en[2] + en[3] + en[4] + ets;
       double de = fabs(eel - eprev);
+#ifdef QCX_SCC_TRACE
+      if (mol == 0 && threadIdx.x == 0 && it <= QCX_SCC_MAXITER) {
+        g_trace[it][0] = res;
+        g_trace[it][1] = de;
+        g_trace[it][2] = eel;
+        g_trace[it][3] = fp32_phase ? 1.0 : 0.0;
+        g_trace[it][4] = efermi;
+        g_trace[it][5] = (double)nocc;
+      }
+      if (mol == 0 && it <= QCX_SCC_MAXITER)
+        for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+          g_trace_vec[it][0][i] = i < n ? eps[i] : 0.0;
+          g_trace_vec[it][1][i] = i < n ? focc[i] : 0.0;
+          g_trace_vec[it][2][i] = i < len ? xin[i] : 0.0;
+          g_trace_vec[it][3][i] = i < len ? xout[i] : 0.0;
+        }
+#endif
       eprev = eel;
       if (fp32_phase) {
         // hand over to FP64 once the FP32 iterations reach their noise floor
@@ -2356,7 +2407,8 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
         } else {
           ++stall32;
         }
-        if ((it > 1 && res < kMixedSwitch) || (stall32 >= 4 && res < 1e-3) || it >= bt.max_iter - 12)
+        if ((it > 1 && res < kMixedSwitch) || (stall32 >= 4 && res < QCX_STALL_HANDOVER) || it >= QCX_FP32_MAXIT ||
+            it >= bt.max_iter - 12)
           fp32_phase = false;
       } else {
         ++n64;
@@ -2488,6 +2540,18 @@ extern "C" int qcx_debug_phase_cycles(unsigned long long* out, int reset) {
     cudaMemcpyToSymbol(qcx::g_phase_cycles, z, sizeof(z));
   }
   return 0;
+}
+namespace qcx {
+#endif
+
+#ifdef QCX_SCC_TRACE
+}  // namespace qcx
+extern "C" int qcx_debug_trace(double* out) {
+  return cudaMemcpyFromSymbol(out, qcx::g_trace, sizeof(double) * (QCX_SCC_MAXITER + 1) * 6) == cudaSuccess ? 0 : -1;
+}
+extern "C" int qcx_debug_trace_vec(double* out) {
+  return cudaMemcpyFromSymbol(out, qcx::g_trace_vec, sizeof(double) * (QCX_SCC_MAXITER + 1) * 4 * 128) == cudaSuccess
+             ? 0 : -1;
 }
 namespace qcx {
 #endif
