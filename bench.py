@@ -50,14 +50,16 @@ def bf16_tensor_peak():
         pass
     return 1900.0, "fallback (1.9 PFLOP/s bf16 burst, one earlier GB300 measurement)"
 NTRAJ, NMIN, NMAX = 256, 5, 40
-# SCC iterations one step grants the batch's largest molecule (a molecule of n
-# AOs gets 20 (nmax / n)^2); an SCC that needs more continues in the next step
-# while its trajectory waits. Measured on the 256-trajectory workload: 20
-# iterations gave the highest completed-step rate of 10-120 (and of a flat or
-# linear scaling with n).
+# SCC iterations one step grants the largest molecule of a molecule group (a
+# molecule of n AOs gets 20 (nmax / n)^2, nmax the group's largest); an SCC
+# that needs more continues in the next step while its trajectory waits.
 SCC_BUDGET = 20
-# candidates of the budget autotuner of paced runs (0: no budget)
-AUTOTUNE_BUDGETS = (0, 10, 20, 40)
+# candidates of the budget autotuner of paced runs (0, no budget, measured
+# 40-50 % slower on this workload, is left out)
+AUTOTUNE_BUDGETS = (10, 20, 40)
+# MD steps of the largest molecules' group per timed paced call (the other
+# groups take as many as fit into the same time)
+PACED_STEPS = 1
 DT_FS = 0.5
 ETEMP = 300.0
 
@@ -361,11 +363,13 @@ def run_gpu(args):
 
     paced = args.stepping == "paced"
 
+    kstep = args.md_steps if args.md_steps else (PACED_STEPS if paced else 1)
+
     def one_step():
         if paced:
-            b.step_paced(1, dt)
+            b.step_paced(kstep, dt)
         else:
-            b.step(1, dt)
+            b.step(kstep, dt)
 
     # ---- device-resident timing: graph replay, L2 flushed between steps ----
     # Whole-batch steps: timing marks inside the step graph give the SCC phase of
@@ -376,7 +380,7 @@ def run_gpu(args):
     tune = None
     if paced and not args.no_autotune:
         # untimed: pick the per-step SCC budget on this batch (real MD steps)
-        best, rates = b.autotune_budget(AUTOTUNE_BUDGETS, calls=2, tstep=dt)
+        best, rates = b.autotune_budget(AUTOTUNE_BUDGETS, calls=2, tstep=dt, steps_per_call=kstep)
         tune = {"candidates": {str(k): round(v, 1) for k, v in rates.items()}, "chosen": best}
     for _ in range(args.warmup):
         one_step()
@@ -482,13 +486,14 @@ def run_gpu(args):
         if paced:
             _, gsteps, gms = b.group_info()
             execution = ("size-bucketed: 8 molecule groups by size, each stepping from its own CUDA graph on its own "
-                         "stream; per step of the largest molecules' group the groups took %s steps"
-                         % gsteps.tolist())
+                         "stream; one timed step = one paced call in which the largest molecules' group takes %d MD "
+                         "steps and the groups took %s steps" % (kstep, gsteps.tolist()))
             unit = ("all k_scc launches of the timed region (the groups' launches overlap one another and the "
                     "integral and gradient kernels); time = the timed region; FLOPs from the device's per-molecule "
                     "iteration counters")
         else:
-            execution = "one CUDA graph per MD step, 8 molecule groups on separate streams"
+            execution = ("one CUDA graph per MD step, 8 molecule groups on separate streams; one timed step = %d MD "
+                         "steps of the whole batch" % kstep)
             unit = ("the SCC phase of one timed step: one k_scc launch per molecule group (8, concurrent); time = "
                     "first group's SCC start to last group's SCC end, from event marks inside the step graph; "
                     "FLOPs from the device's per-molecule iteration counters")
@@ -507,6 +512,7 @@ def run_gpu(args):
                                       "energies and gradient") if mixed else "FP64 throughout",
                        "md_rules_on_device": bool(args.md_rules),
                        "execution": execution,
+                       "md_steps_per_timed_step": kstep,
                        "l2": "flushed between timed steps (256 MiB write)",
                        "mean_nao": float(np.mean(nao)),
                        "mean_scc_iters": float(np.mean(iters_cat)) if len(iters_cat) else 0.0,
@@ -624,6 +630,9 @@ def main():
     ap.add_argument("--scc-budget", type=int, default=SCC_BUDGET,
                     help="SCC iterations per step for the largest molecule (0: none); slower SCCs continue in the "
                          "next step while their trajectory waits, as independent trajectory processes would")
+    ap.add_argument("--md-steps", type=int, default=0,
+                    help="MD steps per timed step (paced: of the largest molecules' group); default %d paced, "
+                         "1 graph" % PACED_STEPS)
     ap.add_argument("--guess", default="zero", choices=["zero", "previous"],
                     help="SCC start: zero moments every step (the reference's behaviour, default) or the "
                          "trajectory's converged moments of the previous step (opt-in)")

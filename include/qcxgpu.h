@@ -120,7 +120,8 @@ int qcx_batch_set_guess(qcx_batch* b, int guess);
  * a batch that steps all trajectories together waits in every step for the
  * slowest SCC. With a budget b, the SCC of a molecule of n AOs stops after
  * ceil(b (nmax / n)^2) iterations of one qcx_batch_step (nmax: the batch's
- * largest molecule; mixed precision stops only between FP32 iterations) and
+ * largest molecule, or in qcx_batch_step_groups/_paced the largest of the
+ * molecule's group; mixed precision stops only between FP32 iterations) and
  * the next step continues it at the same coordinates: that trajectory does
  * not move and counts no step until its SCC has converged (status
  * QCX_STATUS_SCC_PENDING meanwhile), so trajectories advance at their own
@@ -139,16 +140,20 @@ int qcx_batch_set_scc_budget(qcx_batch* b, int iters);
  * continues after all of them. Trajectories never interact (bin/pqcxms runs
  * each as its own process), so groups of small molecules can take several
  * steps while the largest molecules take one. qcx_batch_step_paced gives group
- * 0 nsteps steps and every other group as many as fit into the same time, from
- * the per-step times the previous paced call measured (the first call gives
- * every group nsteps). Both return 0 or -1. */
+ * 0 nsteps steps and every other group as many as fit into the same time (at
+ * most 16 nsteps), from the per-step times the previous paced call measured
+ * (the first call gives every group nsteps). Both return 0 or -1. */
 int qcx_batch_step_groups(qcx_batch* b, const int32_t* nsteps, double tstep);
 int qcx_batch_step_paced(qcx_batch* b, int nsteps, double tstep);
 /* Autotuner of the per-step SCC budget for paced stepping: for every candidate
- * budget cand[c] (0: none) one untimed paced step and then `calls` timed ones
- * on the batch's own trajectories (real MD steps: the run continues), rates[c]
- * (may be NULL) = completed trajectory-steps per second; the batch keeps the
- * fastest budget, which the call returns (or -1). */
+ * budget cand[c] (0: none) one untimed paced call and then `calls` timed ones
+ * of qcx_batch_step_paced(b, steps_per_call, tstep) on the batch's own
+ * trajectories (real MD steps: the run continues), rates[c] (may be NULL) =
+ * completed trajectory-steps per second; the batch keeps the fastest budget,
+ * which the call returns (or -1). qcx_batch_autotune_budget is the same with
+ * steps_per_call = 1. */
+int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, const int32_t* cand, int ncand,
+                             int calls, double* rates);
 int qcx_batch_autotune_budget(qcx_batch* b, double tstep, const int32_t* cand, int ncand, int calls,
                               double* rates);
 /* Number of groups; group_of_mol [nmol], the step counts of the last grouped

@@ -125,6 +125,8 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_step_paced.argtypes = [ctypes.c_void_p, c_int, c_double]
     lib.qcx_batch_autotune_budget.argtypes = [ctypes.c_void_p, c_double, P(ctypes.c_int32), c_int, c_int,
                                               P(c_double)]
+    lib.qcx_batch_autotune_paced.argtypes = [ctypes.c_void_p, c_double, c_int, P(ctypes.c_int32), c_int, c_int,
+                                             P(c_double)]
     lib.qcx_batch_group_info.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double)]
     lib.qcx_batch_get_iterations.argtypes = [ctypes.c_void_p, P(ctypes.c_int64)]
     lib.qcx_batch_mo_populations.argtypes = [ctypes.c_void_p, c_int, P(c_double), P(c_double), P(c_double),
@@ -434,13 +436,14 @@ class Batch:
         many as fit into the same time (measured at the previous paced call)."""
         self._check(self._lib.qcx_batch_step_paced(self._h, int(nsteps), float(tstep)), "step_paced")
 
-    def autotune_budget(self, candidates=(0, 10, 20, 40), calls=3, tstep=0.5 * constants.FSTOAU):
+    def autotune_budget(self, candidates=(0, 10, 20, 40), calls=3, tstep=0.5 * constants.FSTOAU, steps_per_call=1):
         """Pick the per-step SCC budget with the highest completed-step rate of
-        paced steps on this batch (the measured steps are real MD steps).
-        Returns (chosen budget, {budget: trajectory-steps/s})."""
+        paced calls of ``steps_per_call`` steps on this batch (the measured steps
+        are real MD steps). Returns (chosen budget, {budget: trajectory-steps/s})."""
         c = np.ascontiguousarray(candidates, dtype=np.int32)
         rates = np.zeros(len(c))
-        best = self._lib.qcx_batch_autotune_budget(self._h, float(tstep), _ip(c), len(c), int(calls), _dp(rates))
+        best = self._lib.qcx_batch_autotune_paced(self._h, float(tstep), int(steps_per_call), _ip(c), len(c),
+                                                  int(calls), _dp(rates))
         if best < 0:
             raise RuntimeError("autotune_budget failed: " + _err(self._lib))
         return int(best), {int(k): float(v) for k, v in zip(c, rates)}

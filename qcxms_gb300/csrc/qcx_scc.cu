@@ -73,6 +73,17 @@ namespace qcx {
 #ifndef QCX_HARD_ROUNDS
 #define QCX_HARD_ROUNDS 6
 #endif
+// FP32 refinement: pairs of orbitals both further than this from the previous
+// Fermi level, on the same side, are not rotated (negative: all pairs rotate).
+// Off: the Fermi level of the previous iteration can move by 0.1 Eh in the
+// early SCC iterations, so an orbital judged fully occupied may not be, and
+// rotating all pairs measured 6-9 % faster on the 256-trajectory workload.
+#ifndef QCX_OCC_GAP_KT
+#define QCX_OCC_GAP_KT -1.0
+#endif
+#ifndef QCX_OCC_GAP_ABS
+#define QCX_OCC_GAP_ABS 0.0
+#endif
 // Newton-Schulz steps (at most) after a first-order refinement step in FP64
 // and in double-float
 #ifndef QCX_NS64_STEPS
@@ -2053,7 +2064,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       if (backoff32 > 0) --backoff32;
       bool ok32 = try32 &&
                   refine<float>(JA32, JV32, (const float*)F, S32, T32, (float*)C, eps, n, QCX_REFINE32_KFAIL, QCX_REFINE32_KTOL,
-                                QCX_REFINE32_PASSES, 1e-3, sh, efermi, 25.0 * md.kT, mc);
+                                QCX_REFINE32_PASSES, 1e-3, sh, efermi, QCX_OCC_GAP_KT * md.kT + QCX_OCC_GAP_ABS, mc);
       PHASE_MARK(16);
       if (try32 && !ok32) backoff32 = QCX_REFINE32_BACKOFF;
       // the first (cold) solve only seeds the FP32 iterations: it stops at a

@@ -250,7 +250,13 @@ def test_mixed_md_matches_fp64(gpu):
         out[prec] = b.get()
     ok = (out["fp64"]["status"] == 0) & (out["mixed"]["status"] == 0)
     assert ok.sum() >= 2
-    assert np.abs(out["fp64"]["energy"] - out["mixed"]["energy"])[ok].max() < 1e-6
+    # After 20 steps the two runs sit at slightly different geometries: at the
+    # default SCC thresholds their gradients differ by up to ~2e-6 Eh/Bohr, which
+    # moves an H atom by ~0.5 (2e-6 / 1836) (20 * 20.7)^2 ~ 1e-4 Bohr, worth a
+    # few 1e-6 Eh at gradients of 0.05 Eh/Bohr. The single-point contract (1e-6 Eh)
+    # is tested at identical geometries elsewhere; here the trajectories stay
+    # within that propagated bound.
+    assert np.abs(out["fp64"]["energy"] - out["mixed"]["energy"])[ok].max() < 5e-6
     xa = qg_split(out["fp64"]["xyz"], mols)
     xb = qg_split(out["mixed"]["xyz"], mols)
     for i in np.nonzero(ok)[0]:
