@@ -31,9 +31,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "GFN2-xTB trajectory-steps/s"
 # DRAM bytes (read + write) of one k_scc launch per molecule, from an ncu capture of a
-# launch over 2 molecules of the 16-trajectory batch (1.897 MB read, 0.047 MB written);
+# launch over 2 molecules of the 16-trajectory batch (1.845 MB read, 0.050 MB written);
 # a launch touches each molecule's own data only.
-SCC_DRAM_BYTES_PER_MOLECULE = (1.89696e6 + 4.6848e4) / 2
+SCC_DRAM_BYTES_PER_MOLECULE = (1.844736e6 + 4.992e4) / 2
 
 
 def bf16_tensor_peak():
