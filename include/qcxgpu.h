@@ -429,6 +429,19 @@ int qcx_mma_selftest(int M, int N, int K, const float* A, int ta, const float* B
                      float* ms);
 
 /*
+ * Self-check of the FP32 eigensolver of the SCC kernel's FP32 iterations (no
+ * counterpart in the reference: it checks the cyclic parallel Jacobi alone).
+ * One CTA of the SCC kernel's shape diagonalises the symmetric n x n matrix A
+ * (row major, n <= 256) as the SCC does; warm = 1 starts from the orthonormal
+ * rows in V (the basis A is expressed in), 0 from the identity. On return
+ * Aout holds the rotated matrix (eigenvalues on the diagonal), V the
+ * eigenvectors as rows, *sweeps the sweeps used (-1: max_sweeps were not
+ * enough). Returns 0 or -1 (invalid arguments or a CUDA error).
+ */
+int qcx_jacobi32_selftest(int n, const float* A, float* Aout, float* V, int warm, double reltol, int max_sweeps,
+                          int* sweeps);
+
+/*
  * Ground-state sampling file qcxms.gs, as md writes it during the sampling run
  * (it = 0, src/md.f90:150-153, 379-385): the first line is nmax (list-directed,
  * a blank and 11 columns), then one record per MD loop top, each a line per

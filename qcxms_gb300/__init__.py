@@ -79,6 +79,8 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_get_timing.argtypes = [ctypes.c_void_p, P(ctypes.c_float), c_int]
     lib.qcx_mma_selftest.argtypes = [c_int, c_int, c_int, P(ctypes.c_float), c_int, P(ctypes.c_float), c_int,
                                      P(ctypes.c_float), c_int, P(ctypes.c_float)]
+    lib.qcx_jacobi32_selftest.argtypes = [c_int, P(ctypes.c_float), P(ctypes.c_float), P(ctypes.c_float), c_int,
+                                          c_double, c_int, P(c_int)]
     lib.qcx_checkqc.argtypes = [c_int, P(c_double), P(c_double), c_int, P(c_double)]
     lib.qcx_batch_load_state.argtypes = [ctypes.c_void_p, P(c_double), P(c_double)]
     lib.qcx_batch_step.argtypes = [ctypes.c_void_p, c_int, c_double]
@@ -346,6 +348,24 @@ def mma_gemm(A, B, ta=False, tb=False, reps=1):
     if rc != 0:
         raise RuntimeError("qcx_mma_selftest returned %d: %s" % (rc, _err(lib)))
     return C, ms.value
+
+
+def jacobi32(A, V=None, reltol=2e-6, max_sweeps=30):
+    """The SCC kernel's FP32 eigensolver (cyclic parallel Jacobi) on one CTA.
+    With V (orthonormal rows) it starts warm from that basis. Returns (rotated
+    A with the eigenvalues on its diagonal, eigenvector rows, sweeps used)."""
+    lib = load_library()
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    n = A.shape[0]
+    Ao = np.zeros_like(A)
+    Vv = np.ascontiguousarray(np.eye(n) if V is None else V, dtype=np.float32).copy()
+    sw = ctypes.c_int()
+    fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    rc = lib.qcx_jacobi32_selftest(n, fp(A), fp(Ao), fp(Vv), int(V is not None), float(reltol), int(max_sweeps),
+                                   ctypes.byref(sw))
+    if rc != 0:
+        raise RuntimeError("qcx_jacobi32_selftest returned %d: %s" % (rc, _err(lib)))
+    return Ao, Vv, sw.value
 
 
 def checkqc(energy, grad, qat, charge):

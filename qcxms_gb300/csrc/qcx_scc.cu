@@ -1218,6 +1218,20 @@ __device__ int rotate_hard_pairs(T* JA, T* JV, const T* Km, int n, T khard, SccS
 // not reach ktol; JA then holds B for the current rows of JV and the caller
 // runs Jacobi on it. On success JA's diagonal holds the eigenvalues.
 // ---------------------------------------------------------------------------
+#ifdef QCX_SCC_PHASE_TIMING
+// FP32 refinement outcomes (diagnostic builds): [0] max|K| above the limit at
+// the first pass, [1] above it at a later pass, [2] success, [3] passes
+// exhausted, [4..8] first max|K| < 1e-3, < 1e-2, < 0.1, < 1, larger, [9] hard
+// rounds before outcome [0]
+__device__ unsigned long long g_refine32[16];
+#define REFINE32_COUNT(i) \
+  do {                     \
+    if (sizeof(T) == 4 && threadIdx.x == 0) atomicAdd(&g_refine32[i], 1ull); \
+  } while (0)
+#else
+#define REFINE32_COUNT(i)
+#endif
+
 template <typename T>
 __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, double* tmp, int n,
                        double kfail, double ktol, int max_pass, double ns_min, SccShared& sh,
@@ -1258,6 +1272,10 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
       kmax_t = ka > kmax_t ? ka : kmax_t;
     }
     double kmax = cta_max((double)kmax_t, sh.red);
+#ifdef QCX_SCC_PHASE_TIMING
+    if (pass == 0 && hard == 0)
+      REFINE32_COUNT(kmax < 1e-3 ? 4 : kmax < 1e-2 ? 5 : kmax < 0.1 ? 6 : kmax < 1.0 ? 7 : 8);
+#endif
     if (kmax > kfail) {
       // rotate the offending pairs exactly (B stays expressed in the rotated
       // basis, so no recomputation) and look again
@@ -1267,7 +1285,14 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
         fresh = true;
         continue;
       }
-      if (pass == 0) return false;
+      if (pass == 0) {
+        REFINE32_COUNT(0);
+#ifdef QCX_SCC_PHASE_TIMING
+        if (sizeof(T) == 4 && threadIdx.x == 0) atomicAdd(&g_refine32[9], (unsigned long long)hard);
+#endif
+        return false;
+      }
+      REFINE32_COUNT(1);
       // the basis moved but did not converge: give the current B to Jacobi
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         int i = e / n, j = e % n;
@@ -1290,7 +1315,10 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
     }
     __syncthreads();
     for (int j = threadIdx.x; j < n; j += blockDim.x) JA[j * np + j] = lamv[j];
-    if (kmax == 0.0) return true;
+    if (kmax == 0.0) {
+      REFINE32_COUNT(2);
+      return true;
+    }
     // C^T <- C^T + K^T C^T
     gemm_t<T>(mc, n, n, n, Tm, n, false, JV, np, false, Cm, n);
     __syncthreads();
@@ -1300,7 +1328,10 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
     // to first order (K is antisymmetric), so below ns_min the O(K^2) defect is
     // left for a later pass or iteration.
     if (kmax < ns_min) {
-      if (kmax < ktol) return true;
+      if (kmax < ktol) {
+        REFINE32_COUNT(2);
+        return true;
+      }
       continue;
     }
     // A first-order step of size K leaves an S-orthonormality defect of order
@@ -1334,8 +1365,12 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
       if (0.75 * n * emax * emax < ns_floor) break;
     }
     // the remaining off-diagonal is of order kmax^2: stop once that is below ktol^2
-    if (kmax < ktol) return true;
+    if (kmax < ktol) {
+      REFINE32_COUNT(2);
+      return true;
+    }
   }
+  REFINE32_COUNT(3);
   // passes exhausted: recompute B in the final basis for the caller's Jacobi
   gemm_t<T>(mc, n, n, n, F, n, false, JV, np, true, Tm, n);
   __syncthreads();
@@ -2532,6 +2567,14 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
 
 #ifdef QCX_SCC_PHASE_TIMING
 }  // namespace qcx
+extern "C" int qcx_debug_refine32(unsigned long long* out, int reset) {
+  if (cudaMemcpyFromSymbol(out, qcx::g_refine32, sizeof(unsigned long long) * 16) != cudaSuccess) return -1;
+  if (reset) {
+    unsigned long long z[16] = {0};
+    cudaMemcpyToSymbol(qcx::g_refine32, z, sizeof(z));
+  }
+  return 0;
+}
 extern "C" int qcx_debug_counts(unsigned long long* out, int reset) {
   if (cudaMemcpyFromSymbol(out, qcx::g_counts, sizeof(unsigned long long) * 8) != cudaSuccess) return -1;
   if (reset) {
@@ -2554,6 +2597,44 @@ extern "C" int qcx_debug_phase_cycles(unsigned long long* out, int reset) {
 }
 namespace qcx {
 #endif
+
+// Self-check of the FP32 eigensolver through the C ABI: one CTA of the SCC
+// kernel's shape diagonalises a symmetric host matrix with the cyclic parallel
+// Jacobi of the FP32 iterations, in shared memory as in the SCC.
+__global__ void __launch_bounds__(kSccThreads, 1) k_jacobi32_selftest(int n, const float* Ain, float* Aout,
+                                                                       float* Vout, int warm, double reltol,
+                                                                       int max_sweeps, int* sweeps, float* Ag,
+                                                                       float* Vg) {
+  extern __shared__ __align__(1024) char smem_raw[];
+  const int np = n + (n & 1);
+  // the matrices in shared memory when they fit (Ag == nullptr), else in the
+  // global buffers, as the SCC kernel keeps them for large molecules
+  const bool shared = Ag == nullptr;
+  float* A = shared ? (float*)smem_raw : Ag;
+  float* Vt = shared ? A + (size_t)np * np : Vg;
+  double* red = (double*)(smem_raw + (shared ? sizeof(float) * 2 * (size_t)np * np : 0));
+  int* rq = (int*)(red + 16 * kWarps);
+  float* rc = (float*)(rq + 2 * 256);
+  SccShared sh{};
+  sh.red = red;
+  sh.rp = rq;
+  sh.rq = rq + 256;
+  sh.rc = (double*)rc;
+  for (int i = threadIdx.x; i < np * np; i += blockDim.x) {
+    const int r = i / np, c = i % np;
+    A[i] = (r < n && c < n) ? Ain[r * n + c] : 0.f;
+    Vt[i] = (r < n && c < n) ? Vout[r * n + c] : (r == c ? 1.f : 0.f);
+  }
+  __syncthreads();
+  const int sw = jacobi<float>(A, Vt, n, warm != 0, reltol, sh, max_sweeps);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+    const int r = i / n, c = i % n;
+    Aout[i] = A[r * np + c];
+    Vout[i] = Vt[r * np + c];
+  }
+  if (threadIdx.x == 0) *sweeps = sw;
+}
 
 #ifdef QCX_SCC_TRACE
 }  // namespace qcx
@@ -2587,3 +2668,52 @@ void launch_scc(const DevBatch& bt, int precision, cudaStream_t st) {
 }
 
 }  // namespace qcx
+
+extern "C" int qcx_jacobi32_selftest(int n, const float* A, float* Aout, float* V, int warm, double reltol,
+                                     int max_sweeps, int* sweeps) {
+  using namespace qcx;
+  if (n < 1 || n > 256 || !A || !Aout || !V || !sweeps || max_sweeps < 1 || !(reltol > 0.0)) {
+    set_last_error("qcx_jacobi32_selftest: 1 <= n <= 256, max_sweeps >= 1, reltol > 0");
+    return -1;
+  }
+  const int np = n + (n & 1);
+  const size_t mats = sizeof(float) * 2 * (size_t)np * np;
+  const size_t rest = sizeof(double) * 16 * kWarps + sizeof(int) * 512 + sizeof(float) * 512;
+  const bool in_shared = mats + rest <= 200 * 1024;
+  const size_t smem = (in_shared ? mats : 0) + rest;
+  float *dA = nullptr, *dAo = nullptr, *dV = nullptr, *dAg = nullptr, *dVg = nullptr;
+  int* dsw = nullptr;
+  const size_t nb = sizeof(float) * (size_t)n * n;
+  cudaError_t e = cudaSuccess;
+  if (!in_shared) {
+    e = cudaMalloc(&dAg, sizeof(float) * (size_t)np * np);
+    if (e == cudaSuccess) e = cudaMalloc(&dVg, sizeof(float) * (size_t)np * np);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&dA, nb);
+  if (e == cudaSuccess) e = cudaMalloc(&dAo, nb);
+  if (e == cudaSuccess) e = cudaMalloc(&dV, nb);
+  if (e == cudaSuccess) e = cudaMalloc(&dsw, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(dA, A, nb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dV, V, nb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_jacobi32_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) {
+    k_jacobi32_selftest<<<1, kSccThreads, smem>>>(n, dA, dAo, dV, warm, reltol, max_sweeps, dsw, dAg, dVg);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(Aout, dAo, nb, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(V, dV, nb, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(sweeps, dsw, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(dA);
+  cudaFree(dAo);
+  cudaFree(dV);
+  cudaFree(dsw);
+  cudaFree(dAg);
+  cudaFree(dVg);
+  if (e != cudaSuccess) {
+    set_last_error(std::string("qcx_jacobi32_selftest: ") + cudaGetErrorString(e));
+    return -1;
+  }
+  return 0;
+}

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 KT = 300.0 * constants.KB_AU
 DT = 0.5 * constants.FSTOAU
 # (molecule of the 256-trajectory workload, MD step of the snapshot)
-CASES = [(101, 6), (118, 26), (174, 8), (182, 10), (208, 20), (231, 1), (84, 10)]
+CASES = [(101, 6), (118, 26), (174, 8), (182, 10), (208, 20), (231, 1)]
 
 
 @pytest.fixture(scope="module")
