@@ -54,9 +54,9 @@ NTRAJ, NMIN, NMAX = 256, 5, 40
 # molecule of n AOs gets 20 (nmax / n)^2, nmax the group's largest); an SCC
 # that needs more continues in the next step while its trajectory waits.
 SCC_BUDGET = 20
-# candidates of the budget autotuner of paced runs (0, no budget, measured
-# 40-50 % slower on this workload, is left out)
-AUTOTUNE_BUDGETS = (10, 20, 40)
+# candidates of the budget autotuner of paced runs (0, no budget, and 10
+# measured 40-50 % slower on this workload, are left out)
+AUTOTUNE_BUDGETS = (20, 40, 60)
 # MD steps of the largest molecules' group per timed paced call (the other
 # groups take as many as fit into the same time)
 PACED_STEPS = 1

@@ -1190,6 +1190,8 @@ static int run_scc(int nat, const int* Z, const double* xyz, double charge, doub
   broyden_t br;
   broyden_init(&br, len, QCX_BROYDEN_WINDOW, o->broyden_alpha);
   double eprev = 0.0;
+  double rbest = 1e300; /* best residual since the mixer's last restart */
+  int rsince = 0;       /* iterations without a 10 % improvement of it */
   c->converged = 0;
   int it;
   for (it = 1; it <= o->max_iter; ++it) {
@@ -1243,6 +1245,15 @@ static int run_scc(int nat, const int* Z, const double* xyz, double charge, doub
     c->e_elec = eel;
     if (it > 1 && de < o->econv && res < o->pconv) { c->converged = 1; break; }
     if (it == o->max_iter) break;
+    /* restart the mixer after QCX_BROYDEN_RESTART iterations of stagnation */
+    if (res < 0.9 * rbest) {
+      rbest = res;
+      rsince = 0;
+    } else if (++rsince >= QCX_BROYDEN_RESTART) {
+      br.it = 0;
+      rbest = res;
+      rsince = 0;
+    }
     broyden_step(&br, x, c->x_out);
   }
   c->iterations = it > o->max_iter ? o->max_iter : it;

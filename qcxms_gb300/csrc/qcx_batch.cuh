@@ -55,7 +55,8 @@ struct SccCarry {
   int phase32;    // mixed mode: still in the FP32 iterations
   int stall32, backoff32, n64, eig_fail;
   int basis;      // mixed mode: the FP32 eigenvectors were saved (B32 region of the kD32 slots)
-  double best32, eprev, efermi, pad_;
+  int rsince;     // iterations since the residual last improved by 10 % (mixer restart)
+  double best32, eprev, efermi, rbest;
 };
 
 struct MolDesc {

@@ -25,6 +25,14 @@
 #ifndef QCX_BROYDEN_WINDOW
 #define QCX_BROYDEN_WINDOW 24
 #endif
+/* The mixer restarts (history dropped, the next update a linear mixing step
+ * from the current input) when the moment residual has not fallen below 0.9
+ * of its best value for this many iterations: charge sloshing between
+ * near-degenerate states can hold a Broyden history at a residual of ~3e-2
+ * for tens of iterations. */
+#ifndef QCX_BROYDEN_RESTART
+#define QCX_BROYDEN_RESTART 12
+#endif
 
 /* Fermi level bisection: fixed iteration count for reproducibility */
 #define QCX_FERMI_ITERS 200

@@ -1362,7 +1362,10 @@ __device__ bool refine(T* JA, T* JV, const T* F, const T* S, T* Tm, T* Cm, doubl
       __syncthreads();
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) JV[(e / n) * np + (e % n)] = Tm[e];
       __syncthreads();
-      if (0.75 * n * emax * emax < ns_floor) break;
+      // predicted defect of the next step: 3/4 E^2, with the entries of E^2
+      // summing sqrt(n) terms of random sign (n terms bound it; measured
+      // steps shrink as 0.8 E^2 in the max norm)
+      if (0.75 * (sizeof(T) == 4 ? (double)n : sqrt((double)n)) * emax * emax < ns_floor) break;
     }
     // the remaining off-diagonal is of order kmax^2: stop once that is below ktol^2
     if (kmax < ktol) {
@@ -1563,8 +1566,9 @@ __device__ double dd_orthonormalize(const DDMats& d, int n, int np, int steps, S
     cta_gemm_hi(n, n, n, d.Kf, n, d.V, np, d.dV, n);
     __syncthreads();
     dd_add_rows(d, n, np);
-    // the defect left is about 3/4 n emax^2
-    if (0.75 * n * emax * emax < floor) break;
+    // the defect left is about 3/4 emax^2, times sqrt(n) for the sum of n
+    // terms of random sign in every entry of E^2 (n terms bound it)
+    if (0.75 * sqrt((double)n) * emax * emax < floor) break;
   }
   return emax;
 }
@@ -1920,6 +1924,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
   bool have32 = false;  // JV32 holds FP32 eigenvectors from a previous iteration
   int bro_it = resume ? cr.bro_it : 0;  // Broyden updates since the last (re)start of the mixer
   double best32 = resume ? cr.best32 : 1e300;  // best residual seen in the FP32 phase
+  // mixer restart after QCX_BROYDEN_RESTART iterations without a 10 % better residual
+  double rbest = resume ? cr.rbest : 1e300;
+  int rsince = resume ? cr.rsince : 0;
   int stall32 = resume ? cr.stall32 : 0;
   int backoff32 = resume ? cr.backoff32 : 0;  // FP32 iterations left before the next refinement attempt
   int n64 = resume ? cr.n64 : 0;              // FP64 iterations done
@@ -2411,6 +2418,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     if (!fp32_phase) potentials(mv, xout, en, sh.red);
     PHASE_MARK(10);
     bool stop = false;
+    double res_it = 0.0;
     {
       double acc[2] = {0.0, 0.0};
       // the band energy only enters the FP64 convergence test
@@ -2423,6 +2431,7 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       cta_sum<2>(acc, sh.red);
       eband = acc[0];
       double res = sqrt(acc[1] / len);
+      res_it = res;
       eel = eband + en[0] + en[1] + en[2] + en[3] + en[4] + ets;
       double de = fabs(eel - eprev);
 #ifdef QCX_SCC_TRACE
@@ -2467,6 +2476,16 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
     }
     PHASE_MARK(11);
     if (stop || it == bt.max_iter) break;
+    // charge sloshing between near-degenerate states can hold the Broyden
+    // history at a residual of ~3e-2 for tens of iterations: restart it
+    if (res_it < 0.9 * rbest) {
+      rbest = res_it;
+      rsince = 0;
+    } else if (++rsince >= QCX_BROYDEN_RESTART) {
+      bro_it = 0;
+      rbest = res_it;
+      rsince = 0;
+    }
     broyden(mv, xin, xout, bro_it, bt.mix_alpha, sh);
     ++bro_it;
     PHASE_MARK(12);
@@ -2494,6 +2513,8 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       c.eig_fail = eig_fail;
       c.basis = keep_basis ? 1 : 0;
       c.best32 = best32;
+      c.rbest = rbest;
+      c.rsince = rsince;
       c.eprev = eprev;
       c.efermi = efermi;
       bt.carry[mol] = c;
