@@ -392,6 +392,33 @@ def run_gpu(args):
     scc_iters_all = []
     scc_launches = []
     phase = {"step": [], "scc_span": [], "scc_sum": [], "integrals_sum": [], "gradient_sum": []}
+    # End to end through the public API with pinned host buffers, interleaved with
+    # the device-resident steps so that both legs see the same trajectory states
+    # (the batch ages: trajectories fragment and stop, small molecules run ahead).
+    # Every end-to-end step: coordinates and velocities in (qcx_batch_load_state:
+    # running trajectories continue, stopped ones stay stopped), one step,
+    # coordinates, velocities and energies out, host clock around all three.
+    r = b.get()
+    hx = torch.from_numpy(r["xyz"]).pin_memory()
+    hv = torch.from_numpy(r["vel"]).pin_memory()
+    he = torch.zeros(b.nmol, dtype=torch.float64).pin_memory()
+    e2e_s = e2e_done = dev_done = 0.0
+
+    def e2e_step():
+        # the host buffers take the current state first (untimed), then the timed
+        # round trip; L2 flushed before it as before every device-resident step
+        b.get_ptr(hx.data_ptr(), hv.data_ptr(), he.data_ptr())
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        _, q0 = b.progress()
+        t0 = time.perf_counter()
+        b.load_state_ptr(hx.data_ptr(), hv.data_ptr())
+        one_step()
+        b.get_ptr(hx.data_ptr(), hv.data_ptr(), he.data_ptr())
+        dt_s = time.perf_counter() - t0
+        _, q1 = b.progress()
+        return dt_s, float(np.sum(q1 - q0))
+
     with ClockSampler(local) as clk:
         barrier()
         for _ in range(args.steps):
@@ -413,6 +440,7 @@ def run_gpu(args):
             # iteration, 2 n^3 per completed evaluation (all launches of the step)
             dit = (b.iterations() - isum0).astype(np.float64)
             nev = (st_after_steps - st_before_steps).astype(np.float64)
+            dev_done += float(nev.sum())
             n3 = nao.astype(np.float64) ** 3
             scc_flops_sum += float(np.sum(dit * 11.0 * n3 + nev * 2.0 * n3))
             scc_iters_all.append(it[(nev > 0) & ((st & qg.STATUS_SCC_PENDING) == 0)])
@@ -429,36 +457,14 @@ def run_gpu(args):
                 phase["scc_sum"].append(tm["scc_sum"])
                 phase["integrals_sum"].append(float(np.sum(mk[:, 1] - mk[:, 0])))
                 phase["gradient_sum"].append(float(np.sum(mk[:, 3] - mk[:, 2])))
+            es, ed = e2e_step()
+            e2e_s += es
+            e2e_done += ed
         barrier()
     act_end, steps1 = b.progress()
-    done = float(np.sum(steps1 - steps0))
-    total_ms, done_all = reduce_over_ranks(total_ms, done, world, "cuda")
+    total_ms, done_all = reduce_over_ranks(total_ms, dev_done, world, "cuda")
     value = done_all / (total_ms * 1e-3)
     iters_cat = np.concatenate(scc_iters_all) if scc_iters_all else np.zeros(1)
-
-    # ---- end to end through the public API with pinned host buffers ----
-    # every step: coordinates and velocities in (qcx_batch_load_state: running
-    # trajectories continue, stopped ones stay stopped), one step, coordinates,
-    # velocities and energies out
-    b.set_timing(False)
-    r = b.get()
-    hx = torch.from_numpy(r["xyz"]).pin_memory()
-    hv = torch.from_numpy(r["vel"]).pin_memory()
-    he = torch.zeros(b.nmol, dtype=torch.float64).pin_memory()
-    e2e_steps = max(3, min(args.steps, 10))
-    one_step()  # capture the graph without timing marks outside the timed region
-    b.sync()
-    _, s0 = b.progress()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        b.load_state_ptr(hx.data_ptr(), hv.data_ptr())
-        one_step()
-        b.get_ptr(hx.data_ptr(), hv.data_ptr(), he.data_ptr())
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    _, s1 = b.progress()
-    e2e_done = float(np.sum(s1 - s0))
     e2e_s, e2e_done = reduce_over_ranks(e2e_s, e2e_done, world, "cuda")
     e2e = e2e_done / e2e_s
     h2d = 2 * 3 * 8 * b.natom
