@@ -381,8 +381,9 @@ def run_gpu(args):
     tune = None
     if paced and not args.no_autotune:
         # untimed: pick the per-step SCC budget on this batch (real MD steps)
-        best, rates = b.autotune_budget(AUTOTUNE_BUDGETS, calls=2, tstep=dt, steps_per_call=kstep)
-        tune = {"candidates": {str(k): round(v, 1) for k, v in rates.items()}, "chosen": best}
+        (best, per_group), rates = b.autotune_budget(AUTOTUNE_BUDGETS, calls=2, tstep=dt, steps_per_call=kstep)
+        tune = {"candidates": {"%d/%s" % (k, "group" if g else "batch"): round(v, 1) for (k, g), v in rates.items()},
+                "chosen": best, "scale": "largest molecule of each group" if per_group else "largest molecule of the batch"}
     for _ in range(args.warmup):
         one_step()
     barrier()

@@ -145,13 +145,21 @@ int qcx_batch_set_scc_budget(qcx_batch* b, int iters);
  * (the first call gives every group nsteps). Both return 0 or -1. */
 int qcx_batch_step_groups(qcx_batch* b, const int32_t* nsteps, double tstep);
 int qcx_batch_step_paced(qcx_batch* b, int nsteps, double tstep);
+/* Scale of the SCC budget in grouped and paced steps: per_group = 1 (the
+ * default) scales it with the largest molecule of each molecule's group, 0
+ * with the batch's largest. Returns 0 or -1. qcx_batch_get_scc_budget returns
+ * the current budget and scale (either pointer may be NULL). */
+int qcx_batch_set_scc_budget_scale(qcx_batch* b, int per_group);
+int qcx_batch_get_scc_budget(qcx_batch* b, int32_t* iters, int32_t* per_group);
 /* Autotuner of the per-step SCC budget for paced stepping: for every candidate
- * budget cand[c] (0: none) one untimed paced call and then `calls` timed ones
- * of qcx_batch_step_paced(b, steps_per_call, tstep) on the batch's own
- * trajectories (real MD steps: the run continues), rates[c] (may be NULL) =
- * completed trajectory-steps per second; the batch keeps the fastest budget,
- * which the call returns (or -1). qcx_batch_autotune_budget is the same with
- * steps_per_call = 1. */
+ * budget cand[c] (0: none) and both budget scales, one untimed paced call and
+ * then `calls` timed ones of qcx_batch_step_paced(b, steps_per_call, tstep) on
+ * the batch's own trajectories (real MD steps: the run continues); rates (may
+ * be NULL, 2 ncand entries) = completed trajectory-steps per second, rates[c]
+ * with the per-group scale and rates[ncand + c] with the batch-wide one. The
+ * batch keeps the fastest budget and scale; the call returns the budget (or
+ * -1), qcx_batch_get_scc_budget the scale. qcx_batch_autotune_budget is the
+ * same with steps_per_call = 1. */
 int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, const int32_t* cand, int ncand,
                              int calls, double* rates);
 int qcx_batch_autotune_budget(qcx_batch* b, double tstep, const int32_t* cand, int ncand, int calls,

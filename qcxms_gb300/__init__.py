@@ -127,6 +127,8 @@ def load_library(build_if_missing=True):
     lib.qcx_batch_step_paced.argtypes = [ctypes.c_void_p, c_int, c_double]
     lib.qcx_batch_autotune_budget.argtypes = [ctypes.c_void_p, c_double, P(ctypes.c_int32), c_int, c_int,
                                               P(c_double)]
+    lib.qcx_batch_set_scc_budget_scale.argtypes = [ctypes.c_void_p, c_int]
+    lib.qcx_batch_get_scc_budget.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32)]
     lib.qcx_batch_autotune_paced.argtypes = [ctypes.c_void_p, c_double, c_int, P(ctypes.c_int32), c_int, c_int,
                                              P(c_double)]
     lib.qcx_batch_group_info.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32), P(c_double)]
@@ -457,16 +459,28 @@ class Batch:
         self._check(self._lib.qcx_batch_step_paced(self._h, int(nsteps), float(tstep)), "step_paced")
 
     def autotune_budget(self, candidates=(0, 10, 20, 40), calls=3, tstep=0.5 * constants.FSTOAU, steps_per_call=1):
-        """Pick the per-step SCC budget with the highest completed-step rate of
-        paced calls of ``steps_per_call`` steps on this batch (the measured steps
-        are real MD steps). Returns (chosen budget, {budget: trajectory-steps/s})."""
+        """Pick the per-step SCC budget and its scale (each group's largest
+        molecule or the batch's) with the highest completed-step rate of paced
+        calls of ``steps_per_call`` steps on this batch (the measured steps are
+        real MD steps). Returns ((chosen budget, per_group), {(budget, per_group):
+        trajectory-steps/s})."""
         c = np.ascontiguousarray(candidates, dtype=np.int32)
-        rates = np.zeros(len(c))
+        rates = np.zeros(2 * len(c))
         best = self._lib.qcx_batch_autotune_paced(self._h, float(tstep), int(steps_per_call), _ip(c), len(c),
                                                   int(calls), _dp(rates))
         if best < 0:
             raise RuntimeError("autotune_budget failed: " + _err(self._lib))
-        return int(best), {int(k): float(v) for k, v in zip(c, rates)}
+        it = ctypes.c_int32(); pg = ctypes.c_int32()
+        self._check(self._lib.qcx_batch_get_scc_budget(self._h, ctypes.byref(it), ctypes.byref(pg)), "get_scc_budget")
+        out = {}
+        for k, v in enumerate(rates):
+            out[(int(c[k % len(c)]), 1 if k < len(c) else 0)] = float(v)
+        return (int(best), int(pg.value)), out
+
+    def set_scc_budget_scale(self, per_group=True):
+        """Scale of the SCC budget in grouped and paced steps: each group's
+        largest molecule (True) or the batch's largest."""
+        self._check(self._lib.qcx_batch_set_scc_budget_scale(self._h, int(bool(per_group))), "set_scc_budget_scale")
 
     def group_info(self):
         """(group of every molecule, step counts of the last grouped call, measured ms per step)."""

@@ -157,6 +157,9 @@ struct qcx_batch {
   std::vector<int> g_start, g_count;      // range of each group in the size order
   std::vector<int> g_smem;                // SCC shared memory of each group (its largest molecule's)
   std::vector<int> g_max_nao;             // AOs of each group's largest molecule
+  // grouped steps: the SCC budget scales with each group's largest molecule
+  // (else with the batch's largest)
+  bool budget_per_group = true;
   std::vector<int> g_pair_start;          // first pair of each group in d_gpairs
   std::vector<std::array<int, 10>> g_pair_off;  // class offsets inside the group
   ShellPair* d_gpairs = nullptr;          // shell pairs ordered by group, then class
@@ -186,13 +189,15 @@ DevBatch group_dev(const qcx_batch* b, int g) {
   // molecules leave room for more CTAs per SM
   d.smem_bytes = b->g_smem[g];
   // the per-step SCC budget of a group's step scales with the group's own
-  // largest molecule: every group's step is then bounded by about the same
-  // number of iterations of its largest molecule, and an outlier among small
-  // molecules (an SCC that needs several times the usual count) waits for the
-  // next step instead of holding its group back. Measured on the 256-trajectory
-  // workload (paced, budget 20): 5685 trajectory-steps/s against 3512 with the
-  // batch's largest molecule as the scale.
-  d.budget_nao = b->g_max_nao[g];
+  // largest molecule (by default): every group's step is then bounded by about
+  // the same number of iterations of its largest molecule, and an outlier among
+  // small molecules (an SCC that needs several times the usual count) waits for
+  // the next step instead of holding its group back. Measured on the
+  // 256-trajectory workload (paced, budget 20): 5685 trajectory-steps/s against
+  // 3512 with the batch's largest molecule as the scale; on the collision
+  // workload (4096 ions of 18-281 AOs, groups of 512) the batch-wide scale was
+  // faster (budget 10: 817 against 595), which the autotuner finds.
+  if (b->budget_per_group) d.budget_nao = b->g_max_nao[g];
   return d;
 }
 
@@ -1079,7 +1084,8 @@ int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, con
       return -1;
     }
   // Completed trajectory-steps per second of paced steps under every candidate
-  // budget, measured on the batch's own trajectories (the steps are real MD
+  // budget and both budget scales (each group's largest molecule, the batch's
+  // largest), measured on the batch's own trajectories (the steps are real MD
   // steps: every candidate continues the run where the previous one left it).
   // One untimed call per candidate lets the pacing settle to it.
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1089,8 +1095,9 @@ int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, con
   int best = -1;
   double best_rate = -1.0;
   int rc = 0;
-  for (int c = 0; c < ncand && rc == 0; ++c) {
-    rc = qcx_batch_set_scc_budget(b, cand[c]);
+  for (int c = 0; c < 2 * ncand && rc == 0; ++c) {
+    rc = qcx_batch_set_scc_budget(b, cand[c % ncand]);
+    if (!rc) rc = qcx_batch_set_scc_budget_scale(b, c < ncand ? 1 : 0);
     if (!rc) rc = qcx_batch_step_paced(b, steps_per_call, tstep);
     if (!rc && cudaMemcpyAsync(s0.data(), b->d_steps, sizeof(long long) * b->nmol, cudaMemcpyDeviceToHost,
                                b->stream) != cudaSuccess) rc = -1;
@@ -1118,8 +1125,9 @@ int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, con
     set_error("qcx_batch_autotune_paced: a timed step failed");
     return -1;
   }
-  if (qcx_batch_set_scc_budget(b, cand[best])) return -1;
-  return cand[best];
+  if (qcx_batch_set_scc_budget(b, cand[best % ncand]) || qcx_batch_set_scc_budget_scale(b, best < ncand ? 1 : 0))
+    return -1;
+  return cand[best % ncand];
 }
 
 int qcx_batch_group_info(qcx_batch* b, int32_t* group_of_mol, int32_t* nsteps_last, double* ms_per_step) {
@@ -1345,6 +1353,23 @@ int qcx_batch_set_scc_budget(qcx_batch* b, int iters) {
   if (iters != b->dev.scc_budget) drop_graph(b);
   b->dev.scc_budget = iters;
   b->dev.budget_nao = b->max_nao;
+  return 0;
+}
+
+int qcx_batch_set_scc_budget_scale(qcx_batch* b, int per_group) {
+  if (!b || (per_group != 0 && per_group != 1)) {
+    set_error("qcx_batch_set_scc_budget_scale: per_group must be 0 or 1");
+    return -1;
+  }
+  if ((per_group != 0) != b->budget_per_group) drop_graph(b);
+  b->budget_per_group = per_group != 0;
+  return 0;
+}
+
+int qcx_batch_get_scc_budget(qcx_batch* b, int32_t* iters, int32_t* per_group) {
+  if (!b) return -1;
+  if (iters) *iters = b->dev.scc_budget;
+  if (per_group) *per_group = b->budget_per_group ? 1 : 0;
   return 0;
 }
 

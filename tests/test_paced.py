@@ -123,9 +123,12 @@ def test_budget_autotuner(gpu):
     b = qg.Batch(mols)
     b.egrad()
     _, s0 = b.progress()
-    best, rates = b.autotune_budget((0, 8, 30), calls=2, tstep=DT)
-    assert best in (0, 8, 30) and set(rates) == {0, 8, 30}
-    assert all(v > 0 for v in rates.values()) and rates[best] == max(rates.values())
+    (best, per_group), rates = b.autotune_budget((0, 8, 30), calls=2, tstep=DT)
+    # every candidate with both budget scales (each group's largest molecule,
+    # the batch's largest)
+    assert best in (0, 8, 30) and per_group in (0, 1)
+    assert set(rates) == {(k, g) for k in (0, 8, 30) for g in (0, 1)}
+    assert all(v > 0 for v in rates.values()) and rates[(best, per_group)] == max(rates.values())
     _, s1 = b.progress()
     assert np.sum(s1 - s0) > 0  # the measured steps advanced the trajectories
     b.step_paced(1, DT)
