@@ -23,10 +23,16 @@ namespace qcx {
 // warm FP32 Jacobi sweeps (at most) when the first-order refinement cannot
 // update the eigenvectors: a single sweep left errors of order 1e-2 in the
 // density of molecules with near-degenerate orbitals at the Fermi level, which
-// stalled the FP32 phase (measured: 43 iterations per evaluation with one
-// sweep, 38 with two or three, and fewer stopped trajectories)
+// stalled the FP32 phase (measured on 5-40-atom cations: 43 iterations per
+// evaluation with one sweep, 38 with two or three, and fewer stopped
+// trajectories). A sweep costs ~n^2 cycles, so molecules above
+// QCX_JAC32_WARM2_MAX_NAO AOs take one (collision workload, 18-281 AOs: 907
+// trajectory-steps/s with one sweep for every molecule against 818 with two)
 #ifndef QCX_JAC32_WARM_SWEEPS
 #define QCX_JAC32_WARM_SWEEPS 2
+#endif
+#ifndef QCX_JAC32_WARM2_MAX_NAO
+#define QCX_JAC32_WARM2_MAX_NAO 128
 #endif
 #ifndef QCX_JAC32_COLD_TOL
 #define QCX_JAC32_COLD_TOL 2e-6
@@ -2112,8 +2118,9 @@ __global__ void __launch_bounds__(kSccThreads, QCX_SCC_MINBLOCKS) k_scc(DevBatch
       // the first (cold) solve only seeds the FP32 iterations: it stops at a
       // looser tolerance, the warm sweeps and refinements of later iterations
       // take the basis further
-      if (!ok32) jacobi<float>(JA32, JV32, n, have32 || seeded, have32 ? 2e-6 : QCX_JAC32_COLD_TOL, sh,
-                               have32 ? QCX_JAC32_WARM_SWEEPS : 30);
+      if (!ok32)
+        jacobi<float>(JA32, JV32, n, have32 || seeded, have32 ? 2e-6 : QCX_JAC32_COLD_TOL, sh,
+                      have32 ? (n <= QCX_JAC32_WARM2_MAX_NAO ? QCX_JAC32_WARM_SWEEPS : 1) : 30);
 #ifdef QCX_SCC_PHASE_TIMING
       if (threadIdx.x == 0) atomicAdd(&g_phase_cycles[ok32 ? 13 : 14], 1ull);
 #endif
