@@ -214,3 +214,21 @@ def test_getspin_gnorm_checkqc(oracle_lib):
     assert not ok and e == 0.0
     ok, e = oracle_lib.checkqc(-10.0, np.array([[0.1, 0.0, 0.0]]), np.array([1e-6]), 1)
     assert not ok and e == 0.0
+
+
+def test_scc_mixer_restart_gets_sloshing_molecules_out(oracle_lib):
+    # MD snapshots of hot cations of the 256-trajectory workload whose SCC slosh
+    # between near-degenerate states. Without the restart of the Broyden history
+    # after 12 stagnating iterations, molecule 215 after 20 steps stops at the
+    # limit of 250 (checked with a build without the restart); with it both
+    # converge.
+    kT = 300.0 * constants.KB_AU
+    dt = 0.5 * constants.FSTOAU
+    mols = molgen.batch_workload(256, 5, 40)
+    for i, ns in ((215, 20), (210, 27)):
+        m = mols[i]
+        rc, e, g, q = oracle_lib.egrad_batch([m], kT, nthreads=1)
+        fails, xyz, vel, grad, ep, its = oracle_lib.md_batch([m], ns, dt, g, kT, nthreads=1)
+        assert fails == 0
+        r, e, g, q, info = oracle_lib.egrad(m["Z"], xyz, 1, kT=kT)
+        assert r == 0 and info["converged"] == 1 and info["iterations"] < 200, (i, info["iterations"])
