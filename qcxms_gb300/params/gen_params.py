@@ -199,9 +199,9 @@ def _self_energy_rule(z, l):
     return {0: -0.30 - 0.09 * nv, 1: -0.16 - 0.045 * nv, 2: -0.08}[l]
 
 
-def main():
+def main(out=None):
     here = os.path.dirname(os.path.abspath(__file__))
-    out = os.path.join(here, "..", "csrc", "qcx_params.h")
+    out = out or os.path.join(here, "..", "csrc", "qcx_params.h")
     fits = {}
     for (n, l) in [(1, 0), (2, 0), (2, 1), (3, 0), (3, 1), (3, 2)]:
         np_ = NPRIM if l < 2 else 4
