@@ -399,7 +399,6 @@ def run_gpu(args):
     for _ in range(args.warmup):
         one_step()
     barrier()
-    _, steps0 = b.progress()
     total_ms = 0.0
     launches = 0
     scc_flops_sum = scc_ms_sum = 0.0
