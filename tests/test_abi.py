@@ -53,6 +53,14 @@ def test_batch_entry_points_reject_null_handles_without_gpu():
     assert lib.qcx_batch_set_cid_rules(None, 300.0, 100) == -1
     assert lib.qcx_batch_get_cid_state(None, *([None] * 9)) == -1
     assert lib.qcx_boltz(2, 0, 1, 300.0, None, None) == -1
+    # SCC budget scale, its getter and the paced autotuner
+    assert lib.qcx_batch_set_scc_budget_scale(None, 1) == -1
+    assert lib.qcx_batch_get_scc_budget(None, None, None) == -1
+    assert lib.qcx_batch_autotune_paced(None, 20.0, 1, None, 1, 1, None) == -1
+    # the FP32 eigensolver self-check validates its arguments before any CUDA call
+    assert lib.qcx_jacobi32_selftest(0, None, None, None, 0, 2e-6, 30, None) == -1
+    assert lib.qcx_jacobi32_selftest(300, None, None, None, 0, 2e-6, 30, None) == -1
+    assert b"n <= 256" in lib.qcx_last_error()
 
 
 def test_header_is_plain_c_and_links(tmp_path):
