@@ -25,21 +25,66 @@ fragments. Their charges come from the Boltzmann weights of the fragment IPs
 the reference's own assignment (``src/write_fragments.f90:116-121``) reads
 ``fragip(i,0)``, outside its array, so its numbers are not reproducible.
 
+Several GPUs of one node (``torchrun --nproc-per-node N -m qcxms_gb300.driver
+...``): the trajectories are independent, as ``bin/pqcxms``'s processes are, so
+each rank runs its own shard of the ensemble (``shard_ensemble``) on its own GPU
+with no exchange on the data path; the ranks' result records are merged at the
+end (``gather_results``), the one collective.
+
 Usage: ``python -m qcxms_gb300.driver TMPQCXMS --max-steps 10000 --res qcxms.res``
 """
 import argparse
 import json
+import os
 
 import numpy as np
 
-from . import Batch, boltz, constants, format_res, fragment_formula, fragment_ips, read_ensemble
+from . import Batch, basis, boltz, constants, format_res, fragment_formula, fragment_ips, read_ensemble
+
+
+def shard_ensemble(mols, world):
+    """Split the trajectories of an ensemble over ``world`` ranks with balanced
+    work. An evaluation's cost is dominated by the SCC's eigen work, O(nao^3)
+    per iteration with one CTA per molecule, so each trajectory is weighted by
+    nao^3 and the trajectories are dealt largest first to the rank with the least
+    weight so far (greedy longest-processing-time partition: the heaviest rank
+    carries at most 4/3 of the best possible split's maximum, and at most the
+    mean plus one trajectory's weight). Ties go to the lower rank and the lower
+    index, so every rank computes the same split. Returns one ascending index
+    list per rank; every index appears in exactly one."""
+    if world < 1:
+        raise ValueError("world must be at least 1")
+    cost = [float(basis.nao_of(m["Z"])) ** 3 for m in mols]
+    load = [0.0] * world
+    out = [[] for _ in range(world)]
+    for i in sorted(range(len(mols)), key=lambda i: (-cost[i], i)):
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(i)
+        load[r] += cost[i]
+    return [sorted(s) for s in out]
+
+
+def gather_results(res, world):
+    """The result records of every rank merged in trajectory order (``itrj``):
+    the only exchange between the ranks of a sharded run (gloo, host objects)."""
+    if world == 1:
+        return res
+    import torch.distributed as dist
+    parts = [None] * world
+    dist.all_gather_object(parts, res)
+    return sorted((t for p in parts for t in p), key=lambda t: t["itrj"])
 
 
 def run_ensemble(root, etemp=-1.0, charge=1, nfragexit=2, more=250, max_steps=10000, tstep_fs=0.5, block=100,
-                 precision="mixed", ip_precision=0, ip_etemp=300.0, ax=0.0, ieetemp=0.0):
-    """Run every trajectory of ``root`` to its end; returns one dict per trajectory.
+                 precision="mixed", ip_precision=0, ip_etemp=300.0, ax=0.0, ieetemp=0.0, rank=0, world=1):
+    """Run every trajectory of ``root`` to its end (with world > 1: this rank's
+    shard of them); returns one dict per trajectory.
     etemp > 0: the start's electronic temperature; otherwise setetemp's."""
     mols = read_ensemble(root, charge=charge)
+    if world > 1:
+        mols = [mols[i] for i in shard_ensemble(mols, world)[rank]]
+        if not mols:
+            return []
     dt = tstep_fs * constants.FSTOAU
     b = Batch(mols, etemp=etemp if etemp > 0 else 5000.0)
     b.set_precision(precision)
@@ -141,8 +186,20 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--out", default=None, help="write the results as JSON here")
     a = ap.parse_args()
+    rank, world = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("gloo")  # host records only; nothing on the data path
     res = run_ensemble(a.root, a.etemp, a.charge, a.nfragexit, max_steps=a.max_steps, precision=a.precision,
-                       ax=a.ax, ieetemp=a.ieetemp)
+                       ax=a.ax, ieetemp=a.ieetemp, rank=rank, world=world)
+    res = gather_results(res, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+        if rank != 0:
+            return
     if a.res:
         with open(a.res, "w") as f:
             for t in res:

@@ -1,6 +1,9 @@
 """Multi-rank host logic on CPU (gloo, world size 2): the shards of the batch
 workload are disjoint and the timing reduction takes the slowest rank's time
-and the sum of the trajectory-steps of all ranks (the only collective)."""
+and the sum of the trajectory-steps of all ranks (the only collective); the
+production driver splits an ensemble over ranks by nao^3 (every trajectory in
+one shard, the heaviest rank within one trajectory of the mean) and merges the
+ranks' result records in trajectory order."""
 import os
 import socket
 
@@ -47,3 +50,57 @@ def test_rank_shards_are_disjoint():
     a, b = bench.workload(0, 8), bench.workload(1, 8)
     key = lambda m: (tuple(m["Z"]), round(float(np.asarray(m["xyz"]).sum()), 6))
     assert not set(map(key, a)) & set(map(key, b))
+
+
+def _gather_worker(rank, world, port, out):
+    import sys
+    sys.path.insert(0, ROOT)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from qcxms_gb300 import driver
+    # each rank holds the records of its own shard, in its own order
+    mine = [{"itrj": t, "rank": rank} for t in (range(5, 0, -2) if rank == 0 else (6, 2, 4))]
+    out[rank] = driver.gather_results(mine, world)
+    dist.destroy_process_group()
+
+
+def test_sharded_ensemble_records_merge_over_two_gloo_ranks():
+    world, port = 2, _free_port()
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_gather_worker, args=(world, port, out), nprocs=world, join=True)
+    for r in range(world):
+        assert [t["itrj"] for t in out[r]] == [1, 2, 3, 4, 5, 6]
+        assert [t["rank"] for t in out[r]] == [0, 1, 0, 1, 0, 1]
+
+
+@pytest.mark.parametrize("world", [1, 2, 3, 8])
+def test_ensemble_shards_partition_and_balance(world):
+    from qcxms_gb300 import basis, driver, molgen
+    mols = molgen.batch_workload(256, 5, 40)
+    shards = driver.shard_ensemble(mols, world)
+    assert len(shards) == world
+    flat = sorted(i for s in shards for i in s)
+    assert flat == list(range(len(mols)))
+    assert all(s == sorted(s) for s in shards)
+    assert driver.shard_ensemble(mols, world) == shards  # every rank computes the same split
+    cost = np.array([float(basis.nao_of(m["Z"])) ** 3 for m in mols])
+    load = np.array([cost[s].sum() for s in shards])
+    # greedy bound: the heaviest rank carries at most the mean plus one trajectory
+    assert load.max() <= cost.sum() / world + cost.max() + 1e-6
+    if world > 1:
+        # and far better than consecutive blocks of the ensemble
+        blocks = np.array_split(np.arange(len(mols)), world)
+        assert load.max() <= max(cost[b].sum() for b in blocks)
+        assert load.max() / load.mean() < 1.02
+
+
+def test_more_ranks_than_trajectories():
+    from qcxms_gb300 import driver, molgen
+    mols = molgen.batch_workload(3, 5, 10)
+    shards = driver.shard_ensemble(mols, 5)
+    assert sorted(i for s in shards for i in s) == [0, 1, 2]
+    assert sum(1 for s in shards if not s) == 2
+    with pytest.raises(ValueError):
+        driver.shard_ensemble(mols, 0)
