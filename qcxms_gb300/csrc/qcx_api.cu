@@ -86,6 +86,27 @@ int dalloc(T** p, size_t n) {
   return 0;
 }
 
+// Timing events of one call, destroyed on every return path.
+struct CallEvents {
+  std::vector<cudaEvent_t> ev;
+  explicit CallEvents(size_t n) : ev(n, nullptr) {}
+  ~CallEvents() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  cudaError_t create() {
+    for (cudaEvent_t& e : ev) {
+      const cudaError_t r = cudaEventCreate(&e);
+      if (r != cudaSuccess) {
+        e = nullptr;
+        return r;
+      }
+    }
+    return cudaSuccess;
+  }
+  cudaEvent_t operator[](size_t i) const { return ev[i]; }
+};
+
 }  // namespace
 
 struct qcx_batch {
@@ -1088,9 +1109,9 @@ int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, con
   // largest), measured on the batch's own trajectories (the steps are real MD
   // steps: every candidate continues the run where the previous one left it).
   // One untimed call per candidate lets the pacing settle to it.
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  CallEvents ev(2);
+  CK(ev.create());
+  const cudaEvent_t e0 = ev[0], e1 = ev[1];
   std::vector<long long> s0(b->nmol), s1(b->nmol);
   int best = -1;
   double best_rate = -1.0;
@@ -1119,8 +1140,6 @@ int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, con
       best = c;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (rc) {
     set_error("qcx_batch_autotune_paced: a timed step failed");
     return -1;
@@ -1209,8 +1228,8 @@ void* qcx_batch_stream(qcx_batch* b) { return b ? (void*)b->stream : nullptr; }
 
 int qcx_batch_profile_egrad(qcx_batch* b, float* ms) {
   if (!b || !ms) return -1;
-  cudaEvent_t ev[kEgradPhases + 1];
-  for (auto& e : ev) CK(cudaEventCreate(&e));
+  CallEvents ev(kEgradPhases + 1);
+  CK(ev.create());
   const DevBatch& d = b->dev;
   CK(cudaEventRecord(ev[0], b->stream));
   launch_cn(d, b->stream);
@@ -1227,7 +1246,6 @@ int qcx_batch_profile_egrad(qcx_batch* b, float* ms) {
   CK(cudaEventRecord(ev[6], b->stream));
   CK(cudaEventSynchronize(ev[6]));
   for (int i = 0; i < kEgradPhases; ++i) CK(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
-  for (auto& e : ev) cudaEventDestroy(e);
   b->launches = nl;
   return check_launch();
 }
@@ -1238,8 +1256,9 @@ int qcx_batch_set_timing(qcx_batch* b, int on) {
     return -1;
   }
   if (on && b->t_ev.empty()) {
-    b->t_ev.assign(2 + 4 * (size_t)b->ngroup, nullptr);
-    for (auto& e : b->t_ev) CK(cudaEventCreate(&e));
+    CallEvents ev(2 + 4 * (size_t)b->ngroup);
+    CK(ev.create());
+    b->t_ev.swap(ev.ev);  // the batch owns them from here (destroyed with it)
   }
   if ((on != 0) != b->timing) drop_graph(b);
   b->timing = on != 0;
