@@ -627,12 +627,9 @@ int qcx_batch_set_scc(qcx_batch* b, int max_iter, double econv, double pconv, do
   b->dev.econv = econv;
   b->dev.pconv = pconv;
   b->dev.mix_alpha = mixing;
-  if (b->graph_exec) {
-    cudaGraphExecDestroy(b->graph_exec);
-    cudaGraphDestroy(b->graph);
-    b->graph_exec = nullptr;
-    b->graph = nullptr;
-  }
+  // the step graphs hold the SCC settings as kernel arguments: the whole-batch
+  // graph and the molecule groups' graphs are captured again
+  drop_graph(b);
   return 0;
 }
 
@@ -1026,7 +1023,10 @@ int qcx_batch_step_groups(qcx_batch* b, const int32_t* nsteps, double tstep) {
     }
     for (int g = 0; g < G; ++g) {
       const int n = capture_group(b, g, tstep);
-      if (n < 0) return -1;
+      if (n < 0) {
+        drop_graph(b);  // no partial set of group graphs survives a failed capture
+        return -1;
+      }
       b->gg_kernels[g] = n;
     }
     b->gg_tstep = tstep;

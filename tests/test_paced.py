@@ -133,3 +133,21 @@ def test_budget_autotuner(gpu):
     assert np.sum(s1 - s0) > 0  # the measured steps advanced the trajectories
     b.step_paced(1, DT)
     b.close()
+
+
+def test_group_graphs_take_new_scc_settings(gpu):
+    # the group graphs hold the SCC settings as kernel arguments: after
+    # set_scc they are captured again, so a 2-iteration limit set between two
+    # grouped steps stops every SCC of the second one
+    mols = molgen.batch_workload(16, 6, 24, seed0=300)
+    b = qg.Batch(mols)
+    b.egrad()
+    ones = np.ones(8, dtype=np.int32)
+    b.step_groups(ones, DT)
+    st, _ = b.status_iters()
+    assert np.all(st == 0)
+    b.set_scc(max_iter=2)
+    b.step_groups(ones, DT)
+    st, it = b.status_iters()
+    assert np.all(st != 0) and np.all(it <= 2), (st, it)
+    b.close()
