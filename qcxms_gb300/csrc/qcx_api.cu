@@ -663,7 +663,7 @@ int qcx_batch_set_md_rules(qcx_batch* b, int nfragexit, int more, int max_steps)
                   b->md_etemp ? b->d_etemp0 : nullptr, b->stream);
   if (check_launch()) return -1;
   CK(cudaStreamSynchronize(b->stream));
-  if (!b->md_on || b->cid_on) drop_graph(b);
+  drop_graph(b);  // the rules are kernel arguments of the captured step graphs
   b->md_on = true;
   b->cid_on = false;
   return 0;
@@ -778,6 +778,7 @@ int qcx_batch_set_md_heating(qcx_batch* b, const double* eimp, const double* tad
   if (!b->d_velof && dalloc(&b->d_velof, (size_t)b->natom)) return -1;
   CK(cudaMemcpy(b->d_md_heat, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b->d_velof, vf.data(), sizeof(double) * vf.size(), cudaMemcpyHostToDevice));
+  if (!b->md_heat) drop_graph(b);  // the graphs pass the heating factors only when it is on
   b->md_heat = true;
   b->h_eimp.assign(eimp, eimp + b->nmol);
   return 0;

@@ -153,6 +153,27 @@ def test_gpu_md_rules_match_oracle(gpu, oracle_lib):
     assert not active.any()
 
 
+@pytest.mark.gpu
+def test_new_md_rules_reach_the_captured_step_graphs(gpu):
+    # the loop rules are kernel arguments of the step graphs: rules set again
+    # after a step (a new step limit) apply from the next step, in whole-batch
+    # and in grouped stepping
+    mols = molgen.batch_workload(8, 6, 12, seed0=500)
+    for grouped in (False, True):
+        b = qg.Batch(mols)
+        b.egrad()
+        b.set_md_rules(2, 250, 100000)
+        ngroup = len(b.group_info()[1])
+        step = (lambda: b.step_groups(np.ones(ngroup, dtype=np.int32), DT)) if grouped else (lambda: b.step(1, DT))
+        step()
+        b.set_md_rules(2, 250, 3)
+        for _ in range(5):
+            step()
+        st = b.md_state()
+        assert st["done"].all() and (st["nstep"] <= 3).all(), (grouped, st["nstep"], st["done"])
+        b.close()
+
+
 def test_oracle_impactscale(oracle_lib):
     o = oracle_lib
     mass = [1837.0, 21874.0, 29166.0]
