@@ -51,7 +51,9 @@ const char* qcx_last_error(void);
  * (src/iniqm.f90:641-655) on every MD step. The multiplicity is accepted but,
  * as in the reference (uhf = min(multiplicity-1, 0), src/tblite.f90:111),
  * the calculation is spin-restricted with Fermi smearing at etemp.
- * The device state for a given atom list is cached between calls.
+ * The device state for a given atom list, charge and etemp is cached between
+ * calls, one per GPU (the calling thread's current device); calls are
+ * serialised by a lock.
  * Writes energy (Eh), grad [nat][3] (Eh/Bohr) and qat [nat] (Mulliken charges).
  * The result then goes through checkqc as egrad does after the call
  * (src/iniqm.f90:650, 684-715): a rejected result returns -1, with the energy

@@ -1319,10 +1319,15 @@ int qcx_checkqc(int nat, const double* grad, const double* qat, int charge, doub
 // ---------------------------------------------------------------------------
 int qcx_egrad(int method, int nat, const int32_t* num, const double* xyz, int charge, int multiplicity,
               double etemp, double* energy, double* grad, double* qat) {
+  // one cached device state per GPU (the calling thread's current device)
+  struct Cache {
+    qcx_batch* b = nullptr;
+    std::vector<int> num;
+    double charge = 0.0, etemp = -1.0;
+  };
+  constexpr int kMaxDevices = 64;
   static std::mutex mtx;
-  static qcx_batch* cached = nullptr;
-  static std::vector<int> cached_num;
-  static double cached_charge = 0.0, cached_etemp = -1.0;
+  static Cache caches[kMaxDevices];
   (void)multiplicity;
   if (method != QCX_METHOD_GFN2) {
     set_error("only the GFN2-xTB Hamiltonian is implemented");
@@ -1332,18 +1337,26 @@ int qcx_egrad(int method, int nat, const int32_t* num, const double* xyz, int ch
     set_error("qcx_egrad: invalid arguments");
     return -1;
   }
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("qcx_egrad: device index out of range");
+    return -1;
+  }
   std::lock_guard<std::mutex> lock(mtx);
+  Cache& c = caches[dev];
   std::vector<int> key(num, num + nat);
-  if (!cached || key != cached_num || cached_charge != (double)charge || cached_etemp != etemp) {
-    if (cached) free_batch(cached);
+  if (!c.b || key != c.num || c.charge != (double)charge || c.etemp != etemp) {
+    if (c.b) free_batch(c.b);
     int32_t n1 = nat;
     double ch = charge, et = etemp;
-    cached = qcx_batch_create(1, &n1, num, &ch, &et);
-    if (!cached) return -1;
-    cached_num = key;
-    cached_charge = charge;
-    cached_etemp = etemp;
+    c.b = qcx_batch_create(1, &n1, num, &ch, &et);
+    if (!c.b) return -1;
+    c.num = key;
+    c.charge = charge;
+    c.etemp = etemp;
   }
+  qcx_batch* cached = c.b;
   if (qcx_batch_set_state(cached, xyz, nullptr, nullptr)) return -1;
   if (qcx_batch_egrad(cached)) return -1;
   int32_t st = 0;
