@@ -156,9 +156,12 @@ int qcx_batch_get_scc_budget(qcx_batch* b, int32_t* iters, int32_t* per_group);
 /* Autotuner of the per-step SCC budget for paced stepping: for every candidate
  * budget cand[c] (0: none) and both budget scales, one untimed paced call and
  * then `calls` timed ones of qcx_batch_step_paced(b, steps_per_call, tstep) on
- * the batch's own trajectories (real MD steps: the run continues); rates (may
- * be NULL, 2 ncand entries) = completed trajectory-steps per second, rates[c]
- * with the per-group scale and rates[ncand + c] with the batch-wide one. The
+ * the batch's own trajectories (real MD steps: the run continues), in two
+ * passes over the configurations, the second in reverse order (the batch's
+ * state drifts over the calls; the reverse pass cancels a linear drift);
+ * rates (may be NULL, 2 ncand entries) = completed trajectory-steps per second
+ * over both passes, rates[c] with the per-group scale and rates[ncand + c]
+ * with the batch-wide one. The
  * batch keeps the fastest budget and scale; the call returns the budget (or
  * -1), qcx_batch_get_scc_budget the scale. qcx_batch_autotune_budget is the
  * same with steps_per_call = 1. */

@@ -462,7 +462,8 @@ class Batch:
         """Pick the per-step SCC budget and its scale (each group's largest
         molecule or the batch's) with the highest completed-step rate of paced
         calls of ``steps_per_call`` steps on this batch (the measured steps are
-        real MD steps). Returns ((chosen budget, per_group), {(budget, per_group):
+        real MD steps; two passes over the configurations, the second in reverse
+        order, against the drift of the batch's state). Returns ((chosen budget, per_group), {(budget, per_group):
         trajectory-steps/s})."""
         c = np.ascontiguousarray(candidates, dtype=np.int32)
         rates = np.zeros(2 * len(c))

@@ -1109,15 +1109,19 @@ int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, con
   // budget and both budget scales (each group's largest molecule, the batch's
   // largest), measured on the batch's own trajectories (the steps are real MD
   // steps: every candidate continues the run where the previous one left it).
-  // One untimed call per candidate lets the pacing settle to it.
+  // One untimed call per candidate lets the pacing settle to it. The batch
+  // ages over the calls (trajectories fragment and stop, small molecules run
+  // ahead), so the configurations are measured twice, the second pass in
+  // reverse order, and each rate is taken over both of its measurements.
   CallEvents ev(2);
   CK(ev.create());
   const cudaEvent_t e0 = ev[0], e1 = ev[1];
   std::vector<long long> s0(b->nmol), s1(b->nmol);
-  int best = -1;
-  double best_rate = -1.0;
+  const int ncfg = 2 * ncand;
+  std::vector<double> done_sum(ncfg, 0.0), ms_sum(ncfg, 0.0);
   int rc = 0;
-  for (int c = 0; c < 2 * ncand && rc == 0; ++c) {
+  for (int q = 0; q < 2 * ncfg && rc == 0; ++q) {
+    const int c = q < ncfg ? q : 2 * ncfg - 1 - q;
     rc = qcx_batch_set_scc_budget(b, cand[c % ncand]);
     if (!rc) rc = qcx_batch_set_scc_budget_scale(b, c < ncand ? 1 : 0);
     if (!rc) rc = qcx_batch_step_paced(b, steps_per_call, tstep);
@@ -1134,7 +1138,13 @@ int qcx_batch_autotune_paced(qcx_batch* b, double tstep, int steps_per_call, con
     if (rc) break;
     long long done = 0;
     for (int m = 0; m < b->nmol; ++m) done += s1[m] - s0[m];
-    const double rate = ms > 0.f ? 1e3 * (double)done / ms : 0.0;
+    done_sum[c] += (double)done;
+    ms_sum[c] += (double)ms;
+  }
+  int best = 0;
+  double best_rate = -1.0;
+  for (int c = 0; c < ncfg && rc == 0; ++c) {
+    const double rate = ms_sum[c] > 0.0 ? 1e3 * done_sum[c] / ms_sum[c] : 0.0;
     if (rates) rates[c] = rate;
     if (rate > best_rate) {
       best_rate = rate;
