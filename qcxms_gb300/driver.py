@@ -190,7 +190,8 @@ def main():
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        if torch.cuda.is_available():  # without one, the first Batch fails with the library's error
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("gloo")  # host records only; nothing on the data path
     res = run_ensemble(a.root, a.etemp, a.charge, a.nfragexit, max_steps=a.max_steps, precision=a.precision,
                        ax=a.ax, ieetemp=a.ieetemp, rank=rank, world=world)

@@ -104,3 +104,33 @@ def test_more_ranks_than_trajectories():
     assert sum(1 for s in shards if not s) == 2
     with pytest.raises(ValueError):
         driver.shard_ensemble(mols, 0)
+
+
+def _driver_main_worker(rank, world, port, out_json, res_path):
+    import sys
+    sys.path.insert(0, ROOT)
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    from qcxms_gb300 import driver
+
+    def fake_run(root, *a, rank=0, world=1, **k):
+        # this rank's shard of a 5-trajectory ensemble: two records of rank 0, three of rank 1
+        mine = [1, 4] if rank == 0 else [0, 2, 3]
+        return [{"itrj": i, "mdok": True, "fragstate": 1, "nstep": 10 * i, "nfrag": 2, "formula": ["H2O1"],
+                 "res_lines": ["line %d" % i]} for i in mine]
+
+    driver.run_ensemble = fake_run
+    sys.argv = ["driver", "ENSEMBLE", "--out", out_json, "--res", res_path]
+    driver.main()
+
+
+def test_driver_main_merges_the_ranks_records(tmp_path):
+    world, port = 2, _free_port()
+    out_json, res_path = str(tmp_path / "res.json"), str(tmp_path / "qcxms.res")
+    mp.spawn(_driver_main_worker, args=(world, port, out_json, res_path), nprocs=world, join=True)
+    import json
+    with open(out_json) as f:
+        recs = json.load(f)
+    assert [r["itrj"] for r in recs] == [0, 1, 2, 3, 4]
+    with open(res_path) as f:
+        assert f.read().split("\n")[:5] == ["line %d" % i for i in range(5)]
