@@ -170,7 +170,10 @@ def test_new_md_rules_reach_the_captured_step_graphs(gpu):
         for _ in range(5):
             step()
         st = b.md_state()
-        assert st["done"].all() and (st["nstep"] <= 3).all(), (grouped, st["nstep"], st["done"])
+        active, _ = b.progress()
+        # every run ended at the new limit at the latest (a failed evaluation
+        # would have stopped its trajectory earlier)
+        assert not active.any() and (st["nstep"] <= 3).all(), (grouped, st["nstep"], active)
         b.close()
 
 
