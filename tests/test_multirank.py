@@ -134,3 +134,30 @@ def test_driver_main_merges_the_ranks_records(tmp_path):
     assert [r["itrj"] for r in recs] == [0, 1, 2, 3, 4]
     with open(res_path) as f:
         assert f.read().split("\n")[:5] == ["line %d" % i for i in range(5)]
+
+
+def test_run_ensemble_takes_its_ranks_shard(monkeypatch):
+    import sys
+    sys.path.insert(0, ROOT)
+    from qcxms_gb300 import driver, molgen
+    mols = molgen.batch_workload(12, 5, 30)
+    for i, m in enumerate(mols):
+        m["itrj"] = i
+    monkeypatch.setattr(driver, "read_ensemble", lambda root, charge=1: [dict(m) for m in mols])
+
+    class Seen(Exception):
+        pass
+
+    def fake_batch(ms, etemp=300.0):
+        raise Seen([m["itrj"] for m in ms])
+
+    monkeypatch.setattr(driver, "Batch", fake_batch)
+    shards = driver.shard_ensemble(mols, 3)
+    for rank in range(3):
+        with pytest.raises(Seen) as e:
+            driver.run_ensemble("ENSEMBLE", rank=rank, world=3)
+        assert e.value.args[0] == shards[rank]
+    # one rank: the whole ensemble in order
+    with pytest.raises(Seen) as e:
+        driver.run_ensemble("ENSEMBLE")
+    assert e.value.args[0] == list(range(12))
